@@ -1,0 +1,354 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 PBF step (particle-steps/s) on the 1M-particle dam break.
+
+A step is one full PBF step (predict, cell sort, neighbour grid, 4 Jacobi
+density iterations with s_corr, velocity update, XSPH, vorticity
+confinement, domain clamp, commit) over the 1,000,000-particle dam break
+(100^3 lattice at r = 0.01 m in a 4x2x2 m box, h = 4r, dt = 1/240 s), all
+inputs synthetic and seeded (novaphy_gb300/workloads.py).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours: `value` is device throughput with the scene resident in HBM (CUDA
+events on the scene's stream around K graph-replayed steps; the per-step
+working set, ~190 MB, exceeds the 129 MB L2).  `e2e` is the same metric
+through the drop-in host-array call pbf_solver_step_host (the C ABI of
+PBFSolver::step): every step uploads x, v, densities, lambdas from pinned
+host memory and reads them back.  Under torchrun each rank runs an
+independent replica on its own GPU (the single-scene path does not shard);
+`value` sums the ranks' particle-steps over the slowest rank's time.
+
+reference: the reference's CPU PBF (its own sources built in oracle/_ref
+where the reference tree is present, else the oracle restatement), single
+threaded as the reference is, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from novaphy_gb300 import workloads  # noqa: E402
+
+METRIC = "particle-steps/sec"
+UNIT = "particle-steps/s"
+# Algorithmic (compulsory) HBM bytes per particle per launch of the two
+# constraint kernels: density+lambda reads x* (12 B) and writes rho, lambda
+# (8 B); delta reads x*, lambda (16 B) and writes x*' (12 B).
+ALG_BYTES = {"fluid.pbf.iteration.compute_density": 20.0,
+             "fluid.pbf.iteration.compute_delta_position": 28.0}
+KERNEL_OF_PHASE = {"fluid.pbf.iteration.compute_density": "k_density_lambda",
+                   "fluid.pbf.iteration.compute_delta_position": "k_delta"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_dam_break_1m.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return None
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [t.strip() for t in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_backend():
+    """The reference build where present, else the restatement: (object, kind)."""
+    from oracle import build_oracle
+    from oracle.oracle import Port, Ref
+
+    try:
+        if build_oracle.build_ref() is not None:
+            return Ref(), "reference"
+    except Exception:
+        pass
+    return Port(), "port"
+
+
+def cpu_sample_workload(counts):
+    w = workloads.scaled_dam_break(counts)
+    return w
+
+
+def time_cpu(counts, nsteps, warmup):
+    from oracle.oracle import Settings
+
+    be, kind = cpu_backend()
+    w = cpu_sample_workload(counts)
+    s = Settings.make(**w.settings)
+    x, v = w.x, w.v
+    rho = np.zeros(w.n, np.float32)
+    lam = np.zeros(w.n, np.float32)
+    if warmup:
+        x, v, rho, lam = be.steps(s, x, v, rho, lam, w.dt, w.gravity, w.mass, warmup)
+    t0 = time.perf_counter()
+    x, v, rho, lam = be.steps(s, x, v, rho, lam, w.dt, w.gravity, w.mass, nsteps)
+    el = time.perf_counter() - t0
+    return w.n * nsteps / el, kind, w.n, el
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    counts = (40, 40, 40)
+    val, kind, n, el = time_cpu(counts, args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "dam_break_1m", "sample": f"{n}-particle block "
+                   f"{counts[0]}x{counts[1]}x{counts[2]} of the 1M case's lattice, box and "
+                   "parameters", "threads": 1},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": kind,
+                         "sample": f"{n} particles x {args.steps} steps, 1 thread (the reference "
+                         "CPU PBF has no threading)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, ws, rank, local):
+    from novaphy_gb300 import capi
+
+    capi.load()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("gloo")
+    device = local
+    w = workloads.dam_break_1m(vorticity=args.vorticity)
+    s = capi.default_settings(**w.settings, exact_arithmetic=0)
+    sc = capi.Scene(s, w.x, w.v, mass=w.mass, device=device)
+    sc.set_gravity(w.gravity)
+
+    # warm-up (also captures the step graph)
+    sc.step(w.dt, max(args.warmup, 1))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    barrier()
+    with ClockSampler(device) as clk:
+        ms = sc.step_timed(w.dt, args.steps)
+    barrier()
+    clocks = clk.summary()
+    sec = ms / 1e3
+    if dist is not None:
+        import torch
+
+        t = torch.tensor([sec], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec = float(t.item())
+    value = w.n * args.steps * ws / sec
+
+    # Per-phase device times (one non-graph step each, after the timed region).
+    phases = {}
+    launches = {}
+    reps = 3
+    for _ in range(reps):
+        for k, (t_ms, nl) in sc.step_profiled(w.dt).items():
+            phases[k] = phases.get(k, 0.0) + t_ms / reps
+            launches[k] = nl
+    launches_per_step = sum(launches.values())
+    dom = max(ALG_BYTES, key=lambda k: phases.get(k, 0.0))
+    iters = w.settings["solver_iterations"]
+    launch_ms = phases[dom] / iters
+    alg = ALG_BYTES[dom] * w.n
+    achieved = alg / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    kern = KERNEL_OF_PHASE[dom]
+    traffic = profile_traffic(kern)
+    roofline = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "alg_bytes_per_launch": alg, "launch_ms": launch_ms,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"}
+
+    # End to end through the host-array drop-in call.
+    e2e = None
+    if not args.no_e2e:
+        try:
+            import torch
+
+            def pinned(shape):
+                return torch.empty(shape, dtype=torch.float32).pin_memory().numpy()
+        except Exception:  # pragma: no cover
+            def pinned(shape):
+                return np.empty(shape, np.float32)
+        hx, hv = pinned((w.n, 3)), pinned((w.n, 3))
+        hr, hl = pinned((w.n,)), pinned((w.n,))
+        hx[:] = w.x
+        hv[:] = w.v
+        hr[:] = 0
+        hl[:] = 0
+        drop = capi.Scene(s, w.x[:1], None, mass=w.mass, device=device)
+        L = capi.load()
+        import ctypes as C
+
+        g = np.ascontiguousarray(w.gravity, np.float32)
+        gp = g.ctypes.data_as(C.POINTER(C.c_float))
+
+        def call():
+            capi.check(L.pbf_solver_step_host(drop.handle, w.n, capi._ptr(hx), capi._ptr(hv),
+                                              capi._ptr(hr), capi._ptr(hl), w.dt, gp, w.mass))
+
+        for _ in range(max(args.warmup, 1)):
+            call()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            call()
+        barrier()
+        el = time.perf_counter() - t0
+        if dist is not None:
+            import torch
+
+            t = torch.tensor([el], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        per = w.n * (12 + 12 + 4 + 4)
+        e2e = {"value": w.n * args.steps * ws / el, "unit": UNIT, "h2d_bytes_per_step": per,
+               "d2h_bytes_per_step": per, "call": "pbf_solver_step_host (pinned host arrays)"}
+        drop.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        counts = (50, 50, 50)
+        val, kind, n, el = time_cpu(counts, 1, 0)
+        cpu = {"value": val, "unit": UNIT, "cores": 1, "kind": kind,
+               "sample": f"{n}-particle {counts[0]}x{counts[1]}x{counts[2]} block of the 1M case's "
+                         f"lattice/box/parameters, 1 step, 1 thread ({el:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "dam_break_1m", "particles": w.n, "lattice": "100x100x100",
+                       "r": 0.01, "h": w.settings["kernel_radius"], "iterations": iters,
+                       "dt": w.dt, "vorticity_epsilon": args.vorticity, "arithmetic": "fast (FMA)",
+                       "hash_compat": 1, "l2": "per-step working set ~190 MB > 129 MB L2",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks,
+            "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+        }
+        print(json.dumps(line), flush=True)
+    sc.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--vorticity", type=float, default=1e-4)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

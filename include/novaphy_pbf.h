@@ -1,0 +1,175 @@
+/*
+ * novaphy_pbf.h - C ABI of the GB300 Position Based Fluids step.
+ *
+ * This is the drop-in boundary for NovaPhy's PBF fluid path.  Each entry point
+ * names the reference interface it replaces (paths inside the NovaPhy tree).
+ * Plain C: pointers, sizes and POD structs; no C++ or torch types.
+ *
+ * Conventions
+ *   - Host arrays of 3-vectors are packed float[3*n] in particle order, the
+ *     layout of std::vector<Eigen::Vector3f> (include/novaphy/fluid/
+ *     particle_state.h:16-44).
+ *   - Every function returns PBF_OK (0) or a PBF_ERR_* code; the message of
+ *     the last failure on the calling thread is pbf_last_error().
+ *   - A scene is device-resident particle state plus its scratch; calls on one
+ *     scene are serialised by the scene's mutex and ordered on its stream.
+ */
+#ifndef NOVAPHY_PBF_H
+#define NOVAPHY_PBF_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBF_ABI_VERSION 1
+
+enum pbf_status {
+    PBF_OK = 0,
+    PBF_ERR_INVALID_ARG = 1, /* bad pointer, size or setting (pybind: ValueError) */
+    PBF_ERR_CUDA = 2,        /* CUDA runtime error */
+    PBF_ERR_OOM = 3,         /* device allocation failed */
+    PBF_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    PBF_ERR_NO_DEVICE = 5,   /* no CUDA device / extension unusable */
+    PBF_ERR_NONFINITE = 6,   /* non-finite value found by pbf_scene_check_finite */
+    PBF_ERR_CAPACITY = 7     /* a size exceeds a fixed maximum */
+};
+
+/* Field order of PBFSettings (include/novaphy/fluid/pbf_solver.h:13-38),
+ * followed by this library's extensions. */
+typedef struct pbf_settings {
+    float rest_density;      /* rho0 (kg/m^3) */
+    float kernel_radius;     /* h (m); the neighbour grid cell is h */
+    float particle_radius;   /* domain clamp inset (m) */
+    int solver_iterations;   /* Jacobi density iterations */
+    float epsilon;           /* CFM relaxation */
+    float xsph_viscosity;    /* XSPH coefficient (0 disables) */
+    float vorticity_epsilon; /* vorticity confinement strength (0 disables) */
+    float corr_delta_q;      /* s_corr delta_q as a fraction of h */
+    float corr_k;            /* s_corr k */
+    int corr_n;              /* s_corr exponent: 4, anything else means 2 */
+    int use_domain_bounds;   /* clamp to [lower+r, upper-r] at commit */
+    float domain_lower[3];
+    float domain_upper[3];
+    /* --- extensions (not in the reference) --- */
+    int exact_arithmetic; /* 1 (default): reference operation order with no
+                             fused multiply-add and IEEE div/sqrt (bit-exact
+                             with the reference); 0: FMA + rsqrt fast path */
+    int hash_compat;      /* 1 (default): reproduce the reference's XOR-hash
+                             bucket merging (neighbor_search.cpp:89-97),
+                             including double-visited buckets; 0: plain
+                             27-cell neighbourhood */
+} pbf_settings;
+
+/* Field selectors for pbf_scene_read / pbf_scene_write. */
+enum pbf_field {
+    PBF_FIELD_POSITIONS = 0,  /* float[3n] */
+    PBF_FIELD_VELOCITIES = 1, /* float[3n] */
+    PBF_FIELD_DENSITIES = 2,  /* float[n]  */
+    PBF_FIELD_LAMBDAS = 3     /* float[n]  */
+};
+
+typedef struct pbf_scene pbf_scene;
+
+/* Library identity and the last error message of the calling thread. */
+const char* pbf_version(void);
+const char* pbf_last_error(void);
+
+/* PBFSettings{} defaults (pbf_solver.h:14-27) plus extension defaults
+ * (exact_arithmetic = 1, hash_compat = 1). */
+int pbf_default_settings(pbf_settings* out);
+
+/* Number of visible CUDA devices (0 on a host without a GPU). */
+int pbf_device_count(int* out);
+
+/* Creates a device-resident scene on `device` from host state: x3/v3 are
+ * float[3n] (v3 may be NULL for zero velocity), `mass` the particle mass.
+ * Replaces constructing ParticleState + PBFSolver
+ * (particle_state.cpp:11-20, pbf_solver.cpp:15-16).  n may be 0. */
+int pbf_scene_create(int device, const pbf_settings* settings, int n, const float* x3,
+                     const float* v3, float mass, pbf_scene** out);
+int pbf_scene_destroy(pbf_scene* scene);
+
+/* Settings are re-read every step, as PBFSolver::settings() edits are
+ * (pbf_solver.cpp:24-25). */
+int pbf_scene_set_settings(pbf_scene* scene, const pbf_settings* settings);
+int pbf_scene_get_settings(const pbf_scene* scene, pbf_settings* out);
+int pbf_scene_set_gravity(pbf_scene* scene, const float* g3);
+int pbf_scene_set_mass(pbf_scene* scene, float mass);
+int pbf_scene_num_particles(const pbf_scene* scene, int* out);
+
+/* Replaces the particle state (ParticleState::init, particle_state.cpp:11-20):
+ * positions and velocities are set, densities and lambdas zeroed. */
+int pbf_scene_reset(pbf_scene* scene, int n, const float* x3, const float* v3);
+
+/* Advances `nsteps` PBF steps of size dt on the device
+ * (PBFSolver::step, pbf_solver.cpp:18-127, repeated).  Asynchronous on the
+ * scene's stream; pbf_scene_sync waits and reports device-side errors. */
+int pbf_scene_step(pbf_scene* scene, float dt, int nsteps);
+int pbf_scene_sync(pbf_scene* scene);
+
+/* pbf_scene_step followed by a wait; *ms_out receives the device time of the
+ * nsteps steps measured with CUDA events on the scene's stream. */
+int pbf_scene_step_timed(pbf_scene* scene, float dt, int nsteps, float* ms_out);
+
+/* Copies a field to/from host memory (blocking).  Reading replaces the
+ * ParticleState vector accessors (python/bindings/bind_fluid.cpp:120-131). */
+int pbf_scene_read(pbf_scene* scene, int field, float* host_out);
+int pbf_scene_write(pbf_scene* scene, int field, const float* host_in);
+
+/* Device pointer of a field's float4 (x,y,z,pad) or float array, for callers
+ * that keep state on the device.  Valid until the scene is reset/destroyed. */
+int pbf_scene_device_field(pbf_scene* scene, int field, void** dptr);
+
+/* The CUDA stream (cudaStream_t) the scene's work is ordered on. */
+int pbf_scene_stream(pbf_scene* scene, void** stream);
+
+/* Host-array drop-in of PBFSolver::step(ParticleState&, dt, gravity, mass)
+ * (include/novaphy/fluid/pbf_solver.h:72, pbf_solver.cpp:18-127): uploads x,
+ * v, densities and lambdas, runs one step, downloads them in place.  The
+ * scene is resized to n as needed; n == 0 returns immediately like the
+ * reference (pbf_solver.cpp:21). */
+int pbf_solver_step_host(pbf_scene* scene, int n, float* x3, float* v3, float* densities,
+                         float* lambdas, float dt, const float* g3, float mass);
+
+/* Finite check of positions and velocities; PBF_ERR_NONFINITE when any
+ * component is NaN/Inf. */
+int pbf_scene_check_finite(pbf_scene* scene);
+
+/* Cell coordinates floor(x * (1/h)) of the predicted positions of the next
+ * step (neighbor_search.cpp:99-105), int[3n] in particle order; for parity. */
+int pbf_scene_debug_cells(pbf_scene* scene, float dt, int* cells3);
+
+/* Canonical neighbour sets at the predicted positions of the next step:
+ * for particle i, the sorted {j != i : |x*_i - x*_j|^2 < h^2} taken over the
+ * grid candidates (pbf_solver.cpp:43-51 restricted to the kernel support).
+ * offsets: long long[n+1]; out_idx: int[cap].  Returns the total in *total;
+ * pass out_idx = NULL to size. */
+int pbf_scene_debug_neighbors(pbf_scene* scene, float dt, long long* offsets, int* out_idx,
+                              long long cap, long long* total);
+
+/* Number of phases reported by pbf_scene_step_profiled. */
+#define PBF_NUM_PHASES 7
+
+/* Name of a step phase: the reference's PerformanceMonitor scope it maps to
+ * (pbf_solver.cpp:29-103), NULL when out of range.  Fused kernels report
+ * under the first scope they cover. */
+const char* pbf_phase_name(int phase);
+
+/* Runs ONE step without graph replay, with CUDA events between the phases,
+ * and returns the device time of each phase (ms) and its kernel launches.
+ * phase_ms / launches have PBF_NUM_PHASES entries (launches may be NULL). */
+int pbf_scene_step_profiled(pbf_scene* scene, float dt, float* phase_ms, int* launches);
+
+/* One-shot device radix sort of (key, index) pairs with 32-bit keys below
+ * 2^key_bits, stable: out_keys/out_vals receive keys in ascending order and
+ * the original positions.  Exposed for testing the sort used by the step. */
+int pbf_sort_pairs_host(int device, int n, const unsigned* keys, int key_bits,
+                        unsigned* out_keys, unsigned* out_vals);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NOVAPHY_PBF_H */

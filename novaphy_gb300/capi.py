@@ -1,0 +1,306 @@
+"""ctypes binding of the C ABI in include/novaphy_pbf.h.
+
+This is the thin Python view of ``libnovaphy_pbf.so`` used by tests and
+bench.py; the user-facing NovaPhy API lives in ``novaphy_gb300._core``.
+Loading fails loudly when the library has not been built: there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libnovaphy_pbf.so")
+HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "novaphy_pbf.h")
+
+PBF_OK = 0
+PBF_ERR_INVALID_ARG = 1
+PBF_ERR_CUDA = 2
+PBF_ERR_OOM = 3
+PBF_ERR_TIMEOUT = 4
+PBF_ERR_NO_DEVICE = 5
+PBF_ERR_NONFINITE = 6
+PBF_ERR_CAPACITY = 7
+
+FIELD_POSITIONS = 0
+FIELD_VELOCITIES = 1
+FIELD_DENSITIES = 2
+FIELD_LAMBDAS = 3
+
+
+class PbfError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"pbf error {code}: {msg}")
+        self.code = code
+
+
+class Settings(C.Structure):
+    """pbf_settings: PBFSettings field order plus the library's extensions."""
+
+    _fields_ = [
+        ("rest_density", C.c_float),
+        ("kernel_radius", C.c_float),
+        ("particle_radius", C.c_float),
+        ("solver_iterations", C.c_int),
+        ("epsilon", C.c_float),
+        ("xsph_viscosity", C.c_float),
+        ("vorticity_epsilon", C.c_float),
+        ("corr_delta_q", C.c_float),
+        ("corr_k", C.c_float),
+        ("corr_n", C.c_int),
+        ("use_domain_bounds", C.c_int),
+        ("domain_lower", C.c_float * 3),
+        ("domain_upper", C.c_float * 3),
+        ("exact_arithmetic", C.c_int),
+        ("hash_compat", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load() -> C.CDLL:
+    """Loads libnovaphy_pbf.so (raises if it is missing: build it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} not found: build the CUDA extension with "
+            "`python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(LIB_PATH)
+    f32p = C.POINTER(C.c_float)
+    vp = C.c_void_p
+    sig = {
+        "pbf_version": ([], C.c_char_p),
+        "pbf_last_error": ([], C.c_char_p),
+        "pbf_default_settings": ([C.POINTER(Settings)], C.c_int),
+        "pbf_device_count": ([C.POINTER(C.c_int)], C.c_int),
+        "pbf_scene_create": ([C.c_int, C.POINTER(Settings), C.c_int, vp, vp, C.c_float,
+                              C.POINTER(vp)], C.c_int),
+        "pbf_scene_destroy": ([vp], C.c_int),
+        "pbf_scene_set_settings": ([vp, C.POINTER(Settings)], C.c_int),
+        "pbf_scene_get_settings": ([vp, C.POINTER(Settings)], C.c_int),
+        "pbf_scene_set_gravity": ([vp, f32p], C.c_int),
+        "pbf_scene_set_mass": ([vp, C.c_float], C.c_int),
+        "pbf_scene_num_particles": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "pbf_scene_reset": ([vp, C.c_int, vp, vp], C.c_int),
+        "pbf_scene_step": ([vp, C.c_float, C.c_int], C.c_int),
+        "pbf_scene_sync": ([vp], C.c_int),
+        "pbf_scene_read": ([vp, C.c_int, vp], C.c_int),
+        "pbf_scene_write": ([vp, C.c_int, vp], C.c_int),
+        "pbf_scene_device_field": ([vp, C.c_int, C.POINTER(vp)], C.c_int),
+        "pbf_scene_stream": ([vp, C.POINTER(vp)], C.c_int),
+        "pbf_solver_step_host": ([vp, C.c_int, vp, vp, vp, vp, C.c_float, f32p, C.c_float],
+                                 C.c_int),
+        "pbf_scene_check_finite": ([vp], C.c_int),
+        "pbf_scene_debug_cells": ([vp, C.c_float, vp], C.c_int),
+        "pbf_scene_debug_neighbors": ([vp, C.c_float, vp, vp, C.c_longlong,
+                                       C.POINTER(C.c_longlong)], C.c_int),
+        "pbf_sort_pairs_host": ([C.c_int, C.c_int, vp, C.c_int, vp, vp], C.c_int),
+        "pbf_phase_name": ([C.c_int], C.c_char_p),
+        "pbf_scene_step_timed": ([vp, C.c_float, C.c_int, f32p], C.c_int),
+        "pbf_scene_step_profiled": ([vp, C.c_float, vp, vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/novaphy_pbf.h."""
+    txt = open(HEADER_PATH).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(pbf_[a-z0-9_]+)\s*\(", txt)))
+
+
+def check(rc: int) -> None:
+    if rc != PBF_OK:
+        msg = load().pbf_last_error()
+        raise PbfError(rc, msg.decode() if msg else "")
+
+
+def default_settings(**kw) -> Settings:
+    s = Settings()
+    check(load().pbf_default_settings(C.byref(s)))
+    for k, v in kw.items():
+        if k in ("domain_lower", "domain_upper"):
+            getattr(s, k)[:] = [float(t) for t in v]
+        elif k in ("use_domain_bounds", "exact_arithmetic", "hash_compat"):
+            setattr(s, k, int(bool(v)))
+        else:
+            setattr(s, k, v)
+    return s
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    load().pbf_device_count(C.byref(n))
+    return n.value
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    return a.reshape(shape) if shape is not None else a
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Scene:
+    """Device-resident PBF scene (pbf_scene*)."""
+
+    def __init__(self, settings: Settings, x, v=None, mass: float = 0.0, device: int = 0):
+        L = load()
+        x = _f32(x, (-1, 3))
+        v = None if v is None else _f32(v, (-1, 3))
+        h = C.c_void_p()
+        check(L.pbf_scene_create(device, C.byref(settings), len(x), _ptr(x),
+                                 None if v is None else _ptr(v), mass, C.byref(h)))
+        self._h = h
+        self._L = L
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            self._L.pbf_scene_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n(self) -> int:
+        c = C.c_int()
+        check(self._L.pbf_scene_num_particles(self._h, C.byref(c)))
+        return c.value
+
+    def set_settings(self, s: Settings):
+        check(self._L.pbf_scene_set_settings(self._h, C.byref(s)))
+
+    def get_settings(self) -> Settings:
+        s = Settings()
+        check(self._L.pbf_scene_get_settings(self._h, C.byref(s)))
+        return s
+
+    def set_gravity(self, g):
+        g = _f32(g, (3,))
+        check(self._L.pbf_scene_set_gravity(self._h, g.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def set_mass(self, m: float):
+        check(self._L.pbf_scene_set_mass(self._h, m))
+
+    def reset(self, x, v=None):
+        x = _f32(x, (-1, 3))
+        v = None if v is None else _f32(v, (-1, 3))
+        check(self._L.pbf_scene_reset(self._h, len(x), _ptr(x), None if v is None else _ptr(v)))
+
+    def step(self, dt: float, nsteps: int = 1, sync: bool = True):
+        check(self._L.pbf_scene_step(self._h, dt, nsteps))
+        if sync:
+            self.sync()
+
+    def step_timed(self, dt: float, nsteps: int) -> float:
+        """Device milliseconds of `nsteps` steps (CUDA events on the scene stream)."""
+        ms = C.c_float(0.0)
+        check(self._L.pbf_scene_step_timed(self._h, dt, nsteps, C.byref(ms)))
+        return ms.value
+
+    def sync(self):
+        check(self._L.pbf_scene_sync(self._h))
+
+    def read(self, field: int) -> np.ndarray:
+        n = self.n
+        shape = (n, 3) if field in (FIELD_POSITIONS, FIELD_VELOCITIES) else (n,)
+        out = np.zeros(shape, np.float32)
+        check(self._L.pbf_scene_read(self._h, field, _ptr(out)))
+        return out
+
+    def write(self, field: int, a):
+        n = self.n
+        a = _f32(a, (n, 3) if field in (FIELD_POSITIONS, FIELD_VELOCITIES) else (n,))
+        check(self._L.pbf_scene_write(self._h, field, _ptr(a)))
+
+    def state(self):
+        return (self.read(FIELD_POSITIONS), self.read(FIELD_VELOCITIES),
+                self.read(FIELD_DENSITIES), self.read(FIELD_LAMBDAS))
+
+    def device_field(self, field: int) -> int:
+        p = C.c_void_p()
+        check(self._L.pbf_scene_device_field(self._h, field, C.byref(p)))
+        return p.value or 0
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        check(self._L.pbf_scene_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def check_finite(self) -> int:
+        return self._L.pbf_scene_check_finite(self._h)
+
+    def debug_cells(self, dt: float) -> np.ndarray:
+        out = np.zeros((self.n, 3), np.int32)
+        check(self._L.pbf_scene_debug_cells(self._h, dt, _ptr(out)))
+        return out
+
+    def debug_neighbors(self, dt: float):
+        n = self.n
+        offs = np.zeros(n + 1, np.int64)
+        tot = C.c_longlong(0)
+        check(self._L.pbf_scene_debug_neighbors(self._h, dt, _ptr(offs), None, 0, C.byref(tot)))
+        out = np.zeros(max(tot.value, 1), np.int32)
+        check(self._L.pbf_scene_debug_neighbors(self._h, dt, _ptr(offs), _ptr(out), tot.value,
+                                                C.byref(tot)))
+        return offs, out[:tot.value]
+
+    def step_profiled(self, dt: float) -> dict:
+        """One step with per-phase device times: {phase name: (ms, launches)}."""
+        ms = np.zeros(NUM_PHASES, np.float32)
+        nl = np.zeros(NUM_PHASES, np.int32)
+        check(self._L.pbf_scene_step_profiled(self._h, dt, _ptr(ms), _ptr(nl)))
+        return {phase_name(k): (float(ms[k]), int(nl[k])) for k in range(NUM_PHASES)}
+
+    def solver_step_host(self, x, v, rho, lam, dt, g, mass):
+        """pbf_solver_step_host on copies; returns the updated arrays."""
+        x = _f32(x, (-1, 3)).copy()
+        v = _f32(v, (-1, 3)).copy()
+        rho = _f32(rho).copy()
+        lam = _f32(lam).copy()
+        g = _f32(g, (3,))
+        check(self._L.pbf_solver_step_host(self._h, len(x), _ptr(x), _ptr(v), _ptr(rho),
+                                           _ptr(lam), dt,
+                                           g.ctypes.data_as(C.POINTER(C.c_float)), mass))
+        return x, v, rho, lam
+
+
+NUM_PHASES = 7
+
+
+def phase_name(k: int) -> str:
+    return load().pbf_phase_name(k).decode()
+
+
+def sort_pairs(keys, key_bits: int, device: int = 0):
+    keys = np.ascontiguousarray(keys, dtype=np.uint32)
+    ko = np.zeros_like(keys)
+    vo = np.zeros_like(keys)
+    check(load().pbf_sort_pairs_host(device, len(keys), _ptr(keys), key_bits, _ptr(ko), _ptr(vo)))
+    return ko, vo

@@ -1,0 +1,924 @@
+// C ABI of the PBF step (include/novaphy_pbf.h): scene lifetime, host<->device
+// transfer, settings -> per-step constants, and step orchestration with CUDA
+// graph replay.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "novaphy_pbf.h"
+#include "pbf_launch.cuh"
+#include "pbf_types.cuh"
+#include "radix_sort.cuh"
+
+using namespace pbf;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    const int code = (e == cudaErrorMemoryAllocation) ? PBF_ERR_OOM
+                     : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+                         ? PBF_ERR_NO_DEVICE
+                         : PBF_ERR_CUDA;
+    return fail(code, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define PBF_CUDA(expr)                                  \
+    do {                                                \
+        cudaError_t e_ = (expr);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr); \
+    } while (0)
+
+constexpr float kPi = 3.14159265358979323846f;  // math_utils.h:53
+
+// Sets the device for the lifetime of the guard, restoring the previous one.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+__global__ void k_expand3(const float* __restrict__ a3, float4* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_float4(a3[3 * i], a3[3 * i + 1], a3[3 * i + 2], 0.0f);
+}
+
+__global__ void k_pack3(const float4* __restrict__ in, float* __restrict__ a3, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 t = in[i];
+        a3[3 * i] = t.x;
+        a3[3 * i + 1] = t.y;
+        a3[3 * i + 2] = t.z;
+    }
+}
+
+__global__ void k_finite(const float4* __restrict__ x, const float4* __restrict__ v, int n,
+                         uint32_t* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 a = x[i], b = v[i];
+        if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) &&
+              isfinite(b.z)))
+            atomicOr(flag, 1u);
+    }
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct pbf_scene {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    pbf_settings settings{};
+    float gravity[3] = {0.0f, -9.81f, 0.0f};  // World default (include/novaphy/sim/world.h:157)
+    float mass = 0.0f;
+    int n = 0;
+    int cap = 0;
+    // Region the grid is fitted to when the domain clamp is off.
+    bool have_bbox = false;
+    float bbox_lo[3] = {0, 0, 0}, bbox_hi[3] = {0, 0, 0};
+
+    void* pmem = nullptr;  // per-particle arrays
+    void* smem = nullptr;  // sort scratch
+    uint32_t* off = nullptr;
+    uint32_t off_cap = 0;  // entries
+    float* staging = nullptr;  // float[3 cap]
+    uint32_t* d_flag = nullptr;
+    SortScratch sort{};
+    StepBuffers B{};
+
+    // Graph of one step, re-captured when the constants change.
+    cudaGraphExec_t graph = nullptr;
+    StepConsts graph_consts{};
+    int graph_iters = -1;
+    int graph_exact = -1;
+};
+
+namespace {
+
+void free_particles(pbf_scene* s) {
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    if (s->pmem) cudaFree(s->pmem);
+    if (s->smem) cudaFree(s->smem);
+    s->pmem = s->smem = nullptr;
+    s->cap = 0;
+    s->B = StepBuffers{};
+}
+
+// (Re)allocates the per-particle arrays for `cap` particles.
+int alloc_particles(pbf_scene* s, int cap) {
+    free_particles(s);
+    const int c = cap > 0 ? cap : 1;
+    const size_t f4 = align_up((size_t)c * 16, 256);
+    const size_t f1 = align_up((size_t)c * 4, 256);
+    const size_t f2 = align_up((size_t)c * 8, 256);
+    const size_t f3 = align_up((size_t)c * 12, 256);
+    const size_t f27 = align_up((size_t)c * 27 * 4, 256);
+    const size_t total = 8 * f4 + 3 * f1 + 3 * f1 + f4 + f3 + 2 * f2 + 5 * f1 + f27;
+    PBF_CUDA(cudaMalloc(&s->pmem, total));
+    char* p = reinterpret_cast<char*>(s->pmem);
+    auto take = [&](size_t b) {
+        char* r = p;
+        p += b;
+        return r;
+    };
+    StepBuffers& B = s->B;
+    B.x = reinterpret_cast<float4*>(take(f4));
+    B.v = reinterpret_cast<float4*>(take(f4));
+    B.sx = reinterpret_cast<float4*>(take(f4));
+    B.xa = reinterpret_cast<float4*>(take(f4));
+    B.xb = reinterpret_cast<float4*>(take(f4));
+    B.sv = reinterpret_cast<float4*>(take(f4));
+    B.sv2 = reinterpret_cast<float4*>(take(f4));
+    B.som = reinterpret_cast<float4*>(take(f4));
+    B.rho = reinterpret_cast<float*>(take(f1));
+    B.lam = reinterpret_cast<float*>(take(f1));
+    B.srho = reinterpret_cast<float*>(take(f1));
+    B.keys = reinterpret_cast<uint32_t*>(take(f1));
+    B.skeys = reinterpret_cast<uint32_t*>(take(f1));
+    B.sidx = reinterpret_cast<uint32_t*>(take(f1));
+    B.scell = reinterpret_cast<int4*>(take(f4));
+    s->staging = reinterpret_cast<float*>(take(f3));
+    B.rkeys = reinterpret_cast<unsigned long long*>(take(f2));
+    B.rsorted = reinterpret_cast<unsigned long long*>(take(f2));
+    B.ridx = reinterpret_cast<uint32_t*>(take(f1));
+    B.pos_of = reinterpret_cast<uint32_t*>(take(f1));
+    B.kpos = reinterpret_cast<uint32_t*>(take(f1));
+    B.bend = reinterpret_cast<uint32_t*>(take(f1));
+    B.sown = reinterpret_cast<int*>(take(f1));
+    B.btab = reinterpret_cast<uint32_t*>(take(f27));
+    PBF_CUDA(cudaMemsetAsync(s->pmem, 0, total, s->stream));
+    const size_t sb = sort_scratch_bytes(c);
+    PBF_CUDA(cudaMalloc(&s->smem, sb));
+    PBF_CUDA(cudaMemsetAsync(s->smem, 0, sb, s->stream));
+    sort_scratch_bind(s->sort, s->smem, c);
+    B.err = s->sort.err;
+    B.off = s->off;
+    if (s->off) B.slot_alias = reinterpret_cast<unsigned char*>(s->off) +
+                                align_up((size_t)s->off_cap * 4, 256);
+    s->cap = c;
+    return PBF_OK;
+}
+
+int check_settings(const pbf_settings* st) {
+    if (!st) return fail(PBF_ERR_INVALID_ARG, "settings is NULL");
+    if (!(st->kernel_radius > 0.0f) || !std::isfinite(st->kernel_radius))
+        return fail(PBF_ERR_INVALID_ARG, "kernel_radius must be a positive finite number");
+    if (!(st->rest_density > 0.0f))
+        return fail(PBF_ERR_INVALID_ARG, "rest_density must be positive");
+    if (st->solver_iterations < 0 || st->solver_iterations > 1000)
+        return fail(PBF_ERR_INVALID_ARG, "solver_iterations must be in [0, 1000]");
+    return PBF_OK;
+}
+
+// Grid fitted to the domain (clamp on) or to the particles' bounding box,
+// with two cells of margin; each axis >= 4 and at most 2^24 slots in total.
+GridDesc fit_grid(const pbf_scene* s) {
+    const pbf_settings& st = s->settings;
+    const float inv = 1.0f / st.kernel_radius;
+    float lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        if (st.use_domain_bounds) {
+            lo[d] = std::min(st.domain_lower[d], st.domain_upper[d]);
+            hi[d] = std::max(st.domain_lower[d], st.domain_upper[d]);
+        } else if (s->have_bbox) {
+            lo[d] = s->bbox_lo[d];
+            hi[d] = s->bbox_hi[d];
+        } else {
+            lo[d] = 0.0f;
+            hi[d] = 0.0f;
+        }
+    }
+    long long o[3], g[3];
+    for (int d = 0; d < 3; ++d) {
+        double a = std::floor((double)lo[d] * inv), b = std::floor((double)hi[d] * inv);
+        if (!std::isfinite(a) || !std::isfinite(b) || b - a > 4096.0) b = a + 4096.0;
+        if (!std::isfinite(a) || std::fabs(a) > 1e9) a = 0.0, b = 4096.0;
+        o[d] = (long long)a - 2;
+        g[d] = (long long)(b - a) + 5;
+        if (g[d] < 4) g[d] = 4;
+    }
+    const long long kMaxSlots = 1LL << 24;
+    while (g[0] * g[1] * g[2] > kMaxSlots) {
+        int m = 0;
+        for (int d = 1; d < 3; ++d)
+            if (g[d] > g[m]) m = d;
+        g[m] = std::max(4LL, g[m] / 2);
+    }
+    GridDesc G;
+    G.ox = (int)o[0];
+    G.oy = (int)o[1];
+    G.oz = (int)o[2];
+    G.gx = (int)g[0];
+    G.gy = (int)g[1];
+    G.gz = (int)g[2];
+    G.nslots = (uint32_t)(g[0] * g[1] * g[2]);
+    int bits = 1;
+    while ((1ull << bits) < (unsigned long long)G.nslots) ++bits;
+    G.key_bits = bits;
+    return G;
+}
+
+int ensure_offsets(pbf_scene* s, uint32_t nslots) {
+    if (s->off && s->off_cap >= nslots + 1) return PBF_OK;
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    if (s->off) cudaFree(s->off);
+    s->off = nullptr;
+    // offsets (nslots + 1 words) followed by one alias byte per slot
+    const size_t ob = align_up((size_t)(nslots + 1) * 4, 256);
+    PBF_CUDA(cudaMalloc(&s->off, ob + align_up(nslots, 256)));
+    s->off_cap = nslots + 1;
+    s->B.off = s->off;
+    s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) + ob;
+    return PBF_OK;
+}
+
+float host_poly6(float r_sq, float h) {
+    // sph_kernel.h:24-30, float arithmetic, no contraction.
+    if (r_sq >= h * h) return 0.0f;
+    float h2 = h * h;
+    float diff = h2 - r_sq;
+    float h9 = h2 * h2 * h2 * h2 * h;
+    return (315.0f / (64.0f * kPi * h9)) * diff * diff * diff;
+}
+
+// Per-step constants from settings (operation order of pbf_solver.cpp).
+int make_consts(pbf_scene* s, float dt, StepConsts& C) {
+    const pbf_settings& st = s->settings;
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(PBF_ERR_INVALID_ARG, "dt must be > 0");
+    std::memset(&C, 0, sizeof(C));
+    C.n = s->n;
+    const float h = st.kernel_radius;
+    C.h = h;
+    C.h2 = h * h;
+    {
+        // Smallest float g with sqrtf(g) >= h; any r_sq >= max(h2, g) gives
+        // poly6 == 0 and spiky_grad == 0 (sph_kernel.h:25, :40).
+        float g = C.h2;
+        if (std::sqrt(g) >= h) {
+            for (int k = 0; k < 64; ++k) {
+                float p = std::nextafter(g, 0.0f);
+                if (std::sqrt(p) >= h) g = p;
+                else break;
+            }
+        } else {
+            for (int k = 0; k < 64 && std::sqrt(g) < h; ++k) g = std::nextafter(g, INFINITY);
+        }
+        C.cut = std::max(C.h2, g);
+    }
+    C.inv_cell = 1.0f / h;
+    C.mass = s->mass;
+    C.rho0 = st.rest_density;
+    C.inv_rho0 = 1.0f / st.rest_density;
+    C.eps = st.epsilon;
+    C.mr = s->mass * C.inv_rho0;
+    {
+        float h2 = h * h;
+        float h9 = h2 * h2 * h2 * h2 * h;
+        C.k_poly = 315.0f / (64.0f * kPi * h9);
+        float h6 = h * h * h * h * h * h;
+        C.k_spiky = -(45.0f / (kPi * h6));
+    }
+    const float delta_q = st.corr_delta_q * h;
+    C.w_dq = host_poly6(delta_q * delta_q, h);
+    C.neg_corr_k = -st.corr_k;
+    C.corr_n4 = st.corr_n == 4 ? 1 : 0;
+    C.scorr_on = C.w_dq > 1e-10f ? 1 : 0;
+    C.dt = dt;
+    C.inv_dt = 1.0f / dt;
+    C.max_speed = h / dt;
+    C.max_speed_sq = C.max_speed * C.max_speed;
+    for (int d = 0; d < 3; ++d) C.g[d] = s->gravity[d];
+    C.xsph_c = st.xsph_viscosity;
+    C.xsph_on = st.xsph_viscosity > 0.0f ? 1 : 0;
+    C.vort_eps = st.vorticity_epsilon;
+    C.vort_scale = dt * st.vorticity_epsilon;
+    C.vort_on = st.vorticity_epsilon > 0.0f ? 1 : 0;
+    C.clamp = st.use_domain_bounds ? 1 : 0;
+    const float pr = st.particle_radius;
+    for (int d = 0; d < 3; ++d) {
+        C.lo[d] = st.domain_lower[d] + pr;
+        C.hi[d] = st.domain_upper[d] - pr;
+    }
+    C.hash_compat = st.hash_compat ? 1 : 0;
+    C.grid = fit_grid(s);
+    return ensure_offsets(s, C.grid.nslots);
+}
+
+void update_bbox(pbf_scene* s, const float* x3, int n) {
+    if (n <= 0 || !x3) {
+        s->have_bbox = false;
+        return;
+    }
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            const float t = x3[3 * i + d];
+            if (std::isfinite(t)) {
+                lo[d] = std::min(lo[d], t);
+                hi[d] = std::max(hi[d], t);
+            }
+        }
+    for (int d = 0; d < 3; ++d) {
+        if (!(lo[d] <= hi[d])) lo[d] = hi[d] = 0.0f;
+        // Leave room for the fluid to spread.
+        const float ext = hi[d] - lo[d];
+        s->bbox_lo[d] = lo[d] - 0.5f * ext;
+        s->bbox_hi[d] = hi[d] + 0.5f * ext;
+    }
+    s->have_bbox = true;
+}
+
+int upload3(pbf_scene* s, const float* host3, float4* dst, int n) {
+    if (n <= 0) return PBF_OK;
+    PBF_CUDA(cudaMemcpyAsync(s->staging, host3, (size_t)n * 12, cudaMemcpyHostToDevice, s->stream));
+    k_expand3<<<(n + 255) / 256, 256, 0, s->stream>>>(s->staging, dst, n);
+    PBF_CUDA(cudaGetLastError());
+    return PBF_OK;
+}
+
+int download3(pbf_scene* s, const float4* src, float* host3, int n) {
+    if (n <= 0) return PBF_OK;
+    k_pack3<<<(n + 255) / 256, 256, 0, s->stream>>>(src, s->staging, n);
+    PBF_CUDA(cudaGetLastError());
+    PBF_CUDA(cudaMemcpyAsync(host3, s->staging, (size_t)n * 12, cudaMemcpyDeviceToHost, s->stream));
+    return PBF_OK;
+}
+
+int set_state(pbf_scene* s, int n, const float* x3, const float* v3) {
+    if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n must be >= 0");
+    if (n > 0 && !x3) return fail(PBF_ERR_INVALID_ARG, "positions are NULL");
+    if (n > (1 << 29)) return fail(PBF_ERR_CAPACITY, "at most 2^29 particles per scene");
+    if (n > s->cap || !s->pmem) {
+        int rc = alloc_particles(s, n);
+        if (rc) return rc;
+    }
+    s->n = n;
+    if (n == 0) return PBF_OK;
+    int rc = upload3(s, x3, s->B.x, n);
+    if (rc) return rc;
+    if (v3) {
+        rc = upload3(s, v3, s->B.v, n);
+        if (rc) return rc;
+    } else {
+        PBF_CUDA(cudaMemsetAsync(s->B.v, 0, (size_t)n * 16, s->stream));
+    }
+    PBF_CUDA(cudaMemsetAsync(s->B.rho, 0, (size_t)n * 4, s->stream));
+    PBF_CUDA(cudaMemsetAsync(s->B.lam, 0, (size_t)n * 4, s->stream));
+    // The grid follows the domain when the clamp is on; otherwise it is
+    // fitted to the particles given here.
+    if (!s->settings.use_domain_bounds) update_bbox(s, x3, n);
+    return PBF_OK;
+}
+
+bool consts_equal(const StepConsts& a, const StepConsts& b) {
+    return std::memcmp(&a, &b, sizeof(StepConsts)) == 0;
+}
+
+int enqueue(pbf_scene* s, const StepConsts& C, cudaStream_t st, PhaseMarks* pm = nullptr) {
+    const int iters = s->settings.solver_iterations;
+    cudaError_t e = s->settings.exact_arithmetic
+                        ? exact_enqueue_step(s->B, C, iters, s->sort, st, pm)
+                        : fast_enqueue_step(s->B, C, iters, s->sort, st, pm);
+    if (e != cudaSuccess) return cuda_fail(e, "enqueue_step");
+    return PBF_OK;
+}
+
+bool graphs_enabled() {
+    const char* v = std::getenv("PBF_NO_GRAPH");
+    return !(v && v[0] == '1');
+}
+
+int run_steps(pbf_scene* s, float dt, int nsteps) {
+    if (nsteps < 0) return fail(PBF_ERR_INVALID_ARG, "nsteps must be >= 0");
+    if (s->n == 0 || nsteps == 0) return PBF_OK;  // pbf_solver.cpp:21
+    StepConsts C;
+    int rc = make_consts(s, dt, C);
+    if (rc) return rc;
+    if (!graphs_enabled()) {
+        for (int k = 0; k < nsteps; ++k) {
+            rc = enqueue(s, C, s->stream);
+            if (rc) return rc;
+        }
+        return PBF_OK;
+    }
+    const int iters = s->settings.solver_iterations;
+    const int exact = s->settings.exact_arithmetic ? 1 : 0;
+    if (!s->graph || !consts_equal(C, s->graph_consts) || iters != s->graph_iters ||
+        exact != s->graph_exact) {
+        if (s->graph) {
+            cudaGraphExecDestroy(s->graph);
+            s->graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        PBF_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        const int erc = enqueue(s, C, s->stream);
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+        if (erc) {
+            if (g) cudaGraphDestroy(g);
+            return erc;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&s->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            s->graph = nullptr;
+            return cuda_fail(ce, "cudaGraphInstantiate");
+        }
+        s->graph_consts = C;
+        s->graph_iters = iters;
+        s->graph_exact = exact;
+    }
+    for (int k = 0; k < nsteps; ++k) PBF_CUDA(cudaGraphLaunch(s->graph, s->stream));
+    return PBF_OK;
+}
+
+int sync_and_check(pbf_scene* s) {
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    if (!s->sort.err) return PBF_OK;
+    uint32_t err = 0;
+    PBF_CUDA(cudaMemcpy(&err, s->sort.err, 4, cudaMemcpyDeviceToHost));
+    if (err) {
+        PBF_CUDA(cudaMemset(s->sort.err, 0, 4));
+        return fail(PBF_ERR_TIMEOUT, "device-side wait in the cell sort gave up (error word " +
+                                         std::to_string(err) + ")");
+    }
+    return PBF_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+const char* pbf_version(void) { return "novaphy_gb300 pbf 1 (sm_103a)"; }
+
+const char* pbf_last_error(void) { return g_last_error.c_str(); }
+
+int pbf_default_settings(pbf_settings* out) {
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+    pbf_settings d{};
+    // PBFSettings defaults, include/novaphy/fluid/pbf_solver.h:14-27.
+    d.rest_density = 1000.0f;
+    d.kernel_radius = 0.1f;
+    d.particle_radius = 0.025f;
+    d.solver_iterations = 4;
+    d.epsilon = 100.0f;
+    d.xsph_viscosity = 0.01f;
+    d.vorticity_epsilon = 0.0f;
+    d.corr_delta_q = 0.3f;
+    d.corr_k = 0.001f;
+    d.corr_n = 4;
+    d.use_domain_bounds = 0;
+    d.domain_lower[0] = -10.0f;
+    d.domain_lower[1] = 0.0f;
+    d.domain_lower[2] = -10.0f;
+    d.domain_upper[0] = 10.0f;
+    d.domain_upper[1] = 10.0f;
+    d.domain_upper[2] = 10.0f;
+    d.exact_arithmetic = 1;
+    d.hash_compat = 1;
+    *out = d;
+    return PBF_OK;
+}
+
+int pbf_device_count(int* out) {
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (e != cudaSuccess) {
+        *out = 0;
+        return cuda_fail(e, "cudaGetDeviceCount");
+    }
+    *out = c;
+    return PBF_OK;
+}
+
+int pbf_scene_create(int device, const pbf_settings* settings, int n, const float* x3,
+                     const float* v3, float mass, pbf_scene** out) {
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int rc = check_settings(settings);
+    if (rc) return rc;
+    int count = 0;
+    cudaError_t ce = cudaGetDeviceCount(&count);
+    if (ce != cudaSuccess || count == 0)
+        return fail(PBF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(ce));
+    if (device < 0 || device >= count) return fail(PBF_ERR_INVALID_ARG, "device out of range");
+    DeviceGuard dg(device);
+    if (!dg.ok) return fail(PBF_ERR_NO_DEVICE, "cudaSetDevice failed");
+    pbf_scene* s = new pbf_scene();
+    s->device = device;
+    s->settings = *settings;
+    s->mass = mass;
+    ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        delete s;
+        return cuda_fail(ce, "cudaStreamCreate");
+    }
+    rc = set_state(s, n, x3, v3);
+    if (rc == PBF_OK) {
+        ce = cudaStreamSynchronize(s->stream);
+        if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaStreamSynchronize");
+    }
+    if (rc) {
+        pbf_scene_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return PBF_OK;
+}
+
+int pbf_scene_destroy(pbf_scene* s) {
+    if (!s) return PBF_OK;
+    {
+        DeviceGuard dg(s->device);
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        free_particles(s);
+        if (s->off) cudaFree(s->off);
+        if (s->d_flag) cudaFree(s->d_flag);
+        if (s->stream) cudaStreamDestroy(s->stream);
+    }
+    delete s;
+    return PBF_OK;
+}
+
+int pbf_scene_set_settings(pbf_scene* s, const pbf_settings* settings) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    int rc = check_settings(settings);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->settings = *settings;
+    return PBF_OK;
+}
+
+int pbf_scene_get_settings(const pbf_scene* s, pbf_settings* out) {
+    if (!s || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *out = s->settings;
+    return PBF_OK;
+}
+
+int pbf_scene_set_gravity(pbf_scene* s, const float* g3) {
+    if (!s || !g3) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (int d = 0; d < 3; ++d) s->gravity[d] = g3[d];
+    return PBF_OK;
+}
+
+int pbf_scene_set_mass(pbf_scene* s, float mass) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->mass = mass;
+    return PBF_OK;
+}
+
+int pbf_scene_num_particles(const pbf_scene* s, int* out) {
+    if (!s || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *out = s->n;
+    return PBF_OK;
+}
+
+int pbf_scene_reset(pbf_scene* s, int n, const float* x3, const float* v3) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = set_state(s, n, x3, v3);
+    if (rc) return rc;
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    return PBF_OK;
+}
+
+int pbf_scene_step(pbf_scene* s, float dt, int nsteps) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    return run_steps(s, dt, nsteps);
+}
+
+int pbf_scene_step_timed(pbf_scene* s, float dt, int nsteps, float* ms_out) {
+    if (!s || !ms_out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    *ms_out = 0.0f;
+    cudaEvent_t a = nullptr, b = nullptr;
+    PBF_CUDA(cudaEventCreate(&a));
+    cudaError_t e = cudaEventCreate(&b);
+    int rc = PBF_OK;
+    if (e == cudaSuccess) e = cudaEventRecord(a, s->stream);
+    if (e == cudaSuccess) rc = run_steps(s, dt, nsteps);
+    if (e == cudaSuccess && rc == PBF_OK) e = cudaEventRecord(b, s->stream);
+    if (e == cudaSuccess && rc == PBF_OK) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess && rc == PBF_OK) e = cudaEventElapsedTime(ms_out, a, b);
+    cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "pbf_scene_step_timed");
+    return sync_and_check(s);
+}
+
+int pbf_scene_sync(pbf_scene* s) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    return sync_and_check(s);
+}
+
+int pbf_scene_read(pbf_scene* s, int field, float* host_out) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    if (s->n > 0 && !host_out) return fail(PBF_ERR_INVALID_ARG, "output is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = PBF_OK;
+    switch (field) {
+        case PBF_FIELD_POSITIONS: rc = download3(s, s->B.x, host_out, s->n); break;
+        case PBF_FIELD_VELOCITIES: rc = download3(s, s->B.v, host_out, s->n); break;
+        case PBF_FIELD_DENSITIES:
+            if (s->n) PBF_CUDA(cudaMemcpyAsync(host_out, s->B.rho, (size_t)s->n * 4, cudaMemcpyDeviceToHost, s->stream));
+            break;
+        case PBF_FIELD_LAMBDAS:
+            if (s->n) PBF_CUDA(cudaMemcpyAsync(host_out, s->B.lam, (size_t)s->n * 4, cudaMemcpyDeviceToHost, s->stream));
+            break;
+        default: return fail(PBF_ERR_INVALID_ARG, "unknown field");
+    }
+    if (rc) return rc;
+    return sync_and_check(s);
+}
+
+int pbf_scene_write(pbf_scene* s, int field, const float* host_in) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    if (s->n > 0 && !host_in) return fail(PBF_ERR_INVALID_ARG, "input is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = PBF_OK;
+    switch (field) {
+        case PBF_FIELD_POSITIONS:
+            rc = upload3(s, host_in, s->B.x, s->n);
+            if (!rc) update_bbox(s, host_in, s->n);
+            break;
+        case PBF_FIELD_VELOCITIES: rc = upload3(s, host_in, s->B.v, s->n); break;
+        case PBF_FIELD_DENSITIES:
+            if (s->n) PBF_CUDA(cudaMemcpyAsync(s->B.rho, host_in, (size_t)s->n * 4, cudaMemcpyHostToDevice, s->stream));
+            break;
+        case PBF_FIELD_LAMBDAS:
+            if (s->n) PBF_CUDA(cudaMemcpyAsync(s->B.lam, host_in, (size_t)s->n * 4, cudaMemcpyHostToDevice, s->stream));
+            break;
+        default: return fail(PBF_ERR_INVALID_ARG, "unknown field");
+    }
+    if (rc) return rc;
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    return PBF_OK;
+}
+
+int pbf_scene_device_field(pbf_scene* s, int field, void** dptr) {
+    if (!s || !dptr) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    switch (field) {
+        case PBF_FIELD_POSITIONS: *dptr = s->B.x; break;
+        case PBF_FIELD_VELOCITIES: *dptr = s->B.v; break;
+        case PBF_FIELD_DENSITIES: *dptr = s->B.rho; break;
+        case PBF_FIELD_LAMBDAS: *dptr = s->B.lam; break;
+        default: return fail(PBF_ERR_INVALID_ARG, "unknown field");
+    }
+    return PBF_OK;
+}
+
+int pbf_scene_stream(pbf_scene* s, void** stream) {
+    if (!s || !stream) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *stream = (void*)s->stream;
+    return PBF_OK;
+}
+
+int pbf_solver_step_host(pbf_scene* s, int n, float* x3, float* v3, float* densities,
+                         float* lambdas, float dt, const float* g3, float mass) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    if (n == 0) return PBF_OK;  // pbf_solver.cpp:21
+    if (n < 0 || !x3 || !v3 || !densities || !lambdas || !g3)
+        return fail(PBF_ERR_INVALID_ARG, "NULL argument or negative n");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = set_state(s, n, x3, v3);
+    if (rc) return rc;
+    PBF_CUDA(cudaMemcpyAsync(s->B.rho, densities, (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(s->B.lam, lambdas, (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+    for (int d = 0; d < 3; ++d) s->gravity[d] = g3[d];
+    s->mass = mass;
+    rc = run_steps(s, dt, 1);
+    if (rc) return rc;
+    rc = download3(s, s->B.x, x3, n);
+    if (rc) return rc;
+    rc = download3(s, s->B.v, v3, n);
+    if (rc) return rc;
+    PBF_CUDA(cudaMemcpyAsync(densities, s->B.rho, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(lambdas, s->B.lam, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    return sync_and_check(s);
+}
+
+int pbf_scene_check_finite(pbf_scene* s) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    if (s->n == 0) return PBF_OK;
+    if (!s->d_flag) PBF_CUDA(cudaMalloc(&s->d_flag, 4));
+    PBF_CUDA(cudaMemsetAsync(s->d_flag, 0, 4, s->stream));
+    k_finite<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->B.x, s->B.v, s->n, s->d_flag);
+    PBF_CUDA(cudaGetLastError());
+    uint32_t f = 0;
+    PBF_CUDA(cudaMemcpyAsync(&f, s->d_flag, 4, cudaMemcpyDeviceToHost, s->stream));
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    if (f) return fail(PBF_ERR_NONFINITE, "non-finite particle position or velocity");
+    return PBF_OK;
+}
+
+int pbf_scene_debug_cells(pbf_scene* s, float dt, int* cells3) {
+    if (!s || (s->n > 0 && !cells3)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    if (s->n == 0) return PBF_OK;
+    StepConsts C;
+    int rc = make_consts(s, dt, C);
+    if (rc) return rc;
+    int* d = nullptr;
+    PBF_CUDA(cudaMalloc(&d, (size_t)s->n * 12));
+    cudaError_t e = debug_cells(s->B, C, d, s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(cells3, d, (size_t)s->n * 12, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "debug_cells");
+    return PBF_OK;
+}
+
+int pbf_scene_debug_neighbors(pbf_scene* s, float dt, long long* offsets, int* out_idx,
+                              long long cap, long long* total) {
+    if (!s || !offsets || !total) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    const int n = s->n;
+    *total = 0;
+    offsets[0] = 0;
+    if (n == 0) return PBF_OK;
+    StepConsts C;
+    int rc = make_consts(s, dt, C);
+    if (rc) return rc;
+    long long* d_cnt = nullptr;
+    long long* d_offs = nullptr;
+    int* d_out = nullptr;
+    std::vector<long long> cnt(n);
+    cudaError_t e = cudaMalloc(&d_cnt, (size_t)n * 8);
+    if (e == cudaSuccess) e = debug_neighbors(s->B, C, s->sort, d_cnt, nullptr, nullptr, 0, 0, s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(cnt.data(), d_cnt, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    long long tot = 0;
+    for (int i = 0; i < n; ++i) {
+        offsets[i] = tot;
+        tot += cnt[i];
+    }
+    offsets[n] = tot;
+    *total = tot;
+    if (e == cudaSuccess && out_idx && cap > 0) {
+        e = cudaMalloc(&d_offs, (size_t)(n + 1) * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&d_out, (size_t)std::max<long long>(cap, 1) * 4);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_offs, offsets, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = debug_neighbors(s->B, C, s->sort, nullptr, d_offs, d_out, cap, 1, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(out_idx, d_out, (size_t)std::min(cap, tot) * 4,
+                                cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    }
+    if (d_cnt) cudaFree(d_cnt);
+    if (d_offs) cudaFree(d_offs);
+    if (d_out) cudaFree(d_out);
+    if (e != cudaSuccess) return cuda_fail(e, "debug_neighbors");
+    // Canonical sets: ascending, duplicates (double-visited buckets) removed.
+    if (out_idx && cap >= tot) {
+        long long w = 0;
+        for (int i = 0; i < n; ++i) {
+            const long long a = offsets[i], b = offsets[i + 1];
+            std::sort(out_idx + a, out_idx + b);
+            const long long start = w;
+            for (long long k = a; k < b; ++k)
+                if (k == a || out_idx[k] != out_idx[k - 1]) out_idx[w++] = out_idx[k];
+            offsets[i] = start;
+        }
+        offsets[n] = w;
+        *total = w;
+    }
+    return sync_and_check(s);
+}
+
+const char* pbf_phase_name(int phase) {
+    // Scope names of the reference's PerformanceMonitor (pbf_solver.cpp:29-103).
+    static const char* names[kNumPhases] = {
+        "fluid.pbf.predict",
+        "fluid.pbf.grid_build",
+        "fluid.pbf.neighbor_query",
+        "fluid.pbf.iteration.compute_density",
+        "fluid.pbf.iteration.compute_delta_position",
+        "fluid.pbf.xsph_viscosity",
+        "fluid.pbf.commit_positions",
+    };
+    return (phase >= 0 && phase < kNumPhases) ? names[phase] : nullptr;
+}
+
+int pbf_scene_step_profiled(pbf_scene* s, float dt, float* phase_ms, int* launches) {
+    if (!s || !phase_ms) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    for (int k = 0; k < kNumPhases; ++k) {
+        phase_ms[k] = 0.0f;
+        if (launches) launches[k] = 0;
+    }
+    if (s->n == 0) return PBF_OK;
+    StepConsts C;
+    int rc = make_consts(s, dt, C);
+    if (rc) return rc;
+    PhaseMarks pm;
+    int created = 0;
+    cudaError_t e = cudaSuccess;
+    for (; created < PhaseMarks::kMax && e == cudaSuccess; ++created)
+        e = cudaEventCreate(&pm.ev[created]);
+    if (e == cudaSuccess) {
+        rc = enqueue(s, C, s->stream, &pm);
+        if (rc == PBF_OK) e = cudaStreamSynchronize(s->stream);
+        for (int k = 1; k < pm.count && e == cudaSuccess && rc == PBF_OK; ++k) {
+            float ms = 0.0f;
+            e = cudaEventElapsedTime(&ms, pm.ev[k - 1], pm.ev[k]);
+            const int ph = pm.phase[k];
+            if (ph >= 0 && ph < kNumPhases) {
+                phase_ms[ph] += ms;
+                if (launches) launches[ph] += pm.launches[k];
+            }
+        }
+    }
+    for (int k = 0; k < created; ++k)
+        if (pm.ev[k]) cudaEventDestroy(pm.ev[k]);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "pbf_scene_step_profiled");
+    return sync_and_check(s);
+}
+
+int pbf_sort_pairs_host(int device, int n, const unsigned* keys, int key_bits, unsigned* out_keys,
+                        unsigned* out_vals) {
+    if (n < 0 || (n > 0 && (!keys || !out_keys || !out_vals)))
+        return fail(PBF_ERR_INVALID_ARG, "bad arguments");
+    if (key_bits < 1 || key_bits > 32) return fail(PBF_ERR_INVALID_ARG, "key_bits in [1, 32]");
+    if (n == 0) return PBF_OK;
+    DeviceGuard dg(device);
+    if (!dg.ok) return fail(PBF_ERR_NO_DEVICE, "cudaSetDevice failed");
+    uint32_t *dk = nullptr, *dko = nullptr, *dvo = nullptr;
+    void* scratch = nullptr;
+    SortScratch ss;
+    cudaError_t e = cudaMalloc(&dk, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dko, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dvo, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&scratch, sort_scratch_bytes(n));
+    if (e == cudaSuccess) e = cudaMemset(scratch, 0, sort_scratch_bytes(n));
+    if (e == cudaSuccess) {
+        sort_scratch_bind(ss, scratch, n);
+        e = cudaMemcpy(dk, keys, (size_t)n * 4, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = radix_sort_pairs(dk, dko, dvo, n, key_bits, ss, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    uint32_t err = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&err, ss.err, 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_keys, dko, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_vals, dvo, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(dk);
+    cudaFree(dko);
+    cudaFree(dvo);
+    cudaFree(scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "pbf_sort_pairs_host");
+    if (err) return fail(PBF_ERR_TIMEOUT, "device-side wait in the sort gave up");
+    return PBF_OK;
+}
+
+}  // extern "C"

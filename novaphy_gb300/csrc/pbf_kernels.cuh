@@ -1,0 +1,687 @@
+// PBF step kernels.  This file is compiled twice:
+//   pbf_exact.cu: PBF_FAST=0, built with -fmad=false and IEEE div/sqrt, so
+//                 every expression below rounds exactly like the reference's
+//                 float code (pbf_solver.cpp, sph_kernel.h) term by term;
+//   pbf_fast.cu:  PBF_FAST=1, built with FMA contraction and rsqrt in the
+//                 spiky gradient.
+// Summation order is the reference's in both builds: for particle i the
+// candidates are visited bucket by bucket over the 27 neighbour cells in
+// (dz, dy, dx) order and, inside a bucket, by ascending particle index
+// (neighbor_search.cpp:14-22, :36-48).
+#pragma once
+
+#include <cstdint>
+
+#include "pbf_types.cuh"
+#include "radix_sort.cuh"
+
+#ifndef PBF_FAST
+#error "define PBF_FAST before including pbf_kernels.cuh"
+#endif
+#ifndef PBF_NS
+#error "define PBF_NS before including pbf_kernels.cuh"
+#endif
+
+namespace pbf {
+namespace PBF_NS {
+
+constexpr int kBlock = 128;
+constexpr uint32_t kNoBucket = 0xffffffffu;
+constexpr uint32_t kImpureBit = 0x80000000u;
+
+// ---------------------------------------------------------------------------
+// SPH kernels (include/novaphy/fluid/sph_kernel.h:24-46)
+
+// e0 + (e1 + e2): the 3-term reduction order of Vector3f::squaredNorm.
+__device__ __forceinline__ float sqn(float x, float y, float z) { return x * x + (y * y + z * z); }
+
+__device__ __forceinline__ float poly6(float r_sq, const StepConsts& C) {
+    if (r_sq >= C.h2) return 0.0f;
+    const float diff = C.h2 - r_sq;
+    return C.k_poly * diff * diff * diff;
+}
+
+// Spiky gradient of r (= x_i - x_j) given r_sq = sqn(r); returns the scalar
+// coefficient c so that grad = c * r (0 outside 1e-7 < |r| < h).
+__device__ __forceinline__ float spiky_coeff(float r_sq, const StepConsts& C) {
+#if PBF_FAST
+    if (r_sq >= C.h2 || r_sq <= 1e-14f) return 0.0f;
+    const float ir = rsqrtf(r_sq);
+    const float diff = C.h - r_sq * ir;
+    return C.k_spiky * diff * diff * ir;
+#else
+    const float r_len = sqrtf(r_sq);
+    if (r_len <= 1e-7f || r_len >= C.h) return 0.0f;
+    const float diff = C.h - r_len;
+    return C.k_spiky * diff * diff / r_len;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Grid helpers
+
+__device__ __forceinline__ int wrap(int c, int o, int g) {
+    int t = (c - o) % g;
+    return t < 0 ? t + g : t;
+}
+
+__device__ __forceinline__ uint32_t slot_of(int cx, int cy, int cz, const GridDesc& G) {
+    return (uint32_t)wrap(cx, G.ox, G.gx) +
+           (uint32_t)G.gx * ((uint32_t)wrap(cy, G.oy, G.gy) + (uint32_t)G.gy * (uint32_t)wrap(cz, G.oz, G.gz));
+}
+
+__device__ __forceinline__ bool in_grid(int cx, int cy, int cz, const GridDesc& G) {
+    return (unsigned)(cx - G.ox) < (unsigned)G.gx && (unsigned)(cy - G.oy) < (unsigned)G.gy &&
+           (unsigned)(cz - G.oz) < (unsigned)G.gz;
+}
+
+__device__ __forceinline__ void cell_of(float x, float y, float z, float inv, int& cx, int& cy,
+                                        int& cz) {
+    cx = (int)floorf(x * inv);
+    cy = (int)floorf(y * inv);
+    cz = (int)floorf(z * inv);
+}
+
+// Reference cell hash (neighbor_search.cpp:89-97).
+__device__ __forceinline__ unsigned long long ref_hash(int cx, int cy, int cz) {
+    return ((unsigned long long)(long long)cx * 73856093ULL) ^
+           ((unsigned long long)(long long)cy * 19349663ULL) ^
+           ((unsigned long long)(long long)cz * 83492791ULL);
+}
+
+// lower_bound over the sorted reference keys.
+__device__ __forceinline__ uint32_t key_lower_bound(const unsigned long long* __restrict__ keys,
+                                                    uint32_t n, unsigned long long k) {
+    uint32_t a = 0, b = n;
+    while (a < b) {
+        const uint32_t m = (a + b) >> 1;
+        if (__ldg(keys + m) < k) a = m + 1;
+        else b = m;
+    }
+    return a;
+}
+
+// Visits the candidate sorted positions q of a particle whose step-start cell
+// is `cell`, in the reference's order.
+//
+// cell.w == 0 (clean): every neighbour bucket holds exactly the particles of
+// that cell, so each (dz, dy) row of three cells is one contiguous range of
+// the cell-sorted order.  cell.w == o + 1 (dirty: a neighbour key is shared
+// with another occupied cell, or a slot holds wrapped aliases): the 27 bucket
+// starts are row o of `btab`; a bucket is the run [start, bend) of the
+// key-sorted order and kpos maps it back to cell-sorted positions.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const int4 cell, const uint32_t* __restrict__ off,
+                                                   const uint32_t* __restrict__ kpos,
+                                                   const uint32_t* __restrict__ bend,
+                                                   const uint32_t* __restrict__ btab,
+                                                   const StepConsts& C, F&& f) {
+    const GridDesc& G = C.grid;
+    if (cell.w == 0) {
+        for (int dz = -1; dz <= 1; ++dz) {
+            const uint32_t wz = (uint32_t)wrap(cell.z + dz, G.oz, G.gz);
+            for (int dy = -1; dy <= 1; ++dy) {
+                const uint32_t wy = (uint32_t)wrap(cell.y + dy, G.oy, G.gy);
+                const uint32_t row = (uint32_t)G.gx * (wy + (uint32_t)G.gy * wz);
+                const int wx = wrap(cell.x - 1, G.ox, G.gx);
+                if (wx + 2 < G.gx) {
+                    const uint32_t q1 = __ldg(off + row + wx + 3);
+                    for (uint32_t q = __ldg(off + row + wx); q < q1; ++q) f(q);
+                } else {
+                    for (int d = 0; d < 3; ++d) {
+                        const uint32_t s = row + (uint32_t)wrap(cell.x - 1 + d, G.ox, G.gx);
+                        const uint32_t q1 = __ldg(off + s + 1);
+                        for (uint32_t q = __ldg(off + s); q < q1; ++q) f(q);
+                    }
+                }
+            }
+        }
+    } else {
+        const uint32_t* row = btab + (size_t)(uint32_t)(cell.w - 1) * 27u;
+        for (int k = 0; k < 27; ++k) {
+            const uint32_t b0 = __ldg(row + k);
+            if (b0 == kNoBucket) continue;
+            const uint32_t b1 = __ldg(bend + b0) & ~kImpureBit;
+            for (uint32_t kq = b0; kq < b1; ++kq) f(__ldg(kpos + kq));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Grid construction kernels
+
+// v' = v + g dt;  x* = x + v' dt  (pbf_solver.cpp:31-32), rounded product
+// then sum in both builds so that cell assignment is bit-exact.
+__device__ __forceinline__ void predict(const float4 xi, const float4 vi, const StepConsts& C,
+                                        float& px, float& py, float& pz) {
+    const float vx = __fadd_rn(vi.x, __fmul_rn(C.g[0], C.dt));
+    const float vy = __fadd_rn(vi.y, __fmul_rn(C.g[1], C.dt));
+    const float vz = __fadd_rn(vi.z, __fmul_rn(C.g[2], C.dt));
+    px = __fadd_rn(xi.x, __fmul_rn(vx, C.dt));
+    py = __fadd_rn(xi.y, __fmul_rn(vy, C.dt));
+    pz = __fadd_rn(xi.z, __fmul_rn(vz, C.dt));
+}
+
+// Predict + cell slot and reference hash key per particle (particle order).
+__global__ void __launch_bounds__(kBlock)
+k_predict_key(const float4* __restrict__ x, const float4* __restrict__ v, uint32_t* __restrict__ keys,
+              unsigned long long* __restrict__ rkeys, const StepConsts C) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    float px, py, pz;
+    predict(x[i], v[i], C, px, py, pz);
+    int cx, cy, cz;
+    cell_of(px, py, pz, C.inv_cell, cx, cy, cz);
+    keys[i] = slot_of(cx, cy, cz, C.grid);
+    rkeys[i] = ref_hash(cx, cy, cz);
+}
+
+// off[s] = lower_bound(skeys, s) for s in [0, nslots].
+__global__ void __launch_bounds__(256)
+k_offsets(const uint32_t* __restrict__ skeys, int n, uint32_t* __restrict__ off, uint32_t nslots) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > nslots) return;
+    int a = 0, b = n;
+    while (a < b) {
+        const int m = (a + b) >> 1;
+        if (__ldg(skeys + m) < s) a = m + 1;
+        else b = m;
+    }
+    off[s] = (uint32_t)a;
+}
+
+// Gather particle state into cell-sorted order; recompute x* exactly as
+// predicted.  Records each particle's sorted position and flags slots that
+// receive a particle from outside the grid box (wrapped alias).
+__global__ void __launch_bounds__(kBlock)
+k_gather(const uint32_t* __restrict__ sidx, const float4* __restrict__ x, const float4* __restrict__ v,
+         const float* __restrict__ rho, const float* __restrict__ lam, float4* __restrict__ sx,
+         float4* __restrict__ xa, float* __restrict__ srho, int4* __restrict__ scell,
+         uint32_t* __restrict__ pos_of, unsigned char* __restrict__ slot_alias,
+         uint32_t* __restrict__ err, const StepConsts C) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= C.n) return;
+    uint32_t i = sidx[p];
+    if (i >= (uint32_t)C.n) {  // only after a failed sort; keep every access in range
+        atomicOr(err, 2u);
+        i = 0;
+    }
+    const float4 xi = x[i];
+    float px, py, pz;
+    predict(xi, v[i], C, px, py, pz);
+    int cx, cy, cz;
+    cell_of(px, py, pz, C.inv_cell, cx, cy, cz);
+    sx[p] = make_float4(xi.x, xi.y, xi.z, __uint_as_float(i));
+    xa[p] = make_float4(px, py, pz, lam[i]);
+    srho[p] = rho[i];
+    scell[p] = make_int4(cx, cy, cz, 0);
+    pos_of[i] = (uint32_t)p;
+    if (!in_grid(cx, cy, cz, C.grid)) slot_alias[slot_of(cx, cy, cz, C.grid)] = 1;
+}
+
+// Reference buckets in key-sorted order: kpos maps key-sorted positions to
+// cell-sorted ones; at each bucket start, bend holds the bucket end with
+// kImpureBit set when the bucket mixes cells (hash collision).
+__global__ void __launch_bounds__(256)
+k_buckets(const unsigned long long* __restrict__ rsorted, const uint32_t* __restrict__ ridx,
+          const uint32_t* __restrict__ pos_of, const int4* __restrict__ scell,
+          uint32_t* __restrict__ kpos, uint32_t* __restrict__ bend, int n) {
+    const int kp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kp >= n) return;
+    const uint32_t i0 = ridx[kp];
+    uint32_t p0 = pos_of[i0 < (uint32_t)n ? i0 : 0];
+    if (p0 >= (uint32_t)n) p0 = 0;
+    kpos[kp] = p0;
+    const unsigned long long k = rsorted[kp];
+    if (kp > 0 && rsorted[kp - 1] == k) return;
+    const int4 c0 = scell[p0];
+    bool pure = true;
+    int e = kp + 1;
+    while (e < n && rsorted[e] == k) {
+        if (pure) {
+            const uint32_t ie = ridx[e];
+            uint32_t pe = pos_of[ie < (uint32_t)n ? ie : 0];
+            if (pe >= (uint32_t)n) pe = 0;
+            const int4 ce = scell[pe];
+            if (ce.x != c0.x || ce.y != c0.y || ce.z != c0.z) pure = false;
+        }
+        ++e;
+    }
+    bend[kp] = (uint32_t)e | (pure ? 0u : kImpureBit);
+}
+
+// Marks particles whose neighbourhood differs from the reference's buckets
+// (sown[p] = owner + 1, else 0) and stores their 27 bucket starts in row
+// `owner` of btab.  Within a warp, one lane per distinct
+// cell does the 27 lookups; the other lanes of the cell reuse its table row.
+__global__ void __launch_bounds__(kBlock)
+k_classify(const int4* __restrict__ scell, const unsigned long long* __restrict__ rsorted,
+           const uint32_t* __restrict__ kpos, const uint32_t* __restrict__ bend,
+           const unsigned char* __restrict__ slot_alias, uint32_t* __restrict__ btab,
+           int* __restrict__ sown, const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = p < (uint32_t)C.n;
+    const int lane = threadIdx.x & 31;
+    const int4 cell = active ? scell[p] : make_int4(0x7fffffff, 0x7fffffff, 0x7fffffff, 0);
+    const unsigned long long kxy =
+        ((unsigned long long)(unsigned)cell.x << 32) | (unsigned long long)(unsigned)cell.y;
+    const uint32_t same = __match_any_sync(0xffffffffu, kxy) &
+                          __match_any_sync(0xffffffffu, (unsigned)cell.z) &
+                          __ballot_sync(0xffffffffu, active);
+    const int leader = same ? __ffs(same) - 1 : lane;
+    int dirty = 0;
+    if (active && lane == leader) {
+        uint32_t tab[27];
+        int m = 0;
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx, ++m) {
+                    const int nx = cell.x + dx, ny = cell.y + dy, nz = cell.z + dz;
+                    const unsigned long long k = ref_hash(nx, ny, nz);
+                    const uint32_t lb = key_lower_bound(rsorted, (uint32_t)C.n, k);
+                    if (lb < (uint32_t)C.n && __ldg(rsorted + lb) == k) {
+                        tab[m] = lb;
+                        const uint32_t e = __ldg(bend + lb);
+                        const int4 c0 = scell[__ldg(kpos + lb)];
+                        if ((e & kImpureBit) || c0.x != nx || c0.y != ny || c0.z != nz) dirty = 1;
+                    } else {
+                        tab[m] = kNoBucket;
+                    }
+                    if (slot_alias[slot_of(nx, ny, nz, C.grid)]) dirty = 1;
+                }
+        if (dirty) {
+            uint32_t* row = btab + (size_t)p * 27u;
+            for (int k = 0; k < 27; ++k) row[k] = tab[k];
+        }
+    }
+    const int d = __shfl_sync(0xffffffffu, dirty, leader);
+    const uint32_t owner = __shfl_sync(0xffffffffu, p, leader);
+    if (active) sown[p] = d ? (int)(owner + 1u) : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Constraint and velocity kernels (one thread per cell-sorted particle)
+
+struct Grid {
+    const int4* __restrict__ scell;
+    const int* __restrict__ sown;
+    const uint32_t* __restrict__ off;
+    const uint32_t* __restrict__ kpos;
+    const uint32_t* __restrict__ bend;
+    const uint32_t* __restrict__ btab;
+};
+
+__device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
+    int4 c = G.scell[p];
+    c.w = G.sown[p];
+    return c;
+}
+
+// compute_density + compute_lambda (pbf_solver.cpp:129-179) in one candidate
+// pass.  Reads x* from xin, writes (x*, lambda) to xout and rho to srho.
+__global__ void __launch_bounds__(kBlock)
+k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
+                 const Grid G, const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)C.n) return;
+    const float4 xi = xin[p];
+    float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
+    for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+        const float4 xj = __ldg(xin + q);
+        const float rx = xi.x - xj.x;
+        const float ry = xi.y - xj.y;
+        const float rz = xi.z - xj.z;
+        const float r_sq = sqn(rx, ry, rz);
+        if (r_sq < C.cut) {
+            density += C.mass * poly6(r_sq, C);
+            if (q != p) {
+                const float c = spiky_coeff(r_sq, C);
+                const float gx = C.mr * (c * rx);
+                const float gy = C.mr * (c * ry);
+                const float gz = C.mr * (c * rz);
+                sum_grad_sq += sqn(gx, gy, gz);
+                gix += gx;
+                giy += gy;
+                giz += gz;
+            }
+        }
+    });
+    sum_grad_sq += sqn(gix, giy, giz);
+    const float Ci = density * C.inv_rho0 - 1.0f;
+    const float lam = (Ci < 0.0f) ? 0.0f : -Ci / (sum_grad_sq + C.eps);
+    srho[p] = density;
+    xout[p] = make_float4(xi.x, xi.y, xi.z, lam);
+}
+
+// Velocity update with speed clamp (pbf_solver.cpp:81-93) for sorted p; w is
+// the XSPH weight m / rho' (pbf_solver.cpp:240-241).
+__device__ __forceinline__ float4 update_velocity(float px, float py, float pz, const float4 x0,
+                                                  float rho, const StepConsts& C) {
+    float a = (px - x0.x) * C.inv_dt;
+    float b = (py - x0.y) * C.inv_dt;
+    float c = (pz - x0.z) * C.inv_dt;
+    const float speed_sq = sqn(a, b, c);
+    if (speed_sq > C.max_speed_sq) {
+        const float s = C.max_speed / sqrtf(speed_sq);
+        a *= s;
+        b *= s;
+        c *= s;
+    }
+    const float rho_j = (rho > 1e-6f) ? rho : C.rho0;
+    return make_float4(a, b, c, C.mass / rho_j);
+}
+
+// compute_delta_position + apply_delta (pbf_solver.cpp:181-223, :74-76).
+// Reads (x*, lambda) from xin, writes (x* + dp, lambda_i) to xout; on the last
+// iteration also the updated velocity into sv.
+__global__ void __launch_bounds__(kBlock)
+k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
+        const float* __restrict__ srho, float4* __restrict__ sv, int last, const Grid G,
+        const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)C.n) return;
+    const float4 xi = xin[p];
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+    for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+        if (q == p) return;
+        const float4 xj = __ldg(xin + q);
+        const float rx = xi.x - xj.x;
+        const float ry = xi.y - xj.y;
+        const float rz = xi.z - xj.z;
+        const float r_sq = sqn(rx, ry, rz);
+        if (r_sq < C.cut) {
+            const float lambda_sum = xi.w + xj.w;
+            float s_corr = 0.0f;
+            if (lambda_sum < -1e-10f && C.scorr_on) {
+                float ratio = poly6(r_sq, C) / C.w_dq;
+                ratio = (1.0f < ratio) ? 1.0f : ratio;
+                float rp = ratio * ratio;
+                if (C.corr_n4) rp = rp * rp;
+                s_corr = C.neg_corr_k * rp;
+            }
+            const float c = spiky_coeff(r_sq, C);
+            const float a = (lambda_sum + s_corr) * C.mass;
+            dx += a * (c * rx);
+            dy += a * (c * ry);
+            dz += a * (c * rz);
+        }
+    });
+    const float px = xi.x + dx * C.inv_rho0;
+    const float py = xi.y + dy * C.inv_rho0;
+    const float pz = xi.z + dz * C.inv_rho0;
+    xout[p] = make_float4(px, py, pz, xi.w);
+    if (last) sv[p] = update_velocity(px, py, pz, sx[p], srho[p], C);
+}
+
+// Velocity update alone, for solver_iterations == 0.
+__global__ void __launch_bounds__(kBlock)
+k_velocity(const float4* __restrict__ xin, const float4* __restrict__ sx, const float* __restrict__ srho,
+           float4* __restrict__ sv, const StepConsts C) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= C.n) return;
+    const float4 xi = xin[p];
+    sv[p] = update_velocity(xi.x, xi.y, xi.z, sx[p], srho[p], C);
+}
+
+// Domain clamp + commit (pbf_solver.cpp:102-126), scattered to particle order.
+__device__ __forceinline__ void commit(uint32_t p, float px, float py, float pz, float vx, float vy,
+                                       float vz, float lam, const float4* __restrict__ sx,
+                                       const float* __restrict__ srho, float4* __restrict__ x,
+                                       float4* __restrict__ v, float* __restrict__ rho,
+                                       float* __restrict__ lamo, const StepConsts& C) {
+    if (C.clamp) {
+        if (px < C.lo[0]) { px = C.lo[0]; vx = 0.0f; } else if (px > C.hi[0]) { px = C.hi[0]; vx = 0.0f; }
+        if (py < C.lo[1]) { py = C.lo[1]; vy = 0.0f; } else if (py > C.hi[1]) { py = C.hi[1]; vy = 0.0f; }
+        if (pz < C.lo[2]) { pz = C.lo[2]; vz = 0.0f; } else if (pz > C.hi[2]) { pz = C.hi[2]; vz = 0.0f; }
+    }
+    uint32_t i = __float_as_uint(sx[p].w);
+    if (i >= (uint32_t)C.n) i = 0;
+    x[i] = make_float4(px, py, pz, 0.0f);
+    v[i] = make_float4(vx, vy, vz, 0.0f);
+    rho[i] = srho[p];
+    lamo[i] = lam;
+}
+
+// apply_xsph_viscosity (pbf_solver.cpp:225-250) + commit, no vorticity.
+__global__ void __launch_bounds__(kBlock)
+k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, const float4* __restrict__ sx,
+              const float* __restrict__ srho, float4* __restrict__ x, float4* __restrict__ v,
+              float* __restrict__ rho, float* __restrict__ lam, const Grid G, const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)C.n) return;
+    const float4 xi = xin[p];
+    const float4 vi = sv[p];
+    float vx = vi.x, vy = vi.y, vz = vi.z;
+    if (C.xsph_on) {
+        float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+        for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+            if (q == p) return;
+            const float4 xj = __ldg(xin + q);
+            const float rx = xi.x - xj.x;
+            const float ry = xi.y - xj.y;
+            const float rz = xi.z - xj.z;
+            const float r_sq = sqn(rx, ry, rz);
+            if (r_sq < C.h2) {
+                const float4 vj = __ldg(sv + q);
+                const float w = poly6(r_sq, C);
+                cx += vj.w * (vj.x - vi.x) * w;
+                cy += vj.w * (vj.y - vi.y) * w;
+                cz += vj.w * (vj.z - vi.z) * w;
+            }
+        });
+        vx = vi.x + C.xsph_c * cx;
+        vy = vi.y + C.xsph_c * cy;
+        vz = vi.z + C.xsph_c * cz;
+    }
+    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, x, v, rho, lam, C);
+}
+
+// XSPH correction + vorticity omega in one candidate pass (vorticity path).
+// Writes the post-XSPH velocity to sv2 and (omega, |omega|) to som, with
+//   omega_i = sum_j (m/rho_j') spiky_grad(x*_i - x*_j) x (v_j - v_i),
+// the SPH curl (Macklin & Mueller 2013, section 5, with its volume factor).
+__global__ void __launch_bounds__(kBlock)
+k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, float4* __restrict__ sv2,
+             float4* __restrict__ som, const Grid G, const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)C.n) return;
+    const float4 xi = xin[p];
+    const float4 vi = sv[p];
+    float cx = 0.0f, cy = 0.0f, cz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
+    for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+        if (q == p) return;
+        const float4 xj = __ldg(xin + q);
+        const float rx = xi.x - xj.x;
+        const float ry = xi.y - xj.y;
+        const float rz = xi.z - xj.z;
+        const float r_sq = sqn(rx, ry, rz);
+        if (r_sq < C.cut) {
+            const float4 vj = __ldg(sv + q);
+            const float ux = vj.x - vi.x;
+            const float uy = vj.y - vi.y;
+            const float uz = vj.z - vi.z;
+            const float w = poly6(r_sq, C);
+            cx += vj.w * ux * w;
+            cy += vj.w * uy * w;
+            cz += vj.w * uz * w;
+            const float c = spiky_coeff(r_sq, C);
+            const float gx = c * rx, gy = c * ry, gz = c * rz;
+            wx += vj.w * (gy * uz - gz * uy);
+            wy += vj.w * (gz * ux - gx * uz);
+            wz += vj.w * (gx * uy - gy * ux);
+        }
+    });
+    float vx = vi.x, vy = vi.y, vz = vi.z;
+    if (C.xsph_on) {
+        vx = vi.x + C.xsph_c * cx;
+        vy = vi.y + C.xsph_c * cy;
+        vz = vi.z + C.xsph_c * cz;
+    }
+    sv2[p] = make_float4(vx, vy, vz, 0.0f);
+    som[p] = make_float4(wx, wy, wz, sqrtf(sqn(wx, wy, wz)));
+}
+
+// Vorticity confinement (Macklin & Mueller 2013, section 5) + commit:
+//   eta_i = sum_j (m/rho_j') (|omega_j| - |omega_i|) spiky_grad(x*_i - x*_j),
+//   N = eta / |eta|,  v += dt * eps * (N x omega_i).
+__global__ void __launch_bounds__(kBlock)
+k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv,
+                   const float4* __restrict__ sv2, const float4* __restrict__ som,
+                   const float4* __restrict__ sx, const float* __restrict__ srho,
+                   float4* __restrict__ x, float4* __restrict__ v, float* __restrict__ rho,
+                   float* __restrict__ lam, const Grid G, const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)C.n) return;
+    const float4 xi = xin[p];
+    const float4 wi = som[p];
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+    for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+        if (q == p) return;
+        const float4 xj = __ldg(xin + q);
+        const float rx = xi.x - xj.x;
+        const float ry = xi.y - xj.y;
+        const float rz = xi.z - xj.z;
+        const float r_sq = sqn(rx, ry, rz);
+        if (r_sq < C.cut) {
+            const float c = spiky_coeff(r_sq, C);
+            const float a = __ldg(sv + q).w * (__ldg(som + q).w - wi.w);
+            ex += a * (c * rx);
+            ey += a * (c * ry);
+            ez += a * (c * rz);
+        }
+    });
+    const float el = sqrtf(sqn(ex, ey, ez));
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (el > 1e-9f) {
+        nx = ex / el;
+        ny = ey / el;
+        nz = ez / el;
+    }
+    const float fx = ny * wi.z - nz * wi.y;
+    const float fy = nz * wi.x - nx * wi.z;
+    const float fz = nx * wi.y - ny * wi.x;
+    const float4 vb = sv2[p];
+    const float vx = vb.x + C.vort_scale * fx;
+    const float vy = vb.y + C.vort_scale * fy;
+    const float vz = vb.z + C.vort_scale * fz;
+    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, x, v, rho, lam, C);
+}
+
+// ---------------------------------------------------------------------------
+// Parity probes: cell coordinates and in-radius neighbour lists of x*.
+
+__global__ void __launch_bounds__(kBlock)
+k_debug_cells(const float4* __restrict__ x, const float4* __restrict__ v, int* __restrict__ cells3,
+              const StepConsts C) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    float px, py, pz;
+    predict(x[i], v[i], C, px, py, pz);
+    int cx, cy, cz;
+    cell_of(px, py, pz, C.inv_cell, cx, cy, cz);
+    cells3[3 * i] = cx;
+    cells3[3 * i + 1] = cy;
+    cells3[3 * i + 2] = cz;
+}
+
+// fill == 0: cnt[i] = number of in-radius candidates j != i of particle i;
+// fill == 1: write them (particle indices, candidate order) at out[offs[i]..].
+__global__ void __launch_bounds__(kBlock)
+k_debug_neighbors(const float4* __restrict__ xin, const float4* __restrict__ sx,
+                  long long* __restrict__ cnt, const long long* __restrict__ offs,
+                  int* __restrict__ out, long long cap, int fill, const Grid G,
+                  const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)C.n) return;
+    const float4 xi = xin[p];
+    const uint32_t i = __float_as_uint(sx[p].w);
+    long long k = fill ? offs[i] : 0;
+    for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+        if (q == p) return;
+        const float4 xj = xin[q];
+        if (sqn(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) < C.h2) {
+            if (fill && k < cap) out[k] = (int)__float_as_uint(sx[q].w);
+            ++k;
+        }
+    });
+    if (!fill) cnt[i] = k;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers on `stream`.
+
+inline int grid_of(int n, int b) { return (n + b - 1) / b; }
+
+inline Grid grid_view(const StepBuffers& B) {
+    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab};
+}
+
+// predict, sort by cell and by reference key, cell offsets, gather, reference
+// buckets, classification: the neighbour structure of the step.
+inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, SortScratch& sort,
+                                  cudaStream_t st, PhaseMarks* pm = nullptr) {
+    const int n = C.n;
+    const int nb = grid_of(n, kBlock);
+    cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)C.grid.nslots, st);
+    if (e != cudaSuccess) return e;
+    if (pm) pm->mark(-1, 0, st);
+    k_predict_key<<<nb, kBlock, 0, st>>>(B.x, B.v, B.keys, B.rkeys, C);
+    if (pm) pm->mark(kPhasePredict, 1, st);
+    e = radix_sort_pairs(B.keys, B.skeys, B.sidx, n, C.grid.key_bits, sort, st);
+    if (e != cudaSuccess) return e;
+    int launches = 2 + (C.grid.key_bits + 7) / 8;
+    if (C.hash_compat) {
+        e = radix_sort_pairs64(B.rkeys, B.rsorted, B.ridx, n, 64, sort, st);
+        if (e != cudaSuccess) return e;
+        launches += 9;
+    }
+    k_offsets<<<grid_of((int)C.grid.nslots + 1, 256), 256, 0, st>>>(B.skeys, n, B.off, C.grid.nslots);
+    if (pm) pm->mark(kPhaseGridBuild, launches, st);
+    k_gather<<<nb, kBlock, 0, st>>>(B.sidx, B.x, B.v, B.rho, B.lam, B.sx, B.xa, B.srho, B.scell,
+                                    B.pos_of, B.slot_alias, B.err, C);
+    if (C.hash_compat) {
+        k_buckets<<<grid_of(n, 256), 256, 0, st>>>(B.rsorted, B.ridx, B.pos_of, B.scell, B.kpos,
+                                                   B.bend, n);
+        k_classify<<<nb, kBlock, 0, st>>>(B.scell, B.rsorted, B.kpos, B.bend, B.slot_alias, B.btab,
+                                          B.sown, C);
+    } else {
+        e = cudaMemsetAsync(B.sown, 0, (size_t)n * 4, st);
+        if (e != cudaSuccess) return e;
+    }
+    if (pm) pm->mark(kPhaseNeighborQuery, C.hash_compat ? 3 : 1, st);
+    return cudaGetLastError();
+}
+
+inline cudaError_t enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
+                                SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr) {
+    const int n = C.n;
+    if (n <= 0) return cudaSuccess;
+    const int nb = grid_of(n, kBlock);
+    const Grid G = grid_view(B);
+    cudaError_t e = enqueue_prefix(B, C, sort, st, pm);
+    if (e != cudaSuccess) return e;
+    for (int it = 0; it < iters; ++it) {
+        k_density_lambda<<<nb, kBlock, 0, st>>>(B.xa, B.xb, B.srho, G, C);
+        if (pm) pm->mark(kPhaseDensity, 1, st);
+        k_delta<<<nb, kBlock, 0, st>>>(B.xb, B.xa, B.sx, B.srho, B.sv, it == iters - 1 ? 1 : 0, G, C);
+        if (pm) pm->mark(kPhaseDelta, 1, st);
+    }
+    if (iters <= 0) {
+        k_velocity<<<nb, kBlock, 0, st>>>(B.xa, B.sx, B.srho, B.sv, C);
+        if (pm) pm->mark(kPhaseDelta, 1, st);
+    }
+    if (C.vort_on) {
+        k_xsph_omega<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, G, C);
+        if (pm) pm->mark(kPhaseXsph, 1, st);
+        k_vorticity_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, B.sx, B.srho, B.x, B.v,
+                                                  B.rho, B.lam, G, C);
+        if (pm) pm->mark(kPhaseCommit, 1, st);
+    } else {
+        k_xsph_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sx, B.srho, B.x, B.v, B.rho, B.lam, G, C);
+        if (pm) pm->mark(C.xsph_on ? kPhaseXsph : kPhaseCommit, 1, st);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace PBF_NS
+}  // namespace pbf

@@ -1,0 +1,21 @@
+// Entry points of the two kernel builds (pbf_exact.cu, pbf_fast.cu).
+#pragma once
+
+#include "pbf_types.cuh"
+#include "radix_sort.cuh"
+
+namespace pbf {
+
+cudaError_t exact_enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
+                               SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr);
+cudaError_t fast_enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
+                              SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr);
+
+// Parity probes (exact build).
+cudaError_t debug_cells(const StepBuffers& B, const StepConsts& C, int* d_cells3,
+                        cudaStream_t st);
+cudaError_t debug_neighbors(const StepBuffers& B, const StepConsts& C, SortScratch& sort,
+                            long long* d_cnt, const long long* d_offs, int* d_out, long long cap,
+                            int fill, cudaStream_t st);
+
+}  // namespace pbf

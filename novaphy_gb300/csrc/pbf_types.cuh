@@ -1,0 +1,123 @@
+// Plain data shared by the host orchestration and both kernel builds.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace pbf {
+
+// Neighbour grid: cell = h, coordinates floor(x * inv_cell) as in
+// SpatialHashGrid::world_to_cell (neighbor_search.cpp:99-105).  Cell (cx,cy,cz)
+// lives in slot  wrap(cx-ox) + gx * (wrap(cy-oy) + gy * wrap(cz-oz)),  each
+// axis wrapped modulo its extent (>= 4).  Wrapping never merges two cells of
+// one 27-neighbourhood, and a wrapped alias is >= 3 cells away, beyond the
+// kernel support, so it only adds exact zeros: any origin/extent is correct,
+// and a good fit only saves work.
+struct GridDesc {
+    int ox, oy, oz;
+    int gx, gy, gz;
+    uint32_t nslots;
+    int key_bits;
+};
+
+// Per-step constants, all computed on the host in float32 with the
+// reference's operation order (pbf_solver.cpp, sph_kernel.h).
+struct StepConsts {
+    int n;
+    float h;         // kernel radius
+    float h2;        // h * h                         (sph_kernel.h:25-26)
+    float cut;       // smallest r^2 with poly6 == 0 and spiky_grad == 0
+    float inv_cell;  // 1.0f / h                      (neighbor_search.cpp:101)
+    float mass;
+    float rho0;
+    float inv_rho0;  // 1.0f / rho0                   (pbf_solver.cpp:149)
+    float eps;       // CFM epsilon
+    float mr;        // mass * inv_rho0               (pbf_solver.cpp:170)
+    float k_poly;    // 315 / (64 pi h^9)             (sph_kernel.h:29)
+    float k_spiky;   // -(45 / (pi h^6))              (sph_kernel.h:44)
+    float w_dq;      // poly6((dq h)^2, h)            (pbf_solver.cpp:188-189)
+    float neg_corr_k;
+    int corr_n4;     // corr_n == 4
+    int scorr_on;    // w_dq > 1e-10
+    float dt, inv_dt, max_speed, max_speed_sq;  // (pbf_solver.cpp:81-83)
+    float g[3];
+    float xsph_c;
+    int xsph_on;     // xsph_viscosity > 0            (pbf_solver.cpp:96)
+    float vort_eps;
+    float vort_scale;  // dt * vort_eps
+    int vort_on;
+    int clamp;
+    float lo[3], hi[3];  // domain_lower + pr, domain_upper - pr (pbf_solver.cpp:105-107)
+    int hash_compat;
+    GridDesc grid;
+};
+
+// Device buffers of one step.  Arrays named s* are in sorted (cell) order.
+struct StepBuffers {
+    float4* x;      // positions, particle order (w unused)
+    float4* v;      // velocities, particle order
+    float* rho;     // densities, particle order
+    float* lam;     // lambdas, particle order
+    uint32_t* keys;   // slot per particle, particle order
+    uint32_t* skeys;  // sorted slots
+    uint32_t* sidx;   // particle index of sorted position p
+    uint32_t* off;    // off[s] = first sorted position with slot >= s; nslots+1 entries
+    float4* sx;     // x (w = particle index bits)
+    float4* xa;     // x* ping (w = lambda)
+    float4* xb;     // x* pong
+    float4* sv;     // post-update velocity (w = m / rho')
+    float4* sv2;    // post-XSPH velocity (vorticity path)
+    float4* som;    // vorticity omega (w = |omega|)
+    float* srho;    // densities of the last density pass
+    int4* scell;    // cell of x* at step start
+    // Reference hash buckets (neighbor_search.cpp:14-22) for exact candidate
+    // lists where they differ from the plain 27-cell neighbourhood.
+    unsigned long long* rkeys;    // reference key per particle, particle order
+    unsigned long long* rsorted;  // keys sorted (stable)
+    uint32_t* ridx;      // particle of key-sorted position
+    uint32_t* pos_of;    // cell-sorted position of each particle
+    uint32_t* kpos;      // cell-sorted position of each key-sorted position
+    uint32_t* bend;      // at bucket starts: bucket end | impure bit
+    uint32_t* btab;      // 27 bucket starts per dirty owner row
+    int* sown;           // 0 = clean, else owner row + 1
+    unsigned char* slot_alias;  // slot holds a particle from outside the grid box
+    uint32_t* err;  // device status word
+};
+
+// Phases of one step, named after the reference's PerformanceMonitor scopes
+// (pbf_solver.cpp:29-103).  Fused kernels report under the first scope they
+// cover: density+lambda under compute_density, delta+apply(+velocity update
+// on the last iteration) under compute_delta_position, XSPH(+vorticity omega)
+// under xsph_viscosity, vorticity confinement + clamp + commit under
+// commit_positions.
+enum StepPhase {
+    kPhasePredict = 0,
+    kPhaseGridBuild = 1,
+    kPhaseNeighborQuery = 2,
+    kPhaseDensity = 3,
+    kPhaseDelta = 4,
+    kPhaseXsph = 5,
+    kPhaseCommit = 6,
+    kNumPhases = 7
+};
+
+// Event marks between the launches of one step (profiling only).
+struct PhaseMarks {
+    static constexpr int kMax = 96;
+    cudaEvent_t ev[kMax];
+    int phase[kMax];
+    int launches[kMax];
+    int count = 0;
+    // Records the end of a phase that launched `nl` kernels.
+    void mark(int ph, int nl, cudaStream_t st) {
+        if (count < kMax) {
+            cudaEventRecord(ev[count], st);
+            phase[count] = ph;
+            launches[count] = nl;
+            ++count;
+        }
+    }
+};
+
+}  // namespace pbf

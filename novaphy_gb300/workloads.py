@@ -1,0 +1,87 @@
+"""Seeded synthetic dam-break workloads of the PBF step.
+
+All inputs are synthetic (no dataset is involved): a cubic lattice, x
+fastest then y then z like generate_fluid_block (src/fluid/particle_state.cpp:
+31-58), plus uniform jitter from ``numpy.random.default_rng(seed)``; float32
+throughout so every consumer sees identical bytes.
+
+* ``dam_break_8k``  - 20^3 particles, r = 0.025 m, box [0,1]^3, h = 4r,
+  4 iterations, dt = 1/120 s (the reference CPU-runnable case).
+* ``dam_break_1m``  - 100^3 particles, r = 0.01 m, box [0,4]x[0,2]x[0,2],
+  h = 4r, 4 iterations, dt = 1/240 s (the single-GPU throughput case).
+
+Common parameters: rest density 1000, mass rho0 r^3, gravity -9.81 z,
+s_corr k = 0.1, n = 4, dq = 0.2 h, XSPH c = 0.01, vorticity eps = 1e-4,
+domain clamp on with particle_radius = r/2, block lower corner at r/2 per
+axis so that the initial state is inside the clamp.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Workload:
+    name: str
+    x: np.ndarray            # (n, 3) float32
+    v: np.ndarray            # (n, 3) float32
+    settings: dict           # PBFSettings fields (+ extensions)
+    dt: float
+    gravity: np.ndarray      # (3,) float32
+    mass: float
+    steps: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return len(self.x)
+
+
+def lattice(counts, spacing, lower) -> np.ndarray:
+    """generate_fluid_block order: x fastest; coordinates lower + i * spacing in float32."""
+    nx, ny, nz = counts
+    sp = np.float32(spacing)
+    lo = np.asarray(lower, np.float32)
+    iz, iy, ix = np.meshgrid(np.arange(nz, dtype=np.float32), np.arange(ny, dtype=np.float32),
+                             np.arange(nx, dtype=np.float32), indexing="ij")
+    pts = np.stack([lo[0] + ix.ravel() * sp, lo[1] + iy.ravel() * sp, lo[2] + iz.ravel() * sp],
+                   axis=1)
+    return np.ascontiguousarray(pts.astype(np.float32))
+
+
+def dam_break(counts, r, box_upper, h_factor=4.0, iterations=4, dt=1.0 / 120.0, jitter=1e-4,
+              seed=0, vorticity=1e-4, steps=120, name="dam_break") -> Workload:
+    rng = np.random.default_rng(seed)
+    lower = np.full(3, r / 2, np.float32)
+    x = lattice(counts, r, lower)
+    x = (x + rng.uniform(-jitter, jitter, x.shape)).astype(np.float32)
+    h = np.float32(h_factor * r)
+    settings = dict(
+        rest_density=1000.0, kernel_radius=float(h), particle_radius=float(np.float32(r / 2)),
+        solver_iterations=iterations, epsilon=100.0, xsph_viscosity=0.01,
+        vorticity_epsilon=vorticity, corr_delta_q=0.2, corr_k=0.1, corr_n=4,
+        use_domain_bounds=1, domain_lower=(0.0, 0.0, 0.0), domain_upper=tuple(box_upper),
+    )
+    mass = float(np.float32(1000.0) * np.float32(r) ** 3)
+    return Workload(name=name, x=x, v=np.zeros_like(x), settings=settings, dt=float(np.float32(dt)),
+                    gravity=np.array([0.0, 0.0, -9.81], np.float32), mass=mass, steps=steps,
+                    meta=dict(r=r, counts=tuple(counts), box=tuple(box_upper), seed=seed,
+                              jitter=jitter))
+
+
+def dam_break_8k(vorticity=1e-4) -> Workload:
+    return dam_break((20, 20, 20), 0.025, (1.0, 1.0, 1.0), dt=1.0 / 120.0, jitter=1e-4, seed=0,
+                     vorticity=vorticity, steps=120, name="dam_break_8k")
+
+
+def dam_break_1m(vorticity=1e-4) -> Workload:
+    return dam_break((100, 100, 100), 0.01, (4.0, 2.0, 2.0), dt=1.0 / 240.0, jitter=1e-5, seed=1,
+                     vorticity=vorticity, steps=200, name="dam_break_1m")
+
+
+def scaled_dam_break(counts, vorticity=1e-4, seed=1) -> Workload:
+    """A block of `counts` at the 1M case's density and box (same per-particle work)."""
+    return dam_break(counts, 0.01, (4.0, 2.0, 2.0), dt=1.0 / 240.0, jitter=1e-5, seed=seed,
+                     vorticity=vorticity, steps=200, name=f"dam_break_{np.prod(counts)}")

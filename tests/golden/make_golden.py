@@ -1,0 +1,130 @@
+"""Generates the golden fixtures in this directory from the reference itself.
+
+The reference's own PBF sources (src/fluid/*.cpp) are compiled by
+oracle/build_oracle.py into oracle/_ref and run here on seeded synthetic
+inputs; their outputs become the fixtures.  The script also checks that the
+oracle restatement (oracle/pbf_oracle.c) reproduces every fixture bit for
+bit, so the fixtures pin the restatement.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from novaphy_gb300 import workloads  # noqa: E402
+from oracle.oracle import Port, Ref, Settings  # noqa: E402
+
+
+def digest(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, np.float32).tobytes())
+    return h.hexdigest()
+
+
+def small_block(seed=0):
+    """10^3 lattice at r = 0.025 in [0,1]^3, dam-break parameters, no vorticity."""
+    return workloads.dam_break((10, 10, 10), 0.025, (1.0, 1.0, 1.0), dt=1.0 / 120.0, jitter=1e-4,
+                               seed=seed, vorticity=0.0, name="block_1k")
+
+
+def default_scene():
+    """The reference tests' PBF scene: 0.3 m block at spacing 0.025, h = 0.1,
+    PBFSettings defaults otherwise (no domain clamp), gravity -9.81 y,
+    dt = 1/60 (tests/python/test_pbf.py:28-49)."""
+    x = workloads.lattice((13, 13, 13), 0.025, (0.0, 0.0, 0.0))
+    s = Settings.make(kernel_radius=0.1, solver_iterations=4, epsilon=100.0)
+    return x, s, np.float32(1.0 / 60.0), np.array([0, -9.81, 0], np.float32), \
+        np.float32(1000.0) * np.float32(0.025) ** 3
+
+
+def main():
+    P, R = Port(), Ref()
+    out = {}
+
+    # --- SPH kernels on a sweep of radii, two kernel radii.
+    ker = {}
+    for h in (0.1, 0.04):
+        hf = np.float32(h)
+        r = np.linspace(0.0, 1.2 * h, 97, dtype=np.float32)
+        ker[f"r_{h}"] = r
+        ker[f"poly6_{h}"] = np.array([R.poly6(t * t, hf) for t in r], np.float32)
+        ker[f"spiky_{h}"] = np.array([R.spiky(t, hf) for t in r], np.float32)
+        ker[f"cubic_{h}"] = np.array([R.cubic_spline(t, hf) for t in r], np.float32)
+        dirs = np.random.default_rng(7).normal(size=(97, 3)).astype(np.float32)
+        dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+        vec = (dirs * r[:, None]).astype(np.float32)
+        ker[f"gradvec_{h}"] = vec
+        ker[f"spiky_grad_{h}"] = np.stack([R.spiky_grad(t, hf) for t in vec]).astype(np.float32)
+        for k in ("poly6", "spiky", "cubic"):
+            fn = {"poly6": lambda t: P.poly6(t * t, hf), "spiky": lambda t: P.spiky(t, hf),
+                  "cubic": lambda t: P.cubic_spline(t, hf)}[k]
+            mine = np.array([fn(t) for t in r], np.float32)
+            assert np.array_equal(mine, ker[f"{k}_{h}"]), k
+        mine = np.stack([P.spiky_grad(t, hf) for t in vec])
+        assert np.array_equal(mine, ker[f"spiky_grad_{h}"])
+    np.savez_compressed(os.path.join(HERE, "kernels.npz"), **ker)
+
+    # --- Grid candidate lists on a seeded cloud (query order included).
+    rng = np.random.default_rng(42)
+    cloud = rng.uniform(-0.3, 1.0, size=(600, 3)).astype(np.float32)
+    queries = rng.uniform(-0.3, 1.0, size=(16, 3)).astype(np.float32)
+    lists = [R.grid_query(cloud, 0.1, q) for q in queries]
+    for q, ref_list in zip(queries, lists):
+        assert np.array_equal(P.grid_query(cloud, 0.1, q), ref_list)
+    offs = np.cumsum([0] + [len(t) for t in lists]).astype(np.int64)
+    np.savez_compressed(os.path.join(HERE, "grid.npz"), cloud=cloud, queries=queries,
+                        offsets=offs, cand=np.concatenate(lists).astype(np.int32))
+
+    # --- One and five steps of a 1000-particle dam-break block.
+    w = small_block()
+    s = Settings.make(**w.settings)
+    z = np.zeros(w.n, np.float32)
+    res = {}
+    for k in (1, 5):
+        got = R.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, k)
+        mine = P.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, k)
+        for a, b in zip(got, mine):
+            assert np.array_equal(a, b), "restatement differs from the reference build"
+        for name, a in zip(("x", "v", "rho", "lam"), got):
+            res[f"{name}{k}"] = a
+    np.savez_compressed(os.path.join(HERE, "block_1k.npz"), x0=w.x, v0=w.v, **res)
+
+    # --- The reference tests' default-settings scene, one step.
+    x, s2, dt, g, m = default_scene()
+    z = np.zeros(len(x), np.float32)
+    got = R.steps(s2, x, np.zeros_like(x), z, z, dt, g, m, 1)
+    mine = P.steps(s2, x, np.zeros_like(x), z, z, dt, g, m, 1)
+    for a, b in zip(got, mine):
+        assert np.array_equal(a, b)
+    np.savez_compressed(os.path.join(HERE, "default_scene.npz"), x0=x, x1=got[0], v1=got[1],
+                        rho1=got[2], lam1=got[3])
+
+    # --- Digests of the 8,000-particle dam break after 1 and 10 steps.
+    w8 = workloads.dam_break_8k(vorticity=0.0)
+    s8 = Settings.make(**w8.settings)
+    z = np.zeros(w8.n, np.float32)
+    for k in (1, 10):
+        got = R.steps(s8, w8.x, w8.v, z, z, w8.dt, w8.gravity, w8.mass, k)
+        mine = P.steps(s8, w8.x, w8.v, z, z, w8.dt, w8.gravity, w8.mass, k)
+        for a, b in zip(got, mine):
+            assert np.array_equal(a, b)
+        out[f"dam_break_8k_steps{k}"] = digest(*got)
+    out["dam_break_8k_input"] = digest(w8.x)
+    with open(os.path.join(HERE, "digests.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("fixtures written", out)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,55 @@
+"""The C-ABI library loads and exports what include/novaphy_pbf.h declares
+(CPU: no compute calls)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def test_library_exports_every_declared_symbol(capi):
+    lib = capi.load()
+    declared = capi.declared_symbols()
+    assert len(declared) >= 20
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_version_and_defaults(capi):
+    assert b"sm_103a" in capi.load().pbf_version()
+    s = capi.default_settings()
+    # PBFSettings defaults (include/novaphy/fluid/pbf_solver.h:14-27)
+    assert s.rest_density == 1000.0 and s.solver_iterations == 4
+    assert np.float32(s.kernel_radius) == np.float32(0.1)
+    assert s.corr_n == 4 and s.use_domain_bounds == 0
+    assert list(s.domain_lower) == [-10.0, 0.0, -10.0]
+    assert s.hash_compat == 1 and s.exact_arithmetic == 1
+
+
+def test_settings_layout_matches_oracle():
+    from novaphy_gb300.capi import Settings as S
+    from oracle.oracle import Settings as O
+
+    for (a, ta), (b, tb) in zip(O._fields_, S._fields_):
+        assert a == b and ctypes.sizeof(ta) == ctypes.sizeof(tb)
+        assert getattr(O, a).offset == getattr(S, a).offset
+
+
+def test_invalid_arguments_are_rejected(capi):
+    lib = capi.load()
+    assert lib.pbf_default_settings(None) == capi.PBF_ERR_INVALID_ARG
+    assert b"NULL" in lib.pbf_last_error()
+    assert lib.pbf_scene_step(None, ctypes.c_float(0.01), 1) == capi.PBF_ERR_INVALID_ARG
+    bad = capi.default_settings(kernel_radius=0.0)
+    out = ctypes.c_void_p()
+    rc = lib.pbf_scene_create(0, ctypes.byref(bad), 0, None, None, 1.0, ctypes.byref(out))
+    assert rc == capi.PBF_ERR_INVALID_ARG
+
+
+def test_no_device_is_reported_not_faked(capi):
+    if capi.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    s = capi.default_settings()
+    x = np.zeros((4, 3), np.float32)
+    with pytest.raises(capi.PbfError) as e:
+        capi.Scene(s, x, mass=1.0)
+    assert e.value.code == capi.PBF_ERR_NO_DEVICE

@@ -1,0 +1,205 @@
+"""The oracle restatement against the reference's golden vectors (CPU only).
+
+Fixtures in tests/golden come from the reference's own PBF sources compiled
+by oracle/build_oracle.py (see tests/golden/make_golden.py).  Where the
+reference tree is present, the restatement is also compared live against
+that build.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from novaphy_gb300 import workloads
+from oracle.oracle import Settings
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, np.float32).tobytes())
+    return h.hexdigest()
+
+
+def test_kernels_match_golden(port):
+    g = _load("kernels.npz")
+    for h in (0.1, 0.04):
+        hf = np.float32(h)
+        r = g[f"r_{h}"]
+        assert np.array_equal([port.poly6(t * t, hf) for t in r], g[f"poly6_{h}"])
+        assert np.array_equal([port.spiky(t, hf) for t in r], g[f"spiky_{h}"])
+        assert np.array_equal([port.cubic_spline(t, hf) for t in r], g[f"cubic_{h}"])
+        got = np.stack([port.spiky_grad(t, hf) for t in g[f"gradvec_{h}"]])
+        assert np.array_equal(got, g[f"spiky_grad_{h}"])
+
+
+def test_kernel_known_answers(port):
+    # Reference tests: tests/python/test_fluid.py:11-91.
+    h = np.float32(0.1)
+    assert port.poly6(0.0, h) > 0
+    assert abs(port.poly6(h * h, h)) < 1e-10
+    assert port.poly6(h * h * np.float32(1.1), h) == 0.0
+    dr = h / 1000
+    integral = sum(port.poly6(((i + 0.5) * dr) ** 2, h) * 4 * np.pi * ((i + 0.5) * dr) ** 2 * dr
+                   for i in range(1000))
+    assert abs(integral - 1.0) < 0.02
+    assert port.spiky(0.0, h) > 0 and port.spiky(h, h) == 0.0
+    assert np.allclose(port.spiky_grad([h, 0, 0], h), 0, atol=1e-7)
+    assert port.spiky_grad([0.05, 0, 0], h)[0] < 0
+    assert port.cubic_spline(0.0, h) > 0 and port.cubic_spline(h, h) == 0.0
+
+
+def test_grid_candidates_match_golden(port):
+    g = _load("grid.npz")
+    for k, q in enumerate(g["queries"]):
+        want = g["cand"][g["offsets"][k]:g["offsets"][k + 1]]
+        assert np.array_equal(port.grid_query(g["cloud"], np.float32(0.1), q), want)
+
+
+def test_grid_superset_of_brute_force(port):
+    # Reference test tests/python/test_fluid.py:235-260 (500 uniform points).
+    pts = np.random.default_rng(42).uniform(0, 1, (500, 3)).astype(np.float32)
+    q = np.array([0.5, 0.5, 0.5], np.float32)
+    cand = set(port.grid_query(pts, np.float32(0.1), q).tolist())
+    brute = {i for i, p in enumerate(pts) if np.linalg.norm(p - q) < 0.1}
+    assert brute <= cand
+
+
+def test_block_1k_steps_match_golden(port):
+    g = _load("block_1k.npz")
+    w = workloads.dam_break((10, 10, 10), 0.025, (1.0, 1.0, 1.0), dt=1.0 / 120.0, jitter=1e-4,
+                            seed=0, vorticity=0.0)
+    assert np.array_equal(w.x, g["x0"])
+    s = Settings.make(**w.settings)
+    z = np.zeros(w.n, np.float32)
+    for k in (1, 5):
+        got = port.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, k)
+        for name, a in zip(("x", "v", "rho", "lam"), got):
+            assert np.array_equal(a, g[f"{name}{k}"]), (k, name)
+
+
+def test_default_scene_matches_golden(port):
+    g = _load("default_scene.npz")
+    x = g["x0"]
+    s = Settings.make(kernel_radius=0.1)
+    z = np.zeros(len(x), np.float32)
+    got = port.steps(s, x, np.zeros_like(x), z, z, np.float32(1 / 60),
+                     np.array([0, -9.81, 0], np.float32), np.float32(1000) * np.float32(0.025) ** 3)
+    for name, a in zip(("x1", "v1", "rho1", "lam1"), got):
+        assert np.array_equal(a, g[name]), name
+
+
+def test_dam_break_8k_digests(port):
+    d = json.load(open(os.path.join(GOLDEN, "digests.json")))
+    w = workloads.dam_break_8k(vorticity=0.0)
+    assert _digest(w.x) == d["dam_break_8k_input"]
+    s = Settings.make(**w.settings)
+    z = np.zeros(w.n, np.float32)
+    got = port.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
+    assert _digest(*got) == d["dam_break_8k_steps1"]
+
+
+def test_hash_collisions_are_present_on_the_8k_case(port):
+    # The reference's XOR hash merges cells (-1,-1,z) and (1,1,z) (and
+    # similar); particles next to the coordinate axes see a bucket twice.
+    w = workloads.dam_break_8k()
+    assert port.hash_collisions(w.x, np.float32(0.1)) > 0
+    h = port.lib.orc_hash_cell
+    h.restype = __import__("ctypes").c_ulonglong
+    assert h(-1, -1, 3) == h(1, 1, 3)
+    assert h(-1, 1, 0) == h(1, -1, 0)
+    # far from the axes the 27 keys are distinct
+    far = workloads.lattice((4, 4, 4), 0.025, (3.0, 5.0, 7.0))
+    assert port.hash_collisions(far, np.float32(0.1)) == 0
+
+
+def test_port_matches_reference_build_live(port, ref):
+    w = workloads.dam_break((8, 6, 7), 0.025, (1.0, 1.0, 1.0), dt=1.0 / 120.0, seed=5,
+                            vorticity=0.0)
+    for kw in ({}, {"solver_iterations": 0}, {"xsph_viscosity": 0.0}, {"corr_n": 2},
+               {"use_domain_bounds": 0}, {"solver_iterations": 1, "corr_k": 0.0}):
+        st = dict(w.settings)
+        st.update(kw)
+        s = Settings.make(**st)
+        rng = np.random.default_rng(3)
+        v0 = rng.normal(scale=0.3, size=w.x.shape).astype(np.float32)
+        rho = rng.uniform(900, 1100, w.n).astype(np.float32)
+        lam = rng.normal(scale=1e-3, size=w.n).astype(np.float32)
+        a = port.steps(s, w.x, v0, rho, lam, w.dt, w.gravity, w.mass, 3)
+        b = ref.steps(s, w.x, v0, rho, lam, w.dt, w.gravity, w.mass, 3)
+        for u, t in zip(a, b):
+            assert np.array_equal(u, t), kw
+
+
+def test_vorticity_zero_is_reference(port):
+    w = workloads.dam_break((6, 6, 6), 0.025, (1.0, 1.0, 1.0), vorticity=0.0)
+    s0 = Settings.make(**w.settings)
+    st = dict(w.settings)
+    st["vorticity_epsilon"] = 1e-4
+    s1 = Settings.make(**st)
+    z = np.zeros(w.n, np.float32)
+    a = port.steps(s0, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 2)
+    b = port.steps(s1, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 2)
+    # confinement changes velocities but stays a small perturbation
+    assert not np.array_equal(a[1], b[1])
+    assert np.abs(a[0] - b[0]).max() < 1e-3
+
+
+def test_boundary_sampling_geometry(port):
+    # Reference tests tests/python/test_coupling.py:10-68.
+    box = port.sample_box([0.5, 0.5, 0.5], spacing=0.25)
+    assert len(box) == 6 * 5 * 5
+    assert np.allclose(np.abs(box).max(axis=1), 0.5, atol=1e-6)
+    sph = port.sample_sphere(0.5, spacing=0.1)
+    assert len(sph) > 10
+    assert np.allclose(np.linalg.norm(sph, axis=1), 0.5, atol=0.01)
+    pl = port.sample_plane([0, 1, 0], 0.0, 0.2, 0.5)
+    assert len(pl) == 6 * 6 and np.allclose(pl[:, 1], 0.0, atol=1e-5)
+    assert len(port.generate_block([0, 0, 0], [0.1, 0.1, 0.1], 0.05)) == 27
+    assert len(port.generate_block([0, 0, 0], [0.2, 0, 0], 0.1)) == 3
+
+
+def test_boundary_volumes_and_coupling_small(port):
+    loc = port.sample_sphere(0.1, spacing=0.02)
+    body = np.zeros(len(loc), np.int32)
+    wpos = port.boundary_world_positions(loc, body, [[0.3, 0.3, 0.3]], [[1, 0, 0, 0]])
+    assert np.allclose(wpos.mean(axis=0), [0.3, 0.3, 0.3], atol=2e-3)
+    psi = port.boundary_volumes(wpos, 0.08)
+    assert (psi > 0).all()
+    x = workloads.lattice((6, 6, 6), 0.02, (0.25, 0.25, 0.18))
+    rho = np.full(len(x), 1100.0, np.float32)
+    rho2 = port.boundary_density(x, rho, wpos, psi, 0.08, 1000.0)
+    assert (rho2 >= rho).all() and (rho2 > rho).any()
+    f, t = port.coupling_forces(x, rho2, 0.008, wpos, body, psi, [1], [[0.3, 0.3, 0.3]], 0.08,
+                                1000.0)
+    assert np.isfinite(f).all() and np.abs(f).sum() > 0
+
+
+def test_configured_scorr_is_ill_conditioned(port):
+    # With s_corr k = 0.1 the reference's step switches the full tensile term
+    # on at lambda_i + lambda_j < -1e-10 (pbf_solver.cpp:204); the lattice's
+    # interior density sits within ~1e-4 of rho0, so a last-bit change of the
+    # inputs flips that gate for some particles.  Only bit-exact arithmetic can
+    # meet a 1e-5 relative bound there; with s_corr off the step is smooth.
+    w = workloads.dam_break_8k(vorticity=0.0)
+    z = np.zeros(w.n, np.float32)
+    xp = np.nextafter(w.x, np.float32(2)).astype(np.float32)
+    for k, bound in ((0.1, None), (0.0, 1e-6)):
+        st = dict(w.settings)
+        st["corr_k"] = k
+        s = Settings.make(**st)
+        a = port.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
+        b = port.steps(s, xp, w.v, z, z, w.dt, w.gravity, w.mass, 1)
+        dx = np.linalg.norm(a[0] - b[0], axis=1).max()
+        if bound is None:
+            assert dx > 1e-3
+        else:
+            assert dx < bound
