@@ -1,26 +1,36 @@
 #!/usr/bin/env python
 """Throughput of the GB300 PBF step (particle-steps/s) on the 1M-particle dam break.
 
-A step is one full PBF step (predict, cell sort, neighbour grid, 4 Jacobi
-density iterations with s_corr, velocity update, XSPH, vorticity
-confinement, domain clamp, commit) over the 1,000,000-particle dam break
-(100^3 lattice at r = 0.01 m in a 4x2x2 m box, h = 4r, dt = 1/240 s), all
-inputs synthetic and seeded (novaphy_gb300/workloads.py).
+A step is one full PBF step (predict, cell sort, reference hash buckets,
+4 Jacobi density iterations with s_corr, velocity update, XSPH, vorticity
+confinement, domain clamp, commit) over one batch of synthetic input: the
+seeded 1,000,000-particle dam break (100^3 lattice at r = 0.01 m in a
+4x2x2 m box, h = 4r, dt = 1/240 s; novaphy_gb300/workloads.py).  Every step
+starts from that seeded state (restored from a device-resident snapshot by a
+device-to-device copy inside the timed region): with the configured s_corr
+k = 0.1 the reference's own step explodes within a step or two and
+consecutive steps pile the fluid onto the walls, so a run of consecutive
+steps measures that degenerate state instead (reported separately as
+`consecutive`).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 ours: `value` is device throughput with the scene resident in HBM (CUDA
-events on the scene's stream around K graph-replayed steps; the per-step
-working set, ~190 MB, exceeds the 129 MB L2).  `e2e` is the same metric
-through the drop-in host-array call pbf_solver_step_host (the C ABI of
-PBFSolver::step): every step uploads x, v, densities, lambdas from pinned
-host memory and reads them back.  Under torchrun each rank runs an
-independent replica on its own GPU (the single-scene path does not shard);
-`value` sums the ranks' particle-steps over the slowest rank's time.
+events on the scene's stream around K {restore; graph-replayed step}; the
+per-step working set, ~300 MB, exceeds the 129 MB L2).  Arithmetic is the
+default exact build (bit-identical to the reference); `fast` repeats the
+measurement with the FMA build.  `e2e` is the same metric through the
+drop-in host-array call pbf_solver_step_host (the C ABI of PBFSolver::step):
+each call uploads x, v, densities, lambdas from pinned host memory, steps
+and reads them back; the host arrays are re-seeded between calls outside the
+timed calls.  Under torchrun each rank runs an independent replica on its own
+GPU (the single-scene path does not shard); `value` sums the ranks'
+particle-steps over the slowest rank's time.
 
 reference: the reference's CPU PBF (its own sources built in oracle/_ref
 where the reference tree is present, else the oracle restatement), single
-threaded as the reference is, on a bounded sample of the same workload.
+threaded as the reference is, each step on the seeded state of a bounded
+sample of the same workload.
 """
 from __future__ import annotations
 
@@ -156,26 +166,27 @@ def cpu_sample_workload(counts):
 
 
 def time_cpu(counts, nsteps, warmup):
+    """Reference CPU steps, each from the seeded state of a counts-block sample."""
     from oracle.oracle import Settings
 
     be, kind = cpu_backend()
     w = cpu_sample_workload(counts)
     s = Settings.make(**w.settings)
-    x, v = w.x, w.v
-    rho = np.zeros(w.n, np.float32)
-    lam = np.zeros(w.n, np.float32)
-    if warmup:
-        x, v, rho, lam = be.steps(s, x, v, rho, lam, w.dt, w.gravity, w.mass, warmup)
-    t0 = time.perf_counter()
-    x, v, rho, lam = be.steps(s, x, v, rho, lam, w.dt, w.gravity, w.mass, nsteps)
-    el = time.perf_counter() - t0
+    z = np.zeros(w.n, np.float32)
+    for _ in range(warmup):
+        be.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
+    el = 0.0
+    for _ in range(nsteps):
+        t0 = time.perf_counter()
+        be.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
+        el += time.perf_counter() - t0
     return w.n * nsteps / el, kind, w.n, el
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
-    counts = (40, 40, 40)
+    counts = (32, 32, 32)
     val, kind, n, el = time_cpu(counts, args.steps, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
@@ -186,8 +197,8 @@ def run_reference(args, ws, rank):
                    f"{counts[0]}x{counts[1]}x{counts[2]} of the 1M case's lattice, box and "
                    "parameters", "threads": 1},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": kind,
-                         "sample": f"{n} particles x {args.steps} steps, 1 thread (the reference "
-                         "CPU PBF has no threading)"},
+                         "sample": f"{n} particles x {args.steps} steps, each from the seeded "
+                         "state, 1 thread (the reference CPU PBF has no threading)"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -205,36 +216,38 @@ def run_ours(args, ws, rank, local):
         dist.init_process_group("gloo")
     device = local
     w = workloads.dam_break_1m(vorticity=args.vorticity)
-    s = capi.default_settings(**w.settings, exact_arithmetic=0)
+    s = capi.default_settings(**w.settings, exact_arithmetic=1)
     sc = capi.Scene(s, w.x, w.v, mass=w.mass, device=device)
     sc.set_gravity(w.gravity)
-
-    # warm-up (also captures the step graph)
-    sc.step(w.dt, max(args.warmup, 1))
+    seed = sc.snapshot()
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    barrier()
-    with ClockSampler(device) as clk:
-        ms = sc.step_timed(w.dt, args.steps)
-    barrier()
-    clocks = clk.summary()
-    sec = ms / 1e3
-    if dist is not None:
+    def max_over_ranks(x):
+        if dist is None:
+            return x
         import torch
 
-        t = torch.tensor([sec], dtype=torch.float64)
+        t = torch.tensor([x], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec = float(t.item())
+        return float(t.item())
+
+    sc.replay_timed(seed, w.dt, max(args.warmup, 1))  # warm-up (captures the step graph)
+    barrier()
+    with ClockSampler(device) as clk:
+        ms = sc.replay_timed(seed, w.dt, args.steps)
+    barrier()
+    clocks = clk.summary()
+    sec = max_over_ranks(ms / 1e3)
     value = w.n * args.steps * ws / sec
 
-    # Per-phase device times (one non-graph step each, after the timed region).
-    phases = {}
-    launches = {}
+    # Per-phase device times (one non-graph step from the seed each).
+    phases, launches = {}, {}
     reps = 3
     for _ in range(reps):
+        sc.restore(seed)
         for k, (t_ms, nl) in sc.step_profiled(w.dt).items():
             phases[k] = phases.get(k, 0.0) + t_ms / reps
             launches[k] = nl
@@ -252,6 +265,31 @@ def run_ours(args, ws, rank, local):
                 "alg_bytes_per_launch": alg, "launch_ms": launch_ms,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"}
 
+    # The FMA build on the same batch.
+    fast = None
+    if not args.no_fast:
+        sf = capi.default_settings(**w.settings, exact_arithmetic=0)
+        fs = capi.Scene(sf, w.x, w.v, mass=w.mass, device=device)
+        fs.set_gravity(w.gravity)
+        fseed = fs.snapshot()
+        fs.replay_timed(fseed, w.dt, max(args.warmup, 1))
+        barrier()
+        fsec = max_over_ranks(fs.replay_timed(fseed, w.dt, args.steps) / 1e3)
+        fast = {"value": w.n * args.steps * ws / fsec, "unit": UNIT,
+                "ms_per_step": fsec * 1e3 / args.steps, "arithmetic": "FMA + rsqrt"}
+        fseed.close()
+        fs.close()
+
+    # Consecutive steps of the configured trajectory from the seed.
+    consecutive = None
+    if not args.no_consecutive:
+        ksteps = min(args.steps, 10)
+        sc.restore(seed)
+        cms = sc.step_timed(w.dt, ksteps)
+        consecutive = {"value": w.n * ksteps / (cms / 1e3), "unit": UNIT, "steps": ksteps,
+                       "note": "steps 1..k of the seeded dam break; the configured s_corr "
+                               "makes it explode and cells overfill"}
+
     # End to end through the host-array drop-in call.
     e2e = None
     if not args.no_e2e:
@@ -265,10 +303,6 @@ def run_ours(args, ws, rank, local):
                 return np.empty(shape, np.float32)
         hx, hv = pinned((w.n, 3)), pinned((w.n, 3))
         hr, hl = pinned((w.n,)), pinned((w.n,))
-        hx[:] = w.x
-        hv[:] = w.v
-        hr[:] = 0
-        hl[:] = 0
         drop = capi.Scene(s, w.x[:1], None, mass=w.mass, device=device)
         L = capi.load()
         import ctypes as C
@@ -276,27 +310,32 @@ def run_ours(args, ws, rank, local):
         g = np.ascontiguousarray(w.gravity, np.float32)
         gp = g.ctypes.data_as(C.POINTER(C.c_float))
 
+        def reseed():
+            hx[:] = w.x
+            hv[:] = w.v
+            hr[:] = 0
+            hl[:] = 0
+
         def call():
             capi.check(L.pbf_solver_step_host(drop.handle, w.n, capi._ptr(hx), capi._ptr(hv),
                                               capi._ptr(hr), capi._ptr(hl), w.dt, gp, w.mass))
 
         for _ in range(max(args.warmup, 1)):
+            reseed()
             call()
         barrier()
-        t0 = time.perf_counter()
+        el = 0.0
         for _ in range(args.steps):
+            reseed()
+            t0 = time.perf_counter()
             call()
+            el += time.perf_counter() - t0
         barrier()
-        el = time.perf_counter() - t0
-        if dist is not None:
-            import torch
-
-            t = torch.tensor([el], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(el)
         per = w.n * (12 + 12 + 4 + 4)
         e2e = {"value": w.n * args.steps * ws / el, "unit": UNIT, "h2d_bytes_per_step": per,
-               "d2h_bytes_per_step": per, "call": "pbf_solver_step_host (pinned host arrays)"}
+               "d2h_bytes_per_step": per,
+               "call": "pbf_solver_step_host: pinned host x, v, densities, lambdas in and out"}
         drop.close()
 
     cpu = None
@@ -305,7 +344,8 @@ def run_ours(args, ws, rank, local):
         val, kind, n, el = time_cpu(counts, 1, 0)
         cpu = {"value": val, "unit": UNIT, "cores": 1, "kind": kind,
                "sample": f"{n}-particle {counts[0]}x{counts[1]}x{counts[2]} block of the 1M case's "
-                         f"lattice/box/parameters, 1 step, 1 thread ({el:.1f} s)"}
+                         f"lattice/box/parameters, 1 step from the seeded state, 1 thread "
+                         f"({el:.1f} s)"}
 
     if rank == 0:
         line = {
@@ -315,17 +355,23 @@ def run_ours(args, ws, rank, local):
             "data": "synthetic",
             "config": {"workload": "dam_break_1m", "particles": w.n, "lattice": "100x100x100",
                        "r": 0.01, "h": w.settings["kernel_radius"], "iterations": iters,
-                       "dt": w.dt, "vorticity_epsilon": args.vorticity, "arithmetic": "fast (FMA)",
-                       "hash_compat": 1, "l2": "per-step working set ~190 MB > 129 MB L2",
+                       "dt": w.dt, "vorticity_epsilon": args.vorticity,
+                       "arithmetic": "exact (bit-identical to the reference)", "hash_compat": 1,
+                       "step": "one PBF step from the seeded batch (device snapshot restore "
+                               "inside the timed region)",
+                       "l2": "per-step working set ~300 MB > 129 MB L2",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks,
+            "fast": fast,
+            "consecutive": consecutive,
             "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         }
         print(json.dumps(line), flush=True)
+    seed.close()
     sc.close()
     if dist is not None:
         dist.destroy_process_group()
@@ -341,6 +387,8 @@ def main():
     ap.add_argument("--vorticity", type=float, default=1e-4)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fast", action="store_true")
+    ap.add_argument("--no-consecutive", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -113,6 +113,24 @@ int pbf_scene_sync(pbf_scene* scene);
  * nsteps steps measured with CUDA events on the scene's stream. */
 int pbf_scene_step_timed(pbf_scene* scene, float dt, int nsteps, float* ms_out);
 
+/* Device-resident snapshot of a scene's particle state (positions,
+ * velocities, densities, lambdas) plus its settings, gravity and mass: the
+ * checkpoint/resume unit.  Restoring and stepping k + m steps is bit-identical
+ * to stepping k, snapshotting, restoring and stepping m.  The reference has no
+ * counterpart; ParticleState::init (particle_state.cpp:11-20) is its only way
+ * to re-seed a state. */
+typedef struct pbf_snapshot pbf_snapshot;
+int pbf_snapshot_create(pbf_scene* scene, pbf_snapshot** out);
+int pbf_snapshot_restore(pbf_scene* scene, const pbf_snapshot* snap);
+int pbf_snapshot_destroy(pbf_snapshot* snap);
+int pbf_snapshot_num_particles(const pbf_snapshot* snap, int* out);
+
+/* Benchmark loop: nsteps times { restore `seed`; one step }, bracketed by
+ * CUDA events on the scene's stream (the step graph is captured before the
+ * timed region); *ms_out receives the device time of the whole loop. */
+int pbf_scene_replay_timed(pbf_scene* scene, const pbf_snapshot* seed, float dt, int nsteps,
+                           float* ms_out);
+
 /* Copies a field to/from host memory (blocking).  Reading replaces the
  * ParticleState vector accessors (python/bindings/bind_fluid.cpp:120-131). */
 int pbf_scene_read(pbf_scene* scene, int field, float* host_out);

@@ -108,6 +108,11 @@ def load() -> C.CDLL:
         "pbf_sort_pairs_host": ([C.c_int, C.c_int, vp, C.c_int, vp, vp], C.c_int),
         "pbf_phase_name": ([C.c_int], C.c_char_p),
         "pbf_scene_step_timed": ([vp, C.c_float, C.c_int, f32p], C.c_int),
+        "pbf_snapshot_create": ([vp, C.POINTER(vp)], C.c_int),
+        "pbf_snapshot_restore": ([vp, vp], C.c_int),
+        "pbf_snapshot_destroy": ([vp], C.c_int),
+        "pbf_snapshot_num_particles": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "pbf_scene_replay_timed": ([vp, vp, C.c_float, C.c_int, f32p], C.c_int),
         "pbf_scene_step_profiled": ([vp, C.c_float, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -224,6 +229,18 @@ class Scene:
         check(self._L.pbf_scene_step_timed(self._h, dt, nsteps, C.byref(ms)))
         return ms.value
 
+    def snapshot(self) -> "Snapshot":
+        return Snapshot(self)
+
+    def restore(self, snap: "Snapshot"):
+        check(self._L.pbf_snapshot_restore(self._h, snap.handle))
+
+    def replay_timed(self, seed: "Snapshot", dt: float, nsteps: int) -> float:
+        """Device ms of nsteps x {restore seed; step}."""
+        ms = C.c_float(0.0)
+        check(self._L.pbf_scene_replay_timed(self._h, seed.handle, dt, nsteps, C.byref(ms)))
+        return ms.value
+
     def sync(self):
         check(self._L.pbf_scene_sync(self._h))
 
@@ -289,6 +306,30 @@ class Scene:
                                            _ptr(lam), dt,
                                            g.ctypes.data_as(C.POINTER(C.c_float)), mass))
         return x, v, rho, lam
+
+
+class Snapshot:
+    """Device-resident copy of a scene's particle state (pbf_snapshot*)."""
+
+    def __init__(self, scene: Scene):
+        h = C.c_void_p()
+        check(load().pbf_snapshot_create(scene.handle, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            load().pbf_snapshot_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 NUM_PHASES = 7

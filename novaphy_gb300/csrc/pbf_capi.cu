@@ -643,6 +643,142 @@ int pbf_scene_step_timed(pbf_scene* s, float dt, int nsteps, float* ms_out) {
     return sync_and_check(s);
 }
 
+}  // extern "C"
+
+struct pbf_snapshot {
+    int device = 0;
+    int n = 0;
+    pbf_settings settings{};
+    float gravity[3] = {0, 0, 0};
+    float mass = 0.0f;
+    void* mem = nullptr;  // x (float4 n) | v (float4 n) | rho (n) | lam (n)
+};
+
+namespace {
+size_t snapshot_bytes(int n) { return (size_t)n * (16 + 16 + 4 + 4); }
+}  // namespace
+
+extern "C" {
+
+int pbf_snapshot_create(pbf_scene* s, pbf_snapshot** out) {
+    if (!s || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    pbf_snapshot* snap = new pbf_snapshot();
+    snap->device = s->device;
+    snap->n = s->n;
+    snap->settings = s->settings;
+    for (int d = 0; d < 3; ++d) snap->gravity[d] = s->gravity[d];
+    snap->mass = s->mass;
+    if (s->n > 0) {
+        cudaError_t e = cudaMalloc(&snap->mem, snapshot_bytes(s->n));
+        if (e != cudaSuccess) {
+            delete snap;
+            return cuda_fail(e, "pbf_snapshot_create");
+        }
+        char* p = reinterpret_cast<char*>(snap->mem);
+        const size_t n = (size_t)s->n;
+        e = cudaMemcpyAsync(p, s->B.x, n * 16, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p + n * 16, s->B.v, n * 16, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p + n * 32, s->B.rho, n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p + n * 36, s->B.lam, n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) {
+            cudaFree(snap->mem);
+            delete snap;
+            return cuda_fail(e, "pbf_snapshot_create");
+        }
+    }
+    *out = snap;
+    return PBF_OK;
+}
+
+int pbf_snapshot_destroy(pbf_snapshot* snap) {
+    if (!snap) return PBF_OK;
+    if (snap->mem) {
+        DeviceGuard dg(snap->device);
+        cudaFree(snap->mem);
+    }
+    delete snap;
+    return PBF_OK;
+}
+
+int pbf_snapshot_num_particles(const pbf_snapshot* snap, int* out) {
+    if (!snap || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *out = snap->n;
+    return PBF_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// Copies a snapshot into the scene on its stream (asynchronous).
+int restore_async(pbf_scene* s, const pbf_snapshot* snap) {
+    if (snap->device != s->device) return fail(PBF_ERR_INVALID_ARG, "snapshot is on another device");
+    if (snap->n > s->cap || !s->pmem) {
+        int rc = alloc_particles(s, snap->n);
+        if (rc) return rc;
+    }
+    s->n = snap->n;
+    s->settings = snap->settings;
+    for (int d = 0; d < 3; ++d) s->gravity[d] = snap->gravity[d];
+    s->mass = snap->mass;
+    if (snap->n == 0) return PBF_OK;
+    const char* p = reinterpret_cast<const char*>(snap->mem);
+    const size_t n = (size_t)snap->n;
+    PBF_CUDA(cudaMemcpyAsync(s->B.x, p, n * 16, cudaMemcpyDeviceToDevice, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(s->B.v, p + n * 16, n * 16, cudaMemcpyDeviceToDevice, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(s->B.rho, p + n * 32, n * 4, cudaMemcpyDeviceToDevice, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(s->B.lam, p + n * 36, n * 4, cudaMemcpyDeviceToDevice, s->stream));
+    return PBF_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int pbf_snapshot_restore(pbf_scene* s, const pbf_snapshot* snap) {
+    if (!s || !snap) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = restore_async(s, snap);
+    if (rc) return rc;
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    return PBF_OK;
+}
+
+int pbf_scene_replay_timed(pbf_scene* s, const pbf_snapshot* seed, float dt, int nsteps,
+                           float* ms_out) {
+    if (!s || !seed || !ms_out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    if (nsteps < 0) return fail(PBF_ERR_INVALID_ARG, "nsteps must be >= 0");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    *ms_out = 0.0f;
+    int rc = restore_async(s, seed);
+    if (rc) return rc;
+    rc = run_steps(s, dt, 1);  // capture the step graph outside the timed region
+    if (rc) return rc;
+    cudaEvent_t a = nullptr, b = nullptr;
+    PBF_CUDA(cudaEventCreate(&a));
+    cudaError_t e = cudaEventCreate(&b);
+    if (e == cudaSuccess) e = cudaEventRecord(a, s->stream);
+    for (int k = 0; k < nsteps && e == cudaSuccess && rc == PBF_OK; ++k) {
+        rc = restore_async(s, seed);
+        if (rc == PBF_OK) rc = run_steps(s, dt, 1);
+    }
+    if (e == cudaSuccess && rc == PBF_OK) e = cudaEventRecord(b, s->stream);
+    if (e == cudaSuccess && rc == PBF_OK) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess && rc == PBF_OK) e = cudaEventElapsedTime(ms_out, a, b);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "pbf_scene_replay_timed");
+    return sync_and_check(s);
+}
+
 int pbf_scene_sync(pbf_scene* s) {
     if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
