@@ -186,6 +186,21 @@ int pbf_scene_step_profiled(pbf_scene* scene, float dt, float* phase_ms, int* la
 int pbf_sort_pairs_host(int device, int n, const unsigned* keys, int key_bits,
                         unsigned* out_keys, unsigned* out_vals);
 
+/* Allocation-free cell-key sort.  No counterpart in the reference: it exists
+ * for callers that must not allocate device memory while they run (a host
+ * framework that owns all device memory through its own budgeted pool, or a
+ * latency-bound loop where cudaMalloc/cudaFree could synchronize the device
+ * or fail mid-frame).  Same result as pbf_sort_pairs_host, but keys and
+ * outputs are DEVICE buffers the caller owns, and the sort's scratch is a
+ * fixed static device array (about 4.2 MB held on every GPU that loads the
+ * library, until exit), so at most 262,144 keys (PBF_ERR_CAPACITY beyond).
+ * The first call on a device looks up the array's address with that device
+ * current; make it before any stream capture.  Calls share the array: calls
+ * whose work overlaps on the GPU race and must be serialized.  Returns after
+ * the sort on `stream` (a cudaStream_t, NULL for the default stream) is done. */
+int pbf_sort_pairs_noalloc(int device, int n, const unsigned* d_keys, int key_bits,
+                           unsigned* d_out_keys, unsigned* d_out_vals, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,12 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
 
+namespace pbf {
+// Sets the calling thread's pbf_last_error() text (used by other translation
+// units of the library).
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace pbf
+
 struct pbf_scene {
     int device = 0;
     cudaStream_t stream = nullptr;
