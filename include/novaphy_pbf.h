@@ -151,6 +151,37 @@ int pbf_scene_stream(pbf_scene* scene, void** stream);
 int pbf_solver_step_host(pbf_scene* scene, int n, float* x3, float* v3, float* densities,
                          float* lambdas, float dt, const float* g3, float mass);
 
+/* ---- Akinci rigid-fluid coupling (FluidWorld, src/fluid/fluid_world.cpp) ---- */
+
+/* Boundary particles (BoundaryParticle, include/novaphy/fluid/boundary.h:21-25):
+ * body-frame positions local3[3nb], owning body (-1 = world-owned, local is
+ * world), Akinci volume psi. */
+int pbf_scene_set_boundary(pbf_scene* scene, int nb, const float* local3, const int* body,
+                           const float* psi);
+
+/* Body poses at the start of the next coupled step (World state transforms):
+ * positions pos3[3k], unit quaternions quat4[4k] as (w, x, y, z), and which
+ * bodies are dynamic (static bodies get no coupling force,
+ * fluid_world.cpp:141).  nbodies must cover every body the boundary names. */
+int pbf_scene_set_bodies(pbf_scene* scene, int nbodies, const float* pos3, const float* quat4,
+                         const int* dynamic);
+
+/* The fluid part of FluidWorld::step (fluid_world.cpp:57-81): boundary world
+ * positions from the current body poses, one PBF step, boundary density added
+ * to the final densities, and the coupling force / torque of every boundary
+ * particle accumulated into force3 / torque3 (nbodies * 3 each, in and out)
+ * in boundary order, exactly as World::apply_force / apply_torque add them.
+ * The rigid step that follows stays with the caller. */
+int pbf_scene_step_coupled(pbf_scene* scene, float dt, float* force3, float* torque3);
+
+/* World positions of the boundary particles used by the last coupled step. */
+int pbf_scene_read_boundary(pbf_scene* scene, float* world3);
+
+/* Akinci volumes psi_b = 1 / sum_b' poly6 (boundary.cpp:152-176) of nb boundary
+ * particles at world positions world3, computed on `device`. */
+int pbf_boundary_volumes(int device, int nb, const float* world3, float kernel_radius,
+                         float* psi_out);
+
 /* Finite check of positions and velocities; PBF_ERR_NONFINITE when any
  * component is NaN/Inf. */
 int pbf_scene_check_finite(pbf_scene* scene);

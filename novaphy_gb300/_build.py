@@ -37,8 +37,10 @@ NVCC_COMMON = [
 CU_FLAGS = {
     "pbf_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
     "pbf_fast.cu": ["-fmad=true", "-ftz=false"],
+    "pbf_boundary.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
 }
-CU_SOURCES = ["radix_sort.cu", "pbf_exact.cu", "pbf_fast.cu", "pbf_capi.cu", "pbf_noalloc.cu"]
+CU_SOURCES = ["radix_sort.cu", "pbf_exact.cu", "pbf_fast.cu", "pbf_boundary.cu", "pbf_capi.cu",
+              "pbf_noalloc.cu"]
 
 
 def nvcc() -> str:

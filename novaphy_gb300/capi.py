@@ -113,6 +113,11 @@ def load() -> C.CDLL:
         "pbf_snapshot_destroy": ([vp], C.c_int),
         "pbf_snapshot_num_particles": ([vp, C.POINTER(C.c_int)], C.c_int),
         "pbf_scene_replay_timed": ([vp, vp, C.c_float, C.c_int, f32p], C.c_int),
+        "pbf_scene_set_boundary": ([vp, C.c_int, vp, vp, vp], C.c_int),
+        "pbf_scene_set_bodies": ([vp, C.c_int, vp, vp, vp], C.c_int),
+        "pbf_scene_step_coupled": ([vp, C.c_float, vp, vp], C.c_int),
+        "pbf_scene_read_boundary": ([vp, vp], C.c_int),
+        "pbf_boundary_volumes": ([C.c_int, C.c_int, vp, C.c_float, vp], C.c_int),
         "pbf_scene_step_profiled": ([vp, C.c_float, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -229,6 +234,33 @@ class Scene:
         check(self._L.pbf_scene_step_timed(self._h, dt, nsteps, C.byref(ms)))
         return ms.value
 
+    # -- Akinci coupling --
+    def set_boundary(self, local, body, psi):
+        local = _f32(local, (-1, 3))
+        body = np.ascontiguousarray(body, np.int32)
+        psi = _f32(psi)
+        check(self._L.pbf_scene_set_boundary(self._h, len(local), _ptr(local), _ptr(body),
+                                             _ptr(psi)))
+        self._nb = len(local)
+
+    def set_bodies(self, pos, quat, dynamic):
+        pos = _f32(pos, (-1, 3))
+        quat = _f32(quat, (-1, 4))
+        dyn = np.ascontiguousarray(dynamic, np.int32)
+        check(self._L.pbf_scene_set_bodies(self._h, len(pos), _ptr(pos), _ptr(quat), _ptr(dyn)))
+
+    def step_coupled(self, dt, force, torque):
+        """One coupled fluid step; returns (force, torque) accumulated onto the inputs."""
+        f = _f32(force, (-1, 3)).copy()
+        t = _f32(torque, (-1, 3)).copy()
+        check(self._L.pbf_scene_step_coupled(self._h, dt, _ptr(f), _ptr(t)))
+        return f, t
+
+    def read_boundary(self):
+        out = np.zeros((getattr(self, "_nb", 0), 3), np.float32)
+        check(self._L.pbf_scene_read_boundary(self._h, _ptr(out)))
+        return out
+
     def snapshot(self) -> "Snapshot":
         return Snapshot(self)
 
@@ -330,6 +362,13 @@ class Snapshot:
             self.close()
         except Exception:
             pass
+
+
+def boundary_volumes(world, kernel_radius: float, device: int = 0):
+    world = _f32(world, (-1, 3))
+    psi = np.zeros(len(world), np.float32)
+    check(load().pbf_boundary_volumes(device, len(world), _ptr(world), kernel_radius, _ptr(psi)))
+    return psi
 
 
 NUM_PHASES = 7

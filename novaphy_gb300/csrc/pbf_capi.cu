@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "novaphy_pbf.h"
+#include "pbf_boundary.cuh"
 #include "pbf_launch.cuh"
 #include "pbf_types.cuh"
 #include "radix_sort.cuh"
@@ -118,6 +119,32 @@ struct pbf_scene {
     StepConsts graph_consts{};
     int graph_iters = -1;
     int graph_exact = -1;
+
+    // Akinci boundary (FluidWorld coupling).
+    struct Boundary {
+        int nb = 0, nbodies = 0, needed_bodies = 0;
+        void* mem = nullptr;       // per-boundary-particle arrays
+        void* body_mem = nullptr;  // per-body arrays
+        void* sort_mem = nullptr;
+        void* fq_mem = nullptr;    // fluid-query cells (per fluid particle)
+        int fq_cap = 0;
+        float4* local = nullptr;   // w = psi
+        int* body = nullptr;
+        float4* world = nullptr;   // w = psi
+        float4* Fb = nullptr;
+        PointIndex idx;            // reference buckets over the boundary
+        QuerySet bq;               // boundary queries against the fluid index
+        int4* fq_cell = nullptr;
+        float4* body_pos = nullptr;
+        float4* body_quat = nullptr;
+        int* body_dyn = nullptr;
+        int* list_off = nullptr;
+        int* list = nullptr;
+        float* force3 = nullptr;
+        float* torque3 = nullptr;
+        SortScratch sort{};
+        uint32_t idx_slots = 0;
+    } bnd;
 };
 
 namespace {
@@ -567,6 +594,9 @@ int pbf_scene_destroy(pbf_scene* s) {
     {
         DeviceGuard dg(s->device);
         if (s->stream) cudaStreamSynchronize(s->stream);
+        for (void* m : {s->bnd.mem, s->bnd.body_mem, s->bnd.sort_mem, s->bnd.fq_mem})
+            if (m) cudaFree(m);
+        if (s->bnd.idx.off) cudaFree(s->bnd.idx.off);
         free_particles(s);
         if (s->off) cudaFree(s->off);
         if (s->d_flag) cudaFree(s->d_flag);
@@ -1026,6 +1056,293 @@ int pbf_scene_step_profiled(pbf_scene* s, float dt, float* phase_ms, int* launch
     if (rc) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "pbf_scene_step_profiled");
     return sync_and_check(s);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Carves per-boundary-particle arrays for nb particles.
+int alloc_boundary(pbf_scene* s, int nb) {
+    auto& b = s->bnd;
+    for (void* m : {b.mem, b.sort_mem}) if (m) cudaFree(m);
+    b.mem = b.sort_mem = nullptr;
+    const int c = nb > 0 ? nb : 1;
+    const size_t f4 = align_up((size_t)c * 16, 256), f1 = align_up((size_t)c * 4, 256),
+                 f2 = align_up((size_t)c * 8, 256), f27 = align_up((size_t)c * 27 * 4, 256);
+    const size_t total = 6 * f4 + 9 * f1 + 2 * f2 + f27;
+    PBF_CUDA(cudaMalloc(&b.mem, total));
+    char* p = reinterpret_cast<char*>(b.mem);
+    auto take = [&](size_t n) { char* r = p; p += n; return r; };
+    b.local = reinterpret_cast<float4*>(take(f4));
+    b.world = reinterpret_cast<float4*>(take(f4));
+    b.Fb = reinterpret_cast<float4*>(take(f4));
+    b.idx.spos = reinterpret_cast<float4*>(take(f4));
+    b.idx.scell = reinterpret_cast<int4*>(take(f4));
+    b.bq.qcell = reinterpret_cast<int4*>(take(f4));
+    b.body = reinterpret_cast<int*>(take(f1));
+    b.idx.keys = reinterpret_cast<uint32_t*>(take(f1));
+    b.idx.skeys = reinterpret_cast<uint32_t*>(take(f1));
+    b.idx.sidx = reinterpret_cast<uint32_t*>(take(f1));
+    b.idx.ridx = reinterpret_cast<uint32_t*>(take(f1));
+    b.idx.pos_of = reinterpret_cast<uint32_t*>(take(f1));
+    b.idx.kpos = reinterpret_cast<uint32_t*>(take(f1));
+    b.idx.bend = reinterpret_cast<uint32_t*>(take(f1));
+    b.bq.qown = reinterpret_cast<int*>(take(f1));
+    b.idx.rkeys = reinterpret_cast<unsigned long long*>(take(f2));
+    b.idx.rsorted = reinterpret_cast<unsigned long long*>(take(f2));
+    b.bq.btab = reinterpret_cast<uint32_t*>(take(f27));
+    PBF_CUDA(cudaMemsetAsync(b.mem, 0, total, s->stream));
+    const size_t sb = sort_scratch_bytes(c);
+    PBF_CUDA(cudaMalloc(&b.sort_mem, sb));
+    PBF_CUDA(cudaMemsetAsync(b.sort_mem, 0, sb, s->stream));
+    sort_scratch_bind(b.sort, b.sort_mem, c);
+    b.nb = nb;
+    return PBF_OK;
+}
+
+int ensure_boundary_grid(pbf_scene* s, uint32_t nslots) {
+    auto& b = s->bnd;
+    if (b.idx.off && b.idx_slots >= nslots) return PBF_OK;
+    if (b.idx.off) cudaFree(b.idx.off);
+    b.idx.off = nullptr;
+    const size_t ob = align_up((size_t)(nslots + 1) * 4, 256);
+    PBF_CUDA(cudaMalloc(&b.idx.off, ob + align_up(nslots, 256)));
+    b.idx.slot_alias = reinterpret_cast<unsigned char*>(b.idx.off) + ob;
+    b.idx_slots = nslots;
+    return PBF_OK;
+}
+
+int ensure_fluid_queries(pbf_scene* s) {
+    auto& b = s->bnd;
+    if (b.fq_mem && b.fq_cap >= s->n) return PBF_OK;
+    if (b.fq_mem) cudaFree(b.fq_mem);
+    b.fq_mem = nullptr;
+    const int c = s->n > 0 ? s->n : 1;
+    PBF_CUDA(cudaMalloc(&b.fq_mem, (size_t)c * 16));
+    b.fq_cell = reinterpret_cast<int4*>(b.fq_mem);
+    b.fq_cap = c;
+    return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbf_scene_set_boundary(pbf_scene* s, int nb, const float* local3, const int* body,
+                           const float* psi) {
+    if (!s || nb < 0 || (nb > 0 && (!local3 || !body || !psi)))
+        return fail(PBF_ERR_INVALID_ARG, "bad boundary arguments");
+    if (nb > (1 << 29)) return fail(PBF_ERR_CAPACITY, "at most 2^29 boundary particles");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = alloc_boundary(s, nb);
+    if (rc) return rc;
+    auto& b = s->bnd;
+    b.nbodies = 0;
+    b.needed_bodies = 0;
+    if (b.body_mem) cudaFree(b.body_mem);
+    b.body_mem = nullptr;
+    if (nb == 0) return PBF_OK;
+    std::vector<float4> l(nb);
+    for (int i = 0; i < nb; ++i)
+        l[i] = make_float4(local3[3 * i], local3[3 * i + 1], local3[3 * i + 2], psi[i]);
+    PBF_CUDA(cudaMemcpyAsync(b.local, l.data(), (size_t)nb * 16, cudaMemcpyHostToDevice, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(b.body, body, (size_t)nb * 4, cudaMemcpyHostToDevice, s->stream));
+    // Per-body lists of boundary indices in ascending order (CSR): the
+    // reference applies forces to a body in boundary order (fluid_world.cpp:138-172).
+    int maxb = -1;
+    for (int i = 0; i < nb; ++i) maxb = std::max(maxb, body[i]);
+    const int nbody = maxb + 1;
+    std::vector<int> off(nbody + 1, 0), lst;
+    for (int i = 0; i < nb; ++i)
+        if (body[i] >= 0) ++off[body[i] + 1];
+    for (int k = 0; k < nbody; ++k) off[k + 1] += off[k];
+    lst.resize(off[nbody]);
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (int i = 0; i < nb; ++i)
+        if (body[i] >= 0) lst[fill[body[i]]++] = i;
+    const int cap = std::max(nbody, 1);
+    const size_t s16 = align_up((size_t)cap * 16, 256), s4 = align_up((size_t)(cap + 1) * 4, 256),
+                 sl = align_up(std::max<size_t>(lst.size(), 1) * 4, 256),
+                 s12 = align_up((size_t)cap * 12, 256);
+    const size_t need = 2 * s16 + 2 * s4 + sl + 2 * s12;
+    PBF_CUDA(cudaMalloc(&b.body_mem, need));
+    char* p = reinterpret_cast<char*>(b.body_mem);
+    auto take = [&](size_t n) { char* r = p; p += n; return r; };
+    b.body_pos = reinterpret_cast<float4*>(take(s16));
+    b.body_quat = reinterpret_cast<float4*>(take(s16));
+    b.body_dyn = reinterpret_cast<int*>(take(s4));
+    b.list_off = reinterpret_cast<int*>(take(s4));
+    b.list = reinterpret_cast<int*>(take(sl));
+    b.force3 = reinterpret_cast<float*>(take(s12));
+    b.torque3 = reinterpret_cast<float*>(take(s12));
+    PBF_CUDA(cudaMemsetAsync(b.body_mem, 0, need, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(b.list_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, s->stream));
+    if (!lst.empty())
+        PBF_CUDA(cudaMemcpyAsync(b.list, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice, s->stream));
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    b.needed_bodies = nbody;
+    return PBF_OK;
+}
+
+int pbf_scene_set_bodies(pbf_scene* s, int nbodies, const float* pos3, const float* quat4,
+                         const int* dynamic) {
+    if (!s || nbodies < 0 || (nbodies > 0 && (!pos3 || !quat4 || !dynamic)))
+        return fail(PBF_ERR_INVALID_ARG, "bad body arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    if (!b.body_mem) return fail(PBF_ERR_INVALID_ARG, "set the boundary particles first");
+    if (nbodies < b.needed_bodies)
+        return fail(PBF_ERR_INVALID_ARG, "fewer bodies than the boundary particles reference");
+    // Bodies past the last one with boundary particles receive no coupling.
+    nbodies = b.needed_bodies;
+    std::vector<float4> bp(nbodies), bq(nbodies);
+    for (int k = 0; k < nbodies; ++k) {
+        bp[k] = make_float4(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2], 0.0f);
+        bq[k] = make_float4(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2], quat4[4 * k + 3]);
+    }
+    if (nbodies > 0) {
+        PBF_CUDA(cudaMemcpyAsync(b.body_pos, bp.data(), (size_t)nbodies * 16, cudaMemcpyHostToDevice, s->stream));
+        PBF_CUDA(cudaMemcpyAsync(b.body_quat, bq.data(), (size_t)nbodies * 16, cudaMemcpyHostToDevice, s->stream));
+        PBF_CUDA(cudaMemcpyAsync(b.body_dyn, dynamic, (size_t)nbodies * 4, cudaMemcpyHostToDevice, s->stream));
+    }
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    b.nbodies = nbodies;
+    return PBF_OK;
+}
+
+int pbf_scene_step_coupled(pbf_scene* s, float dt, float* force3, float* torque3) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    const int nbodies = b.nbodies;
+    if (b.nb > 0 && b.nbodies < b.needed_bodies)
+        return fail(PBF_ERR_INVALID_ARG, "set the bodies first");
+    if (nbodies > 0 && (!force3 || !torque3)) return fail(PBF_ERR_INVALID_ARG, "NULL force/torque");
+    if (s->n == 0) return PBF_OK;  // fluid_world.cpp:57
+    StepConsts C;
+    int rc = make_consts(s, dt, C);
+    if (rc) return rc;
+    cudaStream_t st = s->stream;
+    // 1. boundary world positions from the step-start transforms
+    if (b.nb > 0) {
+        cudaError_t e = boundary_xform(b.local, b.body, b.nb, b.body_pos, b.body_quat, nbodies,
+                                       b.world, st);
+        if (e != cudaSuccess) return cuda_fail(e, "boundary_xform");
+    }
+    // 2. the PBF step
+    rc = run_steps(s, dt, 1);
+    if (rc) return rc;
+    if (b.nb == 0) return sync_and_check(s);
+    // 3. boundary density on the final positions (fluid_world.cpp:101-123)
+    rc = ensure_boundary_grid(s, C.grid.nslots);
+    if (rc) return rc;
+    rc = ensure_fluid_queries(s);
+    if (rc) return rc;
+    cudaError_t e = index_build(b.idx, b.world, nullptr, b.nb, C, b.sort, st);
+    QuerySet fq{b.fq_cell, s->B.sown, s->B.btab};
+    if (e == cudaSuccess) e = index_classify(fq, s->B.x, s->n, b.idx, C, st);
+    if (e == cudaSuccess) e = boundary_density(s->B.x, s->n, fq, b.idx, s->B.rho, C, st);
+    if (e != cudaSuccess) return cuda_fail(e, "boundary density");
+    // 4. coupling forces from a fresh fluid grid on the final positions
+    //    (fluid_world.cpp:125-174); the step's sorted buffers are free now.
+    PointIndex fidx;
+    fidx.keys = s->B.keys;
+    fidx.skeys = s->B.skeys;
+    fidx.sidx = s->B.sidx;
+    fidx.rkeys = s->B.rkeys;
+    fidx.rsorted = s->B.rsorted;
+    fidx.ridx = s->B.ridx;
+    fidx.pos_of = s->B.pos_of;
+    fidx.kpos = s->B.kpos;
+    fidx.bend = s->B.bend;
+    fidx.spos = s->B.xb;
+    fidx.scell = s->B.scell;
+    fidx.off = s->B.off;
+    fidx.slot_alias = s->B.slot_alias;
+    e = index_build(fidx, s->B.x, s->B.rho, s->n, C, s->sort, st);
+    if (e == cudaSuccess) e = index_classify(b.bq, b.world, b.nb, fidx, C, st);
+    if (e == cudaSuccess)
+        e = coupling_forces(b.world, b.body, b.body_dyn, b.nb, nbodies, b.bq, fidx, b.Fb, C, st);
+    if (nbodies > 0) {
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b.force3, force3, (size_t)nbodies * 12, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b.torque3, torque3, (size_t)nbodies * 12, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = body_reduce(b.Fb, b.world, b.list_off, b.list, b.body_pos, nbodies, b.force3,
+                            b.torque3, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(force3, b.force3, (size_t)nbodies * 12, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(torque3, b.torque3, (size_t)nbodies * 12, cudaMemcpyDeviceToHost, st);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "coupling forces");
+    return sync_and_check(s);
+}
+
+int pbf_scene_read_boundary(pbf_scene* s, float* world3) {
+    if (!s || (s->bnd.nb > 0 && !world3)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    if (b.nb == 0) return PBF_OK;
+    std::vector<float4> w(b.nb);
+    PBF_CUDA(cudaMemcpyAsync(w.data(), b.world, (size_t)b.nb * 16, cudaMemcpyDeviceToHost, s->stream));
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < b.nb; ++i) {
+        world3[3 * i] = w[i].x;
+        world3[3 * i + 1] = w[i].y;
+        world3[3 * i + 2] = w[i].z;
+    }
+    return PBF_OK;
+}
+
+int pbf_boundary_volumes(int device, int nb, const float* world3, float kernel_radius,
+                         float* psi_out) {
+    if (nb < 0 || (nb > 0 && (!world3 || !psi_out)))
+        return fail(PBF_ERR_INVALID_ARG, "bad arguments");
+    if (!(kernel_radius > 0.0f)) return fail(PBF_ERR_INVALID_ARG, "kernel_radius must be > 0");
+    if (nb == 0) return PBF_OK;
+    // A scratch scene whose "fluid" is the boundary sample: reuses the grid fit.
+    pbf_settings st;
+    pbf_default_settings(&st);
+    st.kernel_radius = kernel_radius;
+    pbf_scene* s = nullptr;
+    int rc = pbf_scene_create(device, &st, 0, nullptr, nullptr, 0.0f, &s);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        DeviceGuard dg(s->device);
+        update_bbox(s, world3, nb);
+        StepConsts C;
+        rc = make_consts(s, 1.0f, C);
+        std::vector<int> bodies(nb, -1);
+        std::vector<float> zero(nb, 0.0f);
+        if (!rc) rc = alloc_boundary(s, nb);
+        if (!rc) rc = ensure_boundary_grid(s, C.grid.nslots);
+        auto& b = s->bnd;
+        cudaError_t e = cudaSuccess;
+        if (!rc) {
+            std::vector<float4> l(nb);
+            for (int i = 0; i < nb; ++i)
+                l[i] = make_float4(world3[3 * i], world3[3 * i + 1], world3[3 * i + 2], 0.0f);
+            e = cudaMemcpyAsync(b.world, l.data(), (size_t)nb * 16, cudaMemcpyHostToDevice, s->stream);
+            if (e == cudaSuccess) e = index_build(b.idx, b.world, nullptr, nb, C, b.sort, s->stream);
+            if (e == cudaSuccess) e = index_classify(b.bq, b.world, nb, b.idx, C, s->stream);
+            float* dpsi = reinterpret_cast<float*>(b.Fb);
+            if (e == cudaSuccess) e = boundary_volumes(b.world, nb, b.bq, b.idx, dpsi, C, s->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(psi_out, dpsi, (size_t)nb * 4, cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            if (e != cudaSuccess) rc = cuda_fail(e, "pbf_boundary_volumes");
+        }
+    }
+    const int rc2 = pbf_scene_destroy(s);
+    return rc ? rc : rc2;
 }
 
 int pbf_sort_pairs_host(int device, int n, const unsigned* keys, int key_bits, unsigned* out_keys,

@@ -102,7 +102,10 @@ __device__ __forceinline__ uint32_t key_lower_bound(const unsigned long long* __
 }
 
 // Visits the candidate sorted positions q of a particle whose step-start cell
-// is `cell`, in the reference's order.
+// is `cell`, in the reference's order.  The particle itself is among them:
+// the reference skips j == i in every pass but the density, and the kernels
+// rely on its terms being exact zeros instead (spiky_grad(0) = 0 and the
+// velocity / |omega| differences vanish), which leaves every sum unchanged.
 //
 // cell.w == 0 (clean): every neighbour bucket holds exactly the particles of
 // that cell, so each (dz, dy) row of three cells is one contiguous range of
@@ -126,6 +129,7 @@ __device__ __forceinline__ void for_each_candidate(const int4 cell, const uint32
                 const int wx = wrap(cell.x - 1, G.ox, G.gx);
                 if (wx + 2 < G.gx) {
                     const uint32_t q1 = __ldg(off + row + wx + 3);
+#pragma unroll 4
                     for (uint32_t q = __ldg(off + row + wx); q < q1; ++q) f(q);
                 } else {
                     for (int d = 0; d < 3; ++d) {
@@ -250,19 +254,21 @@ k_buckets(const unsigned long long* __restrict__ rsorted, const uint32_t* __rest
     bend[kp] = (uint32_t)e | (pure ? 0u : kImpureBit);
 }
 
-// Marks particles whose neighbourhood differs from the reference's buckets
-// (sown[p] = owner + 1, else 0) and stores their 27 bucket starts in row
-// `owner` of btab.  Within a warp, one lane per distinct
-// cell does the 27 lookups; the other lanes of the cell reuse its table row.
+// Marks query points whose neighbourhood differs from the reference's
+// buckets over a source point set (qown[p] = owner + 1, else 0) and stores
+// their 27 bucket starts in row `owner` of btab.  Query cells are qcell[0..nq),
+// the source's key-sorted buckets are (rsorted, kpos, bend) with cells scell
+// and slot alias flags of the source's grid.  Within a warp, one lane per
+// distinct cell does the 27 lookups; the other lanes of the cell reuse its row.
 __global__ void __launch_bounds__(kBlock)
-k_classify(const int4* __restrict__ scell, const unsigned long long* __restrict__ rsorted,
-           const uint32_t* __restrict__ kpos, const uint32_t* __restrict__ bend,
-           const unsigned char* __restrict__ slot_alias, uint32_t* __restrict__ btab,
-           int* __restrict__ sown, const StepConsts C) {
+k_classify(const int4* __restrict__ qcell, int nq, const int4* __restrict__ scell, int ns,
+           const unsigned long long* __restrict__ rsorted, const uint32_t* __restrict__ kpos,
+           const uint32_t* __restrict__ bend, const unsigned char* __restrict__ slot_alias,
+           uint32_t* __restrict__ btab, int* __restrict__ qown, const StepConsts C) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = p < (uint32_t)C.n;
+    const bool active = p < (uint32_t)nq;
     const int lane = threadIdx.x & 31;
-    const int4 cell = active ? scell[p] : make_int4(0x7fffffff, 0x7fffffff, 0x7fffffff, 0);
+    const int4 cell = active ? qcell[p] : make_int4(0x7fffffff, 0x7fffffff, 0x7fffffff, 0);
     const unsigned long long kxy =
         ((unsigned long long)(unsigned)cell.x << 32) | (unsigned long long)(unsigned)cell.y;
     const uint32_t same = __match_any_sync(0xffffffffu, kxy) &
@@ -278,8 +284,8 @@ k_classify(const int4* __restrict__ scell, const unsigned long long* __restrict_
                 for (int dx = -1; dx <= 1; ++dx, ++m) {
                     const int nx = cell.x + dx, ny = cell.y + dy, nz = cell.z + dz;
                     const unsigned long long k = ref_hash(nx, ny, nz);
-                    const uint32_t lb = key_lower_bound(rsorted, (uint32_t)C.n, k);
-                    if (lb < (uint32_t)C.n && __ldg(rsorted + lb) == k) {
+                    const uint32_t lb = key_lower_bound(rsorted, (uint32_t)ns, k);
+                    if (lb < (uint32_t)ns && __ldg(rsorted + lb) == k) {
                         tab[m] = lb;
                         const uint32_t e = __ldg(bend + lb);
                         const int4 c0 = scell[__ldg(kpos + lb)];
@@ -296,7 +302,7 @@ k_classify(const int4* __restrict__ scell, const unsigned long long* __restrict_
     }
     const int d = __shfl_sync(0xffffffffu, dirty, leader);
     const uint32_t owner = __shfl_sync(0xffffffffu, p, leader);
-    if (active) sown[p] = d ? (int)(owner + 1u) : 0;
+    if (active) qown[p] = d ? (int)(owner + 1u) : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -334,16 +340,14 @@ k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, floa
         const float r_sq = sqn(rx, ry, rz);
         if (r_sq < C.cut) {
             density += C.mass * poly6(r_sq, C);
-            if (q != p) {
-                const float c = spiky_coeff(r_sq, C);
-                const float gx = C.mr * (c * rx);
-                const float gy = C.mr * (c * ry);
-                const float gz = C.mr * (c * rz);
-                sum_grad_sq += sqn(gx, gy, gz);
-                gix += gx;
-                giy += gy;
-                giz += gz;
-            }
+            const float c = spiky_coeff(r_sq, C);
+            const float gx = C.mr * (c * rx);
+            const float gy = C.mr * (c * ry);
+            const float gz = C.mr * (c * rz);
+            sum_grad_sq += sqn(gx, gy, gz);
+            gix += gx;
+            giy += gy;
+            giz += gz;
         }
     });
     sum_grad_sq += sqn(gix, giy, giz);
@@ -383,7 +387,6 @@ k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4*
     const float4 xi = xin[p];
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        if (q == p) return;
         const float4 xj = __ldg(xin + q);
         const float rx = xi.x - xj.x;
         const float ry = xi.y - xj.y;
@@ -455,8 +458,7 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
     if (C.xsph_on) {
         float cx = 0.0f, cy = 0.0f, cz = 0.0f;
         for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-            if (q == p) return;
-            const float4 xj = __ldg(xin + q);
+                const float4 xj = __ldg(xin + q);
             const float rx = xi.x - xj.x;
             const float ry = xi.y - xj.y;
             const float rz = xi.z - xj.z;
@@ -489,7 +491,6 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
     const float4 vi = sv[p];
     float cx = 0.0f, cy = 0.0f, cz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        if (q == p) return;
         const float4 xj = __ldg(xin + q);
         const float rx = xi.x - xj.x;
         const float ry = xi.y - xj.y;
@@ -536,7 +537,6 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     const float4 wi = som[p];
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        if (q == p) return;
         const float4 xj = __ldg(xin + q);
         const float rx = xi.x - xj.x;
         const float ry = xi.y - xj.y;
@@ -642,8 +642,8 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     if (C.hash_compat) {
         k_buckets<<<grid_of(n, 256), 256, 0, st>>>(B.rsorted, B.ridx, B.pos_of, B.scell, B.kpos,
                                                    B.bend, n);
-        k_classify<<<nb, kBlock, 0, st>>>(B.scell, B.rsorted, B.kpos, B.bend, B.slot_alias, B.btab,
-                                          B.sown, C);
+        k_classify<<<nb, kBlock, 0, st>>>(B.scell, n, B.scell, n, B.rsorted, B.kpos, B.bend,
+                                          B.slot_alias, B.btab, B.sown, C);
     } else {
         e = cudaMemsetAsync(B.sown, 0, (size_t)n * 4, st);
         if (e != cudaSuccess) return e;
