@@ -1,0 +1,294 @@
+// pybind11 module novaphy_gb300._core: NovaPhy's fluid bindings
+// (python/bindings/bind_fluid.cpp) with the same class, method and argument
+// names, plus the slices of the sim/core/math bindings that FluidWorld and its
+// callers use (bind_sim.cpp, bind_core.cpp, bind_math.cpp,
+// bind_performance.cpp).  Vector3 values are float32 numpy arrays of shape
+// (3,), like the reference's Eigen binding; any length-3 sequence is accepted.
+#include <cstring>
+
+#include <pybind11/numpy.h>
+#include <pybind11/pybind11.h>
+#include <pybind11/stl.h>
+
+#include "novaphy_host.hpp"
+
+namespace py = pybind11;
+using namespace novaphy_gb300;
+
+namespace pybind11 {
+namespace detail {
+template <>
+struct type_caster<Vec3> {
+    PYBIND11_TYPE_CASTER(Vec3, const_name("Vector3"));
+    bool load(handle src, bool) {
+        if (!src || !PySequence_Check(src.ptr()) || PyUnicode_Check(src.ptr())) return false;
+        auto seq = reinterpret_borrow<sequence>(src);
+        if (seq.size() != 3) return false;
+        try {
+            for (size_t i = 0; i < 3; ++i) value[(int)i] = seq[i].cast<float>();
+        } catch (const cast_error&) {
+            return false;
+        }
+        return true;
+    }
+    static handle cast(const Vec3& v, return_value_policy, handle) {
+        array_t<float> a(3);
+        auto m = a.mutable_unchecked<1>();
+        m(0) = v.x;
+        m(1) = v.y;
+        m(2) = v.z;
+        return a.release();
+    }
+};
+}  // namespace detail
+}  // namespace pybind11
+
+namespace {
+
+py::array_t<float> positions_array(const std::vector<Vec3>& v) {
+    py::array_t<float> a({(py::ssize_t)v.size(), (py::ssize_t)3});
+    if (!v.empty()) std::memcpy(a.mutable_data(), &v[0].x, v.size() * sizeof(Vec3));
+    return a;
+}
+
+}  // namespace
+
+PYBIND11_MODULE(_core, m) {
+    m.doc() = "NovaPhy's PBF fluid API on the GB300 (sm_103a) behind a C ABI";
+
+    // --- math / core slices ---
+    py::class_<Transform>(m, "Transform")
+        .def(py::init<>())
+        .def(py::init([](const Vec3& p, py::sequence q) {
+                 if (q.size() != 4) throw py::value_error("rotation must be [x, y, z, w]");
+                 return Transform(p, Quat{q[3].cast<float>(), q[0].cast<float>(),
+                                          q[1].cast<float>(), q[2].cast<float>()});
+             }),
+             py::arg("position"), py::arg("rotation"))
+        .def_readwrite("position", &Transform::position)
+        .def_property(
+            "rotation",
+            [](const Transform& t) {
+                py::array_t<float> a(4);
+                auto r = a.mutable_unchecked<1>();
+                r(0) = t.rotation.x;
+                r(1) = t.rotation.y;
+                r(2) = t.rotation.z;
+                r(3) = t.rotation.w;
+                return a;
+            },
+            [](Transform& t, py::sequence q) {
+                t.rotation = Quat{q[3].cast<float>(), q[0].cast<float>(), q[1].cast<float>(),
+                                  q[2].cast<float>()};
+            })
+        .def("transform_point", &Transform::transform_point, py::arg("point"))
+        .def_static("identity", &Transform::identity)
+        .def_static("from_translation", &Transform::from_translation, py::arg("translation"))
+        .def_static("from_axis_angle", &Transform::from_axis_angle, py::arg("axis"),
+                    py::arg("angle"));
+
+    py::enum_<ShapeType>(m, "ShapeType")
+        .value("Box", ShapeType::Box)
+        .value("Sphere", ShapeType::Sphere)
+        .value("Plane", ShapeType::Plane);
+
+    py::class_<CollisionShape>(m, "CollisionShape")
+        .def(py::init<>())
+        .def_readwrite("type", &CollisionShape::type)
+        .def_readwrite("body_index", &CollisionShape::body_index)
+        .def_readwrite("local_transform", &CollisionShape::local_transform)
+        .def_readwrite("friction", &CollisionShape::friction)
+        .def_readwrite("restitution", &CollisionShape::restitution)
+        .def_readwrite("box_half_extents", &CollisionShape::half_extents)
+        .def_readwrite("sphere_radius", &CollisionShape::radius)
+        .def_readwrite("plane_normal", &CollisionShape::normal)
+        .def_readwrite("plane_offset", &CollisionShape::offset)
+        .def_static("make_box", &CollisionShape::make_box, py::arg("half_extents"),
+                    py::arg("body_idx"), py::arg("local") = Transform::identity(),
+                    py::arg("friction") = 0.5f, py::arg("restitution") = 0.3f)
+        .def_static("make_sphere", &CollisionShape::make_sphere, py::arg("radius"),
+                    py::arg("body_idx"), py::arg("local") = Transform::identity(),
+                    py::arg("friction") = 0.5f, py::arg("restitution") = 0.3f)
+        .def_static("make_plane", &CollisionShape::make_plane, py::arg("normal"), py::arg("offset"),
+                    py::arg("friction") = 0.5f, py::arg("restitution") = 0.0f);
+
+    py::class_<RigidBody>(m, "RigidBody")
+        .def(py::init<>())
+        .def_readwrite("mass", &RigidBody::mass)
+        .def_readwrite("com", &RigidBody::com)
+        .def("inv_mass", &RigidBody::inv_mass)
+        .def("is_static", &RigidBody::is_static)
+        .def_static("from_box", &RigidBody::from_box, py::arg("mass"), py::arg("half_extents"))
+        .def_static("from_sphere", &RigidBody::from_sphere, py::arg("mass"), py::arg("radius"))
+        .def_static("make_static", &RigidBody::make_static);
+
+    py::class_<Model>(m, "Model")
+        .def(py::init<>())
+        .def_readonly("bodies", &Model::bodies)
+        .def_readonly("shapes", &Model::shapes)
+        .def_readonly("initial_transforms", &Model::initial_transforms)
+        .def_property_readonly("num_bodies", &Model::num_bodies)
+        .def_property_readonly("num_shapes", &Model::num_shapes);
+
+    py::class_<ModelBuilder>(m, "ModelBuilder")
+        .def(py::init<>())
+        .def("add_body", &ModelBuilder::add_body, py::arg("body"),
+             py::arg("transform") = Transform::identity())
+        .def("add_shape", &ModelBuilder::add_shape, py::arg("shape"))
+        .def("add_ground_plane", &ModelBuilder::add_ground_plane, py::arg("y") = 0.0f,
+             py::arg("friction") = 0.5f, py::arg("restitution") = 0.0f)
+        .def("build", &ModelBuilder::build);
+
+    py::class_<SolverSettings>(m, "SolverSettings")
+        .def(py::init<>())
+        .def_readwrite("velocity_iterations", &SolverSettings::velocity_iterations)
+        .def_readwrite("baumgarte", &SolverSettings::baumgarte)
+        .def_readwrite("slop", &SolverSettings::slop)
+        .def_readwrite("warm_starting", &SolverSettings::warm_starting)
+        .def_readwrite("sleep_enabled", &SolverSettings::sleep_enabled);
+
+    py::class_<SimState>(m, "SimState")
+        .def(py::init<>())
+        .def_readonly("transforms", &SimState::transforms)
+        .def_readonly("linear_velocities", &SimState::linear_velocities)
+        .def_readonly("angular_velocities", &SimState::angular_velocities)
+        .def("set_linear_velocity", &SimState::set_linear_velocity, py::arg("body_index"),
+             py::arg("velocity"))
+        .def("set_angular_velocity", &SimState::set_angular_velocity, py::arg("body_index"),
+             py::arg("velocity"));
+
+    py::class_<PhaseStat>(m, "PerformancePhaseStat")
+        .def_readonly("name", &PhaseStat::name)
+        .def_readonly("last_ms", &PhaseStat::last_ms)
+        .def_readonly("avg_ms", &PhaseStat::avg_ms)
+        .def_readonly("max_ms", &PhaseStat::max_ms)
+        .def_readonly("samples", &PhaseStat::samples);
+    py::class_<MetricValue>(m, "PerformanceMetric")
+        .def_readonly("name", &MetricValue::name)
+        .def_readonly("value", &MetricValue::value);
+    py::class_<PerformanceMonitor>(m, "PerformanceMonitor")
+        .def(py::init<>())
+        .def_readwrite("enabled", &PerformanceMonitor::enabled)
+        .def("phase_stats", &PerformanceMonitor::phase_stats)
+        .def("last_frame_metrics", &PerformanceMonitor::last_frame_metrics)
+        .def_property_readonly("frame_count", &PerformanceMonitor::frame_count)
+        .def_property_readonly("last_frame_total_ms", &PerformanceMonitor::last_frame_total_ms)
+        .def("reset", &PerformanceMonitor::reset);
+
+    py::class_<World>(m, "World")
+        .def(py::init<const Model&, SolverSettings>(), py::arg("model"),
+             py::arg("solver_settings") = SolverSettings{})
+        .def("step", &World::step, py::arg("dt"), py::call_guard<py::gil_scoped_release>())
+        .def("set_gravity", &World::set_gravity, py::arg("gravity"))
+        .def_property_readonly("gravity", &World::gravity)
+        .def_property_readonly("state", &World::state, py::return_value_policy::reference_internal)
+        .def_property_readonly("model", &World::model, py::return_value_policy::reference_internal)
+        .def_property_readonly("performance_monitor", &World::performance_monitor,
+                               py::return_value_policy::reference_internal)
+        .def("apply_force", &World::apply_force, py::arg("body_index"), py::arg("force"))
+        .def("apply_torque", &World::apply_torque, py::arg("body_index"), py::arg("torque"));
+
+    // --- fluid (bind_fluid.cpp) ---
+    py::class_<SPHKernels>(m, "SPHKernels")
+        .def_static("poly6", &SPHKernels::poly6, py::arg("r_sq"), py::arg("h"))
+        .def_static("spiky_grad", &SPHKernels::spiky_grad, py::arg("r"), py::arg("h"))
+        .def_static("spiky", &SPHKernels::spiky, py::arg("r_len"), py::arg("h"))
+        .def_static("cubic_spline", &SPHKernels::cubic_spline, py::arg("r_len"), py::arg("h"));
+
+    py::class_<FluidBlockDef>(m, "FluidBlockDef")
+        .def(py::init<>())
+        .def_readwrite("lower", &FluidBlockDef::lower)
+        .def_readwrite("upper", &FluidBlockDef::upper)
+        .def_readwrite("particle_spacing", &FluidBlockDef::particle_spacing)
+        .def_readwrite("rest_density", &FluidBlockDef::rest_density)
+        .def_readwrite("initial_velocity", &FluidBlockDef::initial_velocity);
+
+    py::class_<ParticleState>(m, "ParticleState")
+        .def(py::init<>())
+        .def("init", &ParticleState::init, py::arg("initial_positions"),
+             py::arg("initial_velocity") = Vec3{})
+        .def("clear", &ParticleState::clear)
+        .def_property_readonly("num_particles", &ParticleState::num_particles)
+        .def_readonly("positions", &ParticleState::positions)
+        .def_readonly("velocities", &ParticleState::velocities)
+        .def_readonly("densities", &ParticleState::densities)
+        .def_readonly("lambdas", &ParticleState::lambdas)
+        // (n, 3) / (n,) float32 array copies: one call instead of n Vector3 objects
+        .def_property_readonly("positions_array",
+                               [](const ParticleState& s) { return positions_array(s.positions); })
+        .def_property_readonly("velocities_array",
+                               [](const ParticleState& s) { return positions_array(s.velocities); })
+        .def_property_readonly("densities_array", [](const ParticleState& s) {
+            return py::array_t<float>((py::ssize_t)s.densities.size(), s.densities.data());
+        });
+
+    py::class_<SpatialHashGrid>(m, "SpatialHashGrid")
+        .def(py::init<float>(), py::arg("cell_size") = 0.1f)
+        .def("build", &SpatialHashGrid::build, py::arg("positions"))
+        .def("clear", &SpatialHashGrid::clear)
+        .def("query_neighbors", &SpatialHashGrid::query_neighbors, py::arg("point"),
+             py::arg("radius"))
+        .def("query_all_pairs", &SpatialHashGrid::query_all_pairs, py::arg("positions"),
+             py::arg("radius"))
+        .def_property("cell_size", &SpatialHashGrid::cell_size, &SpatialHashGrid::set_cell_size);
+
+    py::class_<PBFSettings>(m, "PBFSettings")
+        .def(py::init<>())
+        .def_readwrite("rest_density", &PBFSettings::rest_density)
+        .def_readwrite("kernel_radius", &PBFSettings::kernel_radius)
+        .def_readwrite("particle_radius", &PBFSettings::particle_radius)
+        .def_readwrite("solver_iterations", &PBFSettings::solver_iterations)
+        .def_readwrite("epsilon", &PBFSettings::epsilon)
+        .def_readwrite("xsph_viscosity", &PBFSettings::xsph_viscosity)
+        .def_readwrite("vorticity_epsilon", &PBFSettings::vorticity_epsilon)
+        .def_readwrite("corr_delta_q", &PBFSettings::corr_delta_q)
+        .def_readwrite("corr_k", &PBFSettings::corr_k)
+        .def_readwrite("corr_n", &PBFSettings::corr_n)
+        .def_readwrite("use_domain_bounds", &PBFSettings::use_domain_bounds)
+        .def_readwrite("domain_lower", &PBFSettings::domain_lower)
+        .def_readwrite("domain_upper", &PBFSettings::domain_upper)
+        .def_readwrite("exact_arithmetic", &PBFSettings::exact_arithmetic)
+        .def_readwrite("hash_compat", &PBFSettings::hash_compat)
+        .def("particle_mass", &PBFSettings::particle_mass, py::arg("spacing"));
+
+    py::class_<PBFSolver>(m, "PBFSolver")
+        .def(py::init<const PBFSettings&>(), py::arg("settings") = PBFSettings{})
+        .def("step", &PBFSolver::step, py::arg("state"), py::arg("dt"), py::arg("gravity"),
+             py::arg("particle_mass"), py::call_guard<py::gil_scoped_release>())
+        .def_property_readonly("settings", &PBFSolver::settings,
+                               py::return_value_policy::reference_internal);
+
+    py::class_<BoundaryParticle>(m, "BoundaryParticle")
+        .def(py::init<>())
+        .def_readwrite("local_position", &BoundaryParticle::local_position)
+        .def_readwrite("body_index", &BoundaryParticle::body_index)
+        .def_readwrite("volume", &BoundaryParticle::volume);
+
+    py::class_<FluidWorld, World>(m, "FluidWorld")
+        .def(py::init<const Model&, const std::vector<FluidBlockDef>&, SolverSettings, PBFSettings,
+                      float>(),
+             py::arg("model"), py::arg("fluid_blocks") = std::vector<FluidBlockDef>{},
+             py::arg("solver_settings") = SolverSettings{}, py::arg("pbf_settings") = PBFSettings{},
+             py::arg("boundary_extent") = 1.0f)
+        .def("step", &FluidWorld::step, py::arg("dt"), py::call_guard<py::gil_scoped_release>())
+        .def_property_readonly("fluid_state", &FluidWorld::fluid_state,
+                               py::return_value_policy::reference_internal)
+        .def_property_readonly("num_particles", &FluidWorld::num_particles)
+        .def_property_readonly("num_boundary_particles", &FluidWorld::num_boundary_particles)
+        .def_property_readonly("boundary_particles", &FluidWorld::boundary_particles,
+                               py::return_value_policy::reference_internal)
+        .def_property_readonly("pbf_settings", &FluidWorld::pbf_settings,
+                               py::return_value_policy::reference_internal);
+
+    m.def("generate_fluid_block", &generate_fluid_block, py::arg("block_def"));
+    m.def("sample_model_boundaries", &sample_model_boundaries, py::arg("model"),
+          py::arg("spacing"), py::arg("plane_extent") = 1.0f);
+
+    py::register_exception_translator([](std::exception_ptr p) {
+        try {
+            if (p) std::rethrow_exception(p);
+        } catch (const std::invalid_argument& e) {
+            PyErr_SetString(PyExc_ValueError, e.what());
+        }
+    });
+}

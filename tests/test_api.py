@@ -1,0 +1,152 @@
+"""The NovaPhy-compatible Python API (novaphy_gb300._core) on CPU: kernels,
+fluid blocks, particle state, host hash grid, settings and boundary sampling.
+Written after the reference's tests/python/test_fluid.py and test_coupling.py;
+the host kernels and sampling are also compared bit-for-bit with the oracle."""
+import math
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+import novaphy_gb300 as novaphy
+
+
+def test_kernel_values_and_normalisation():
+    h = 0.1
+    assert novaphy.SPHKernels.poly6(0.0, h) > 0
+    assert abs(novaphy.SPHKernels.poly6(h * h, h)) < 1e-10
+    assert novaphy.SPHKernels.poly6(h * h * 1.1, h) == 0.0
+    dr = h / 1000
+    integral = sum(novaphy.SPHKernels.poly6(((i + 0.5) * dr) ** 2, h) * 4 * math.pi *
+                   ((i + 0.5) * dr) ** 2 * dr for i in range(1000))
+    npt.assert_allclose(integral, 1.0, atol=0.02)
+    assert novaphy.SPHKernels.spiky(0.0, h) > 0 and novaphy.SPHKernels.spiky(h, h) == 0.0
+    npt.assert_allclose(novaphy.SPHKernels.spiky_grad(np.array([h, 0, 0], np.float32), h), 0,
+                        atol=1e-7)
+    assert novaphy.SPHKernels.spiky_grad(np.array([0.05, 0, 0], np.float32), h)[0] < 0
+    assert novaphy.SPHKernels.cubic_spline(0.0, h) > 0
+    assert novaphy.SPHKernels.cubic_spline(h, h) == 0.0
+
+
+def test_host_kernels_match_oracle(port):
+    rng = np.random.default_rng(3)
+    for h in (np.float32(0.1), np.float32(0.04)):
+        for r in rng.uniform(0, 1.2 * h, 200).astype(np.float32):
+            assert novaphy.SPHKernels.poly6(float(r * r), float(h)) == port.poly6(r * r, h)
+            assert novaphy.SPHKernels.spiky(float(r), float(h)) == port.spiky(r, h)
+            v = (rng.normal(size=3) * r).astype(np.float32)
+            assert np.array_equal(novaphy.SPHKernels.spiky_grad(v, float(h)), port.spiky_grad(v, h))
+
+
+def test_fluid_block_generation():
+    b = novaphy.FluidBlockDef()
+    npt.assert_allclose(b.particle_spacing, 0.02, atol=1e-6)
+    npt.assert_allclose(b.lower, [0, 0, 0])
+    b.lower = np.array([0, 0, 0], np.float32)
+    b.upper = np.array([0.1, 0.1, 0.1], np.float32)
+    b.particle_spacing = 0.05
+    assert len(novaphy.generate_fluid_block(b)) == 27
+    b.upper = [0.2, 0.0, 0.0]
+    b.particle_spacing = 0.1
+    p = novaphy.generate_fluid_block(b)
+    assert len(p) == 3
+    for a, c in zip(p, p[1:]):
+        npt.assert_allclose(np.linalg.norm(c - a), 0.1, atol=1e-5)
+
+
+def test_particle_state():
+    st = novaphy.ParticleState()
+    st.init([np.zeros(3, np.float32), [1, 0, 0], (0, 1, 0)])
+    assert st.num_particles == 3 and len(st.velocities) == 3 and len(st.densities) == 3
+    st.init([[0, 0, 0]], np.array([1.0, 2.0, 3.0], np.float32))
+    npt.assert_allclose(st.velocities[0], [1, 2, 3])
+    assert st.positions_array.shape == (1, 3)
+    st.clear()
+    assert st.num_particles == 0
+
+
+def test_host_hash_grid_matches_reference_order(port):
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden",
+                                           "grid.npz"))
+    grid = novaphy.SpatialHashGrid(0.1)
+    grid.build(g["cloud"])
+    for k, q in enumerate(g["queries"]):
+        want = g["cand"][g["offsets"][k]:g["offsets"][k + 1]]
+        assert np.array_equal(grid.query_neighbors(q, 0.1), want)
+    pts = np.random.default_rng(42).uniform(0, 1, (500, 3)).astype(np.float32)
+    grid.build(pts)
+    q = np.array([0.5, 0.5, 0.5], np.float32)
+    cand = set(grid.query_neighbors(q, 0.1))
+    assert {i for i, p in enumerate(pts) if np.linalg.norm(p - q) < 0.1} <= cand
+    # known answer: tests/cpp/test_core_span_apis.cpp:42-50
+    three = [[0, 0, 0], [0.1, 0, 0], [0.5, 0, 0]]
+    grid = novaphy.SpatialHashGrid(0.2)
+    grid.build(three)
+    assert grid.query_all_pairs(three, 0.2) == [(0, 1)]
+
+
+def test_settings_defaults_and_mass():
+    s = novaphy.PBFSettings()
+    npt.assert_allclose(s.rest_density, 1000.0)
+    npt.assert_allclose(s.kernel_radius, 0.1, atol=1e-6)
+    assert s.solver_iterations == 4 and s.corr_n == 4 and not s.use_domain_bounds
+    assert s.exact_arithmetic and s.hash_compat
+    npt.assert_allclose(s.particle_mass(0.05), 0.125, rtol=1e-5)
+
+
+def test_boundary_sampling_matches_oracle(port):
+    mb = novaphy.ModelBuilder()
+    half = np.array([0.12, 0.08, 0.1], np.float32)
+    b0 = mb.add_body(novaphy.RigidBody.from_box(1.0, half))
+    local = novaphy.Transform(np.array([0.01, 0.02, 0.0], np.float32),
+                              [0.0, 0.0, math.sin(0.3), math.cos(0.3)])
+    mb.add_shape(novaphy.CollisionShape.make_box(half, b0, local))
+    b1 = mb.add_body(novaphy.RigidBody.from_sphere(1.0, 0.1))
+    mb.add_shape(novaphy.CollisionShape.make_sphere(0.1, b1))
+    mb.add_shape(novaphy.CollisionShape.make_plane(np.array([0, 0, 1], np.float32), 0.05))
+    model = mb.build()
+    got = novaphy.sample_model_boundaries(model, 0.025, plane_extent=0.3)
+    q = local.rotation  # [x, y, z, w]
+    want = np.concatenate([
+        port.sample_box(half, local.position, [q[3], q[0], q[1], q[2]], np.float32(0.025)),
+        port.sample_sphere(np.float32(0.1), (0, 0, 0), (1, 0, 0, 0), np.float32(0.025)),
+        port.sample_plane(np.array([0, 0, 1], np.float32), np.float32(0.05), np.float32(0.025),
+                          np.float32(0.3)),
+    ])
+    assert len(got) == len(want)
+    assert np.array_equal(np.stack([p.local_position for p in got]), want)
+    assert [p.body_index for p in got].count(-1) == len(want) - sum(
+        1 for p in got if p.body_index >= 0)
+
+
+def test_reference_sampling_examples():
+    mb = novaphy.ModelBuilder()
+    half = np.array([0.5, 0.5, 0.5], np.float32)
+    idx = mb.add_body(novaphy.RigidBody.from_box(1.0, half))
+    mb.add_shape(novaphy.CollisionShape.make_box(half, idx))
+    ps = novaphy.sample_model_boundaries(mb.build(), 0.25)
+    assert len(ps) > 0 and all(p.body_index == 0 for p in ps)
+    mb = novaphy.ModelBuilder()
+    idx = mb.add_body(novaphy.RigidBody.from_sphere(1.0, 0.5))
+    mb.add_shape(novaphy.CollisionShape.make_sphere(0.5, idx))
+    ps = novaphy.sample_model_boundaries(mb.build(), 0.1)
+    assert len(ps) > 10
+    for p in ps:
+        npt.assert_allclose(np.linalg.norm(p.local_position), 0.5, atol=0.01)
+    mb = novaphy.ModelBuilder()
+    mb.add_ground_plane(y=0.0)
+    ps = novaphy.sample_model_boundaries(mb.build(), 0.2, plane_extent=0.5)
+    assert len(ps) > 0 and all(abs(p.local_position[1]) < 1e-5 and p.body_index == -1 for p in ps)
+    assert len(novaphy.sample_model_boundaries(novaphy.ModelBuilder().build(), 0.1)) == 0
+    bp = novaphy.BoundaryParticle()
+    npt.assert_allclose(bp.local_position, [0, 0, 0])
+    assert bp.body_index == -1 and bp.volume == 0.0
+
+
+def test_stepping_needs_a_device_and_says_so():
+    if novaphy.capi.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    st = novaphy.ParticleState()
+    st.init([[0, 0, 0], [0.02, 0, 0]])
+    with pytest.raises(RuntimeError, match="CUDA"):
+        novaphy.PBFSolver(novaphy.PBFSettings()).step(st, 1 / 60, [0, -9.81, 0], 0.125)

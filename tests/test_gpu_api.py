@@ -1,0 +1,172 @@
+"""The NovaPhy-compatible API on the GPU: PBFSolver and FluidWorld, written
+after the reference's tests/python/test_pbf.py, test_coupling.py and
+test_performance_monitor.py, plus bit-exact checks against the oracle."""
+import os
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+import novaphy_gb300 as novaphy
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def make_pbf_state(spacing=0.025, block_size=0.3):
+    b = novaphy.FluidBlockDef()
+    b.lower = np.array([0, 0, 0], np.float32)
+    b.upper = np.array([block_size] * 3, np.float32)
+    b.particle_spacing = spacing
+    s = novaphy.PBFSettings()
+    s.kernel_radius = spacing * 4.0
+    st = novaphy.ParticleState()
+    st.init(novaphy.generate_fluid_block(b))
+    return st, s, s.particle_mass(spacing)
+
+
+def test_pbf_step_runs_and_particles_fall():
+    st, s, m = make_pbf_state()
+    solver = novaphy.PBFSolver(s)
+    y0 = np.mean([p[1] for p in st.positions])
+    for _ in range(10):
+        solver.step(st, 1 / 60, np.array([0, -9.81, 0], np.float32), m)
+    assert np.mean([p[1] for p in st.positions]) < y0
+    assert max(np.linalg.norm(v) for v in st.velocities) > 0
+
+
+def test_zero_gravity_com_and_density():
+    st, s, m = make_pbf_state()
+    solver = novaphy.PBFSolver(s)
+    c0 = np.mean(st.positions_array, axis=0)
+    for _ in range(5):
+        solver.step(st, 1 / 60, [0, 0, 0], m)
+    assert np.linalg.norm(np.mean(st.positions_array, axis=0) - c0) < 0.05
+    assert np.mean(st.densities) > 0
+
+
+def test_pbf_solver_is_the_reference_step_bit_for_bit():
+    g = np.load(os.path.join(GOLDEN, "default_scene.npz"))
+    st = novaphy.ParticleState()
+    st.init(g["x0"])
+    s = novaphy.PBFSettings()  # defaults: exact arithmetic, reference hash buckets
+    novaphy.PBFSolver(s).step(st, float(np.float32(1 / 60)), [0, -9.81, 0],
+                              float(np.float32(1000) * np.float32(0.025) ** 3))
+    assert np.array_equal(st.positions_array, g["x1"])
+    assert np.array_equal(st.velocities_array, g["v1"])
+    assert np.array_equal(st.densities_array, g["rho1"])
+    assert np.array_equal(np.array(st.lambdas, np.float32), g["lam1"])
+
+
+def test_settings_edits_are_read_every_step():
+    st, s, m = make_pbf_state(block_size=0.15)
+    solver = novaphy.PBFSolver(s)
+    solver.settings.solver_iterations = 0
+    solver.step(st, 1 / 60, [0, -9.81, 0], m)
+    assert all(d == 0.0 for d in st.densities)  # no density pass ran
+    solver.settings.solver_iterations = 2
+    solver.step(st, 1 / 60, [0, -9.81, 0], m)
+    assert max(st.densities) > 0
+
+
+def block(lower, upper, spacing=0.05):
+    b = novaphy.FluidBlockDef()
+    b.lower = np.array(lower, np.float32)
+    b.upper = np.array(upper, np.float32)
+    b.particle_spacing = spacing
+    return b
+
+
+def test_fluid_world_basics():
+    mb = novaphy.ModelBuilder()
+    mb.add_ground_plane(y=0.0)
+    pbf = novaphy.PBFSettings()
+    pbf.kernel_radius = 0.2
+    w = novaphy.FluidWorld(mb.build(), [block([0, 0.1, 0], [0.2, 0.3, 0.2])],
+                           novaphy.SolverSettings(), pbf, boundary_extent=0.5)
+    assert isinstance(w, novaphy.World)
+    assert w.num_boundary_particles > 0 and w.num_particles > 0
+    n0 = w.num_particles
+    w.step(1 / 60)
+    assert w.fluid_state.num_particles == n0
+    empty = novaphy.FluidWorld(novaphy.ModelBuilder().build(), [], novaphy.SolverSettings(), pbf)
+    empty.step(1 / 60)
+    assert empty.num_particles == 0
+
+
+def sphere_scene(fluid=True, y=0.8, mass=0.5, radius=0.2):
+    mb = novaphy.ModelBuilder()
+    mb.add_ground_plane(y=0.0)
+    idx = mb.add_body(novaphy.RigidBody.from_sphere(mass, radius),
+                      novaphy.Transform.from_translation(np.array([0.1, y, 0.1], np.float32)))
+    mb.add_shape(novaphy.CollisionShape.make_sphere(radius, idx))
+    pbf = novaphy.PBFSettings()
+    pbf.kernel_radius = 0.2
+    pbf.solver_iterations = 2
+    blocks = [block([0, 0.05, 0], [0.3, 0.4, 0.3])] if fluid else []
+    return novaphy.FluidWorld(mb.build(), blocks, novaphy.SolverSettings(), pbf,
+                              boundary_extent=0.5)
+
+
+def test_coupled_simulation_runs_and_sphere_falls():
+    w = sphere_scene()
+    for _ in range(5):
+        w.step(1 / 60)
+    assert w.state.transforms[0].position[1] < 0.8
+    nf = sphere_scene(fluid=False)
+    for _ in range(5):
+        nf.step(1 / 60)
+    assert nf.state.transforms[0].position[1] < 0.8
+
+
+def test_monitor_reports_fluid_phases_and_metrics():
+    w = sphere_scene()
+    mon = w.performance_monitor
+    mon.enabled = True
+    w.step(1 / 60)
+    phases = {p.name for p in mon.phase_stats()}
+    assert {"fluid.total", "fluid.pbf.total", "fluid.rigid_step", "world.total",
+            "world.broadphase.sap"} <= phases
+    metrics = {m.name: m.value for m in mon.last_frame_metrics()}
+    assert metrics["fluid_particles"] > 0 and metrics["boundary_particles"] >= 0
+    assert metrics["pbf_solver_iterations"] == 2.0
+    assert abs(metrics["kernel_radius"] - 0.2) < 1e-6
+    assert mon.frame_count == 1
+    mon.reset()
+    assert mon.frame_count == 0 and mon.phase_stats() == []
+
+
+def test_fluid_world_step_matches_oracle(port):
+    """One FluidWorld step: fluid state = reference PBF step + boundary density;
+    the sphere's new velocity comes from the coupling force the oracle gives."""
+    from oracle.oracle import Settings
+
+    w = sphere_scene(y=0.25, radius=0.12)
+    fs0 = w.fluid_state
+    x0 = fs0.positions_array.copy()
+    bps = w.boundary_particles
+    local = np.stack([b.local_position for b in bps]).astype(np.float32)
+    body = np.array([b.body_index for b in bps], np.int32)
+    psi = np.array([b.volume for b in bps], np.float32)
+    body_pos = np.array([[0.1, 0.25, 0.1]], np.float32)
+    world0 = port.boundary_world_positions(local, body, body_pos, [[1, 0, 0, 0]])
+    assert np.array_equal(port.boundary_volumes(world0, np.float32(0.2)), psi)
+    dt = float(np.float32(1 / 60))
+    w.step(dt)
+    s = Settings.make(kernel_radius=0.2, solver_iterations=2)
+    z = np.zeros(len(x0), np.float32)
+    m = np.float32(1000) * np.float32(0.05) ** 3
+    ox, ov, orho, olam = port.steps(s, x0, np.zeros_like(x0), z, z, dt,
+                                    np.array([0, -9.81, 0], np.float32), m, 1)
+    fs = w.fluid_state
+    assert np.array_equal(fs.positions_array, ox)
+    assert np.array_equal(fs.velocities_array, ov)
+    orho = port.boundary_density(ox, orho, world0, psi, np.float32(0.2), np.float32(1000))
+    assert np.array_equal(fs.densities_array, orho)
+    f, _ = port.coupling_forces(ox, orho, m, world0, body, psi, [1], body_pos, np.float32(0.2),
+                                np.float32(1000))
+    # symplectic Euler of the sphere: v = (g + F / m) dt
+    inv_m = np.float32(1) / np.float32(0.5)
+    g = np.array([0, -9.81, 0], np.float32)
+    v_want = (g + f[0] * inv_m) * np.float32(dt)
+    npt.assert_array_equal(np.asarray(w.state.linear_velocities[0], np.float32), v_want)
