@@ -146,8 +146,10 @@ class Port:
 
     def grid_query(self, pts, cell, q):
         pts = _f32(pts, (-1, 3))
-        out = np.zeros(max(len(pts), 1), np.int32)
-        m = self.lib.orc_grid_query(pts, len(pts), cell, _f32(q, (3,)), out, len(out))
+        probe = np.zeros(1, np.int32)
+        m = self.lib.orc_grid_query(pts, len(pts), cell, _f32(q, (3,)), probe, 0)
+        out = np.zeros(max(m, 1), np.int32)
+        self.lib.orc_grid_query(pts, len(pts), cell, _f32(q, (3,)), out, m)
         return out[:m].copy()
 
     def hash_collisions(self, pts, cell):

@@ -189,6 +189,21 @@ static int grid_candidates(const grid_t* g, const int* c, int* out, int cap) {
     return m;
 }
 
+/* Candidate list of cell c into *buf (grown as needed: with double-visited
+ * buckets a list can be longer than the point count). Returns the count or
+ * -1 on allocation failure. */
+static int grid_candidates_buf(const grid_t* g, const int* c, int** buf, int* cap) {
+    int m = grid_candidates(g, c, NULL, 0);
+    if (m > *cap) {
+        int* nb = (int*)realloc(*buf, sizeof(int) * (size_t)m);
+        if (!nb) return -1;
+        *buf = nb;
+        *cap = m;
+    }
+    grid_candidates(g, c, *buf, *cap);
+    return m;
+}
+
 int orc_grid_query(const float* pts, int n, float cell, const float* q, int* out, int cap) {
     grid_t g;
     if (grid_build(&g, pts, n, cell)) return -1;
@@ -248,7 +263,8 @@ long long orc_neighbor_sets(const float* xs, int n, float h, long long* offsets,
                             long long cap) {
     grid_t g;
     if (grid_build(&g, xs, n, h)) return -1;
-    int* cand = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int ccap = n > 0 ? n : 1;
+    int* cand = (int*)malloc(sizeof(int) * (size_t)ccap);
     if (!cand) {
         grid_free(&g);
         return -1;
@@ -258,7 +274,12 @@ long long orc_neighbor_sets(const float* xs, int n, float h, long long* offsets,
     for (int i = 0; i < n; ++i) {
         int c[3];
         world_to_cell(xs + 3 * i, g.inv, c);
-        int m = grid_candidates(&g, c, cand, n);
+        int m = grid_candidates_buf(&g, c, &cand, &ccap);
+        if (m < 0) {
+            free(cand);
+            grid_free(&g);
+            return -1;
+        }
         if (offsets) offsets[i] = tot;
         /* Candidate lists are sorted by (bucket, index); gather the in-radius
          * ones and sort ascending for the canonical set. */
@@ -663,7 +684,8 @@ int orc_boundary_volumes(int nb, const float* world3, float h, float* psi_out) {
     if (nb == 0) return 0;
     grid_t g;
     if (grid_build(&g, world3, nb, h)) return -1;
-    int* cand = (int*)malloc(sizeof(int) * (size_t)nb);
+    int ccap = nb;
+    int* cand = (int*)malloc(sizeof(int) * (size_t)ccap);
     if (!cand) {
         grid_free(&g);
         return -1;
@@ -671,7 +693,12 @@ int orc_boundary_volumes(int nb, const float* world3, float h, float* psi_out) {
     for (int i = 0; i < nb; ++i) {
         int c[3];
         world_to_cell(world3 + 3 * i, g.inv, c);
-        int m = grid_candidates(&g, c, cand, nb);
+        int m = grid_candidates_buf(&g, c, &cand, &ccap);
+        if (m < 0) {
+            free(cand);
+            grid_free(&g);
+            return -1;
+        }
         float sum_w = 0.0f;
         for (int k = 0; k < m; ++k) {
             int j = cand[k];
@@ -693,7 +720,8 @@ int orc_boundary_density(int n, const float* x3, float* rho, int nb, const float
     if (nb == 0 || n == 0) return 0;
     grid_t g;
     if (grid_build(&g, bpos3, nb, h)) return -1;
-    int* cand = (int*)malloc(sizeof(int) * (size_t)nb);
+    int ccap = nb;
+    int* cand = (int*)malloc(sizeof(int) * (size_t)ccap);
     if (!cand) {
         grid_free(&g);
         return -1;
@@ -701,7 +729,12 @@ int orc_boundary_density(int n, const float* x3, float* rho, int nb, const float
     for (int i = 0; i < n; ++i) {
         int c[3];
         world_to_cell(x3 + 3 * i, g.inv, c);
-        int m = grid_candidates(&g, c, cand, nb);
+        int m = grid_candidates_buf(&g, c, &cand, &ccap);
+        if (m < 0) {
+            free(cand);
+            grid_free(&g);
+            return -1;
+        }
         float bd = 0.0f;
         for (int k = 0; k < m; ++k) {
             int j = cand[k];
@@ -725,7 +758,8 @@ int orc_coupling_forces(int n, const float* x3, const float* rho, float mass, in
     if (nb == 0 || n == 0) return 0;
     grid_t g;
     if (grid_build(&g, x3, n, h)) return -1;
-    int* cand = (int*)malloc(sizeof(int) * (size_t)n);
+    int ccap = n;
+    int* cand = (int*)malloc(sizeof(int) * (size_t)ccap);
     if (!cand) {
         grid_free(&g);
         return -1;
@@ -739,7 +773,12 @@ int orc_coupling_forces(int n, const float* x3, const float* rho, float mass, in
         float psi_b = psi[b];
         int c[3];
         world_to_cell(bpos3 + 3 * b, g.inv, c);
-        int m = grid_candidates(&g, c, cand, n);
+        int m = grid_candidates_buf(&g, c, &cand, &ccap);
+        if (m < 0) {
+            free(cand);
+            grid_free(&g);
+            return -1;
+        }
         for (int k = 0; k < m; ++k) {
             int j = cand[k];
             float rx = bpos3[3 * b] - x3[3 * j];

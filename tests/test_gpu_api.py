@@ -155,7 +155,8 @@ def test_fluid_world_step_matches_oracle(port):
     w.step(dt)
     s = Settings.make(kernel_radius=0.2, solver_iterations=2)
     z = np.zeros(len(x0), np.float32)
-    m = np.float32(1000) * np.float32(0.05) ** 3
+    sp = np.float32(0.05)
+    m = np.float32(np.float32(np.float32(1000) * sp) * sp) * sp  # particle_mass order
     ox, ov, orho, olam = port.steps(s, x0, np.zeros_like(x0), z, z, dt,
                                     np.array([0, -9.81, 0], np.float32), m, 1)
     fs = w.fluid_state

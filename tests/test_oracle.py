@@ -203,3 +203,24 @@ def test_configured_scorr_is_ill_conditioned(port):
             assert dx > 1e-3
         else:
             assert dx < bound
+
+
+def test_candidate_lists_longer_than_the_point_count(port):
+    # Around the origin the reference's XOR hash merges cells, and a merged
+    # bucket visited twice can make a candidate list longer than the number of
+    # points; every oracle routine must size its buffers for that.
+    x = workloads.lattice((3, 3, 3), 0.05, (-0.07, -0.07, -0.07))
+    n = len(x)
+    cand = port.grid_query(x, np.float32(0.1), np.zeros(3, np.float32))
+    assert len(cand) > n
+    rho = np.full(n, 1100.0, np.float32)
+    body = np.zeros(n, np.int32)
+    psi = port.boundary_volumes(x, np.float32(0.1))
+    assert np.isfinite(psi).all()
+    r2 = port.boundary_density(x, rho, x, psi, np.float32(0.1), np.float32(1000.0))
+    assert np.isfinite(r2).all()
+    f, t = port.coupling_forces(x, rho, 0.1, x, body, psi, [1], [[0, 0, 0]], np.float32(0.1),
+                                np.float32(1000.0))
+    assert np.isfinite(f).all() and np.isfinite(t).all()
+    off, idx = port.neighbor_sets(x, np.float32(0.1))
+    assert off[-1] == len(idx) and len(idx) <= n * (n - 1)
