@@ -205,6 +205,86 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def percentile(xs, q):
+    return float(np.percentile(np.asarray(xs, np.float64), q)) if len(xs) else None
+
+
+def run_batched(args, device):
+    """Independent dam-break scenes of uneven size (workloads.batched_scenes:
+    1,024 scenes, 2,000-64,000 particles log-uniform, 2-6 iterations) stepped
+    (a) as one batch per step (pbf_batch_step: one sort and one launch per
+    phase for all scenes) and (b) by the plain drop-in path, one
+    pbf_scene_step per scene on its own stream, all issued before one wait.
+    Both arms run the same consecutive steps from the same seeded states
+    (bit-identical trajectories), timed on the host clock from the first call
+    to the end of the last step; the batch arm also reports the device time
+    of seeded batch steps and per-step latency percentiles."""
+    from novaphy_gb300 import capi
+
+    wl = workloads.batched_scenes(nscenes=args.batched_scenes)
+    total = int(sum(w.n for w in wl))
+    scenes = []
+    for w in wl:
+        sc = capi.Scene(capi.default_settings(**w.settings), w.x, w.v, mass=w.mass, device=device)
+        sc.set_gravity(w.gravity)
+        scenes.append(sc)
+    seeds = [sc.snapshot() for sc in scenes]
+    dts = np.array([w.dt for w in wl], np.float32)
+    k = max(1, args.batched_steps)
+
+    def reseed():
+        for sc, sd in zip(scenes, seeds):
+            sc.restore(sd)
+
+    # Batched arm.
+    b = capi.Batch(device)
+    reseed()
+    b.step(scenes, dts)  # warm-up: scratch, graph
+    reseed()
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(k):
+        lat.append(b.step_timed(scenes, dts))
+    t_batch = time.perf_counter() - t0
+    reseed()
+    dev_ms = b.replay_timed(scenes, seeds, dts, k)
+
+    # Plain per-scene arm.
+    reseed()
+    for sc, dt in zip(scenes, dts):  # warm-up: per-scene scratch and graphs
+        sc.step(float(dt), 1, sync=False)
+    for sc in scenes:
+        sc.sync()
+    reseed()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        for sc, dt in zip(scenes, dts):
+            sc.step(float(dt), 1, sync=False)
+    for sc in scenes:
+        sc.sync()
+    t_plain = time.perf_counter() - t0
+
+    out = {
+        "workload": f"batched_scenes: {len(wl)} dam-break scenes, {total} particles "
+                    f"({min(w.n for w in wl)}-{max(w.n for w in wl)} per scene), r = 0.02, "
+                    f"h = 4r, 2-6 iterations, dt = 1/120",
+        "particles": total, "scenes": len(wl), "steps": k,
+        "value": total * k / t_batch, "unit": UNIT,
+        "plain_value": total * k / t_plain,
+        "speedup_vs_plain": t_plain / t_batch,
+        "step_ms_p50": percentile(lat, 50), "step_ms_p99": percentile(lat, 99),
+        "seeded_device_value": total * k / (dev_ms / 1e3),
+        "batch_scratch_bytes": b.device_bytes(),
+        "timing": "host clock over k consecutive steps from the seeded states, both arms",
+    }
+    b.close()
+    for sd in seeds:
+        sd.close()
+    for sc in scenes:
+        sc.close()
+    return out
+
+
 def run_ours(args, ws, rank, local):
     from novaphy_gb300 import capi
 
@@ -338,6 +418,10 @@ def run_ours(args, ws, rank, local):
                "call": "pbf_solver_step_host: pinned host x, v, densities, lambdas in and out"}
         drop.close()
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, device)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         counts = (50, 50, 50)
@@ -368,6 +452,7 @@ def run_ours(args, ws, rank, local):
             "clocks": clocks,
             "fast": fast,
             "consecutive": consecutive,
+            "batched": batched,
             "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         }
         print(json.dumps(line), flush=True)
@@ -389,6 +474,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fast", action="store_true")
     ap.add_argument("--no-consecutive", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-scenes", type=int, default=1024)
+    ap.add_argument("--batched-steps", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

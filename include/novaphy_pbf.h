@@ -232,6 +232,54 @@ int pbf_sort_pairs_host(int device, int n, const unsigned* keys, int key_bits,
 int pbf_sort_pairs_noalloc(int device, int n, const unsigned* d_keys, int key_bits,
                            unsigned* d_out_keys, unsigned* d_out_vals, void* stream);
 
+
+/* ---- Batches of scenes --------------------------------------------------
+ * No counterpart in the reference, which steps one FluidWorld at a time
+ * (src/fluid/fluid_world.cpp:49-97, PBFSolver::step at
+ * src/fluid/pbf_solver.cpp:18-127).  A batch steps many independent scenes
+ * together: one cell-key sort, one reference-key sort and one kernel launch
+ * per phase for all of them, with each scene's own settings, gravity, mass,
+ * time step and iteration count read from a per-scene table on the device.
+ * The scenes keep their state in place; a scene stepped in a batch ends
+ * bit for bit where pbf_scene_step would have left it. */
+typedef struct pbf_batch pbf_batch;
+
+/* A batch context on `device`; its scratch grows to the largest batch. */
+int pbf_batch_create(int device, pbf_batch** out);
+int pbf_batch_destroy(pbf_batch* batch);
+
+/* Steps scenes[k] (distinct, on the batch's device) nsteps[k] times with
+ * time step dt[k]; nsteps may be NULL for one step each.  Scenes with no
+ * particles or no steps are skipped.  Asynchronous: the batch's stream first
+ * waits for the scenes' pending work, and later calls on the scenes are
+ * ordered after the batch.  Scenes with exact_arithmetic 1 and 0 are stepped
+ * as two launches sequences. */
+int pbf_batch_step(pbf_batch* batch, int nscenes, pbf_scene* const* scenes, const float* dt,
+                   const int* nsteps);
+
+/* pbf_batch_step bracketed by CUDA events on the batch's stream; waits for
+ * the end and returns the device time (ms) in *ms_out. */
+int pbf_batch_step_timed(pbf_batch* batch, int nscenes, pbf_scene* const* scenes,
+                         const float* dt, const int* nsteps, float* ms_out);
+
+/* Restores every scene from seeds[k] and runs one batch step, nsteps times,
+ * timed as one region (the seeded step of a benchmark). */
+int pbf_batch_replay_timed(pbf_batch* batch, int nscenes, pbf_scene* const* scenes,
+                           const pbf_snapshot* const* seeds, const float* dt, int nsteps,
+                           float* ms_out);
+
+/* Waits for the batch's stream and checks its device status word. */
+int pbf_batch_sync(pbf_batch* batch);
+
+/* Device bytes held: by a batch's scratch, and by a scene's resident state
+ * plus whatever scratch its own steps have allocated. */
+int pbf_batch_device_bytes(const pbf_batch* batch, size_t* out);
+int pbf_scene_device_bytes(const pbf_scene* scene, size_t* out);
+
+/* Device bytes per particle of a scene's resident state (x, v, rho, lambda
+ * and a staging buffer), the figure an admission budget counts. */
+size_t pbf_state_bytes_per_particle(void);
+
 #ifdef __cplusplus
 }
 #endif

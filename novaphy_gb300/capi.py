@@ -119,6 +119,15 @@ def load() -> C.CDLL:
         "pbf_scene_read_boundary": ([vp, vp], C.c_int),
         "pbf_boundary_volumes": ([C.c_int, C.c_int, vp, C.c_float, vp], C.c_int),
         "pbf_scene_step_profiled": ([vp, C.c_float, vp, vp], C.c_int),
+        "pbf_batch_create": ([C.c_int, vp], C.c_int),
+        "pbf_batch_destroy": ([vp], C.c_int),
+        "pbf_batch_step": ([vp, C.c_int, vp, vp, vp], C.c_int),
+        "pbf_batch_step_timed": ([vp, C.c_int, vp, vp, vp, f32p], C.c_int),
+        "pbf_batch_replay_timed": ([vp, C.c_int, vp, vp, vp, C.c_int, f32p], C.c_int),
+        "pbf_batch_sync": ([vp], C.c_int),
+        "pbf_batch_device_bytes": ([vp, C.POINTER(C.c_size_t)], C.c_int),
+        "pbf_scene_device_bytes": ([vp, C.POINTER(C.c_size_t)], C.c_int),
+        "pbf_state_bytes_per_particle": ([], C.c_size_t),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -338,6 +347,89 @@ class Scene:
                                            _ptr(lam), dt,
                                            g.ctypes.data_as(C.POINTER(C.c_float)), mass))
         return x, v, rho, lam
+
+
+def _handles(objs):
+    arr = (C.c_void_p * max(len(objs), 1))()
+    for k, o in enumerate(objs):
+        arr[k] = o.handle
+    return arr
+
+
+def state_bytes_per_particle() -> int:
+    return int(load().pbf_state_bytes_per_particle())
+
+
+def scene_device_bytes(scene: "Scene") -> int:
+    out = C.c_size_t(0)
+    check(load().pbf_scene_device_bytes(scene.handle, C.byref(out)))
+    return int(out.value)
+
+
+class Batch:
+    """A batch context (pbf_batch*): steps many scenes with one launch per phase."""
+
+    def __init__(self, device: int = 0):
+        self._L = load()
+        h = C.c_void_p()
+        check(self._L.pbf_batch_create(device, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            self._L.pbf_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _args(scenes, dt, nsteps):
+        ns = len(scenes)
+        dts = np.ascontiguousarray(np.broadcast_to(np.float32(dt) if np.isscalar(dt) else
+                                                   np.asarray(dt, np.float32), (ns,)), np.float32)
+        steps = None
+        if nsteps is not None:
+            steps = np.ascontiguousarray(np.broadcast_to(np.asarray(nsteps, np.int32), (ns,)),
+                                         np.int32)
+        return ns, _handles(scenes), dts, steps
+
+    def step(self, scenes, dt, nsteps=None, sync: bool = True):
+        ns, hs, dts, steps = self._args(scenes, dt, nsteps)
+        check(self._L.pbf_batch_step(self._h, ns, hs, _ptr(dts),
+                                     _ptr(steps) if steps is not None else None))
+        if sync:
+            self.sync()
+
+    def step_timed(self, scenes, dt, nsteps=None) -> float:
+        ns, hs, dts, steps = self._args(scenes, dt, nsteps)
+        ms = C.c_float(0.0)
+        check(self._L.pbf_batch_step_timed(self._h, ns, hs, _ptr(dts),
+                                           _ptr(steps) if steps is not None else None,
+                                           C.byref(ms)))
+        return ms.value
+
+    def replay_timed(self, scenes, seeds, dt, nsteps: int) -> float:
+        ns, hs, dts, _ = self._args(scenes, dt, None)
+        ms = C.c_float(0.0)
+        check(self._L.pbf_batch_replay_timed(self._h, ns, hs, _handles(seeds), _ptr(dts),
+                                             nsteps, C.byref(ms)))
+        return ms.value
+
+    def sync(self):
+        check(self._L.pbf_batch_sync(self._h))
+
+    def device_bytes(self) -> int:
+        out = C.c_size_t(0)
+        check(self._L.pbf_batch_device_bytes(self._h, C.byref(out)))
+        return int(out.value)
 
 
 class Snapshot:

@@ -1,0 +1,531 @@
+// C ABI of batched stepping (include/novaphy_pbf.h, "Batches of scenes"):
+// many independent scenes share one cell-key sort, one reference-key sort and
+// one kernel launch per phase.  Each scene keeps its state in place; the
+// kernels reach it through a per-scene table (state pointers, particle range,
+// step constants, slot range) uploaded before every step.
+//
+// The batch's particle order is the concatenation of the scenes' particle
+// orders and its cell-slot space the concatenation of their grids, so within
+// a scene every sort is stable in the scene's own particle order and every
+// neighbour walk visits the same candidates in the same order as a step of
+// the scene alone: results do not depend on what else is in the batch.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "pbf_internal.cuh"
+#include "pbf_launch.cuh"
+
+using namespace pbf;
+using namespace pbf::capi;
+
+namespace {
+
+// The launch sequence of a batch step depends on these; a cached graph is
+// reused (with updated kernel parameters) while they stay the same.
+struct GraphKey {
+    int exact = -1, n = 0, nscenes = 0, key_bits = 0, scene_bits = 0, max_iters = 0;
+    uint32_t nslots = 0;
+    bool any_zero = false, any_vort = false, any_plain = false, xsph_on = false;
+    bool operator==(const GraphKey& o) const {
+        return exact == o.exact && n == o.n && nscenes == o.nscenes && key_bits == o.key_bits &&
+               scene_bits == o.scene_bits && max_iters == o.max_iters && nslots == o.nslots &&
+               any_zero == o.any_zero && any_vort == o.any_vort && any_plain == o.any_plain &&
+               xsph_on == o.xsph_on;
+    }
+};
+
+int bits_for(unsigned long long v) {
+    int b = 1;
+    while ((1ull << b) < v) ++b;
+    return b;
+}
+
+}  // namespace
+
+struct pbf_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    std::mutex mu;
+
+    int cap = 0;  // particles
+    void* wmem = nullptr;  // step scratch (bind_work)
+    void* smem = nullptr;  // sort scratch
+    void* xmem = nullptr;  // scene ids, scene-pass temporaries
+    StepBuffers B{};
+    SortScratch sort{};
+    uint32_t *pid = nullptr, *spid = nullptr, *kpid = nullptr, *itmp = nullptr, *perm = nullptr,
+             *stmp = nullptr;
+    unsigned long long* rtmp = nullptr;
+
+    uint32_t* off = nullptr;  // nslots + 1 offsets, then one alias byte per slot
+    uint32_t off_cap = 0;     // entries
+
+    int tab_cap = 0;  // scenes
+    void* tmem = nullptr;  // per-scene tables: StepConsts | StateRef | firsts
+    size_t tab_refs_at = 0, tab_firsts_at = 0, tab_bytes = 0;
+    std::vector<char> h_tab;
+
+    cudaGraphExec_t graph = nullptr;
+    GraphKey key{};
+};
+
+namespace {
+
+void drop_graph(pbf_batch* b) {
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->key = GraphKey{};
+}
+
+size_t extra_bytes(int c) {
+    return 6 * align_up((size_t)c * 4, 256) + align_up((size_t)c * 8, 256);
+}
+
+int ensure_particles(pbf_batch* b, int n) {
+    if (b->wmem && b->cap >= n) return PBF_OK;
+    drop_graph(b);
+    for (void* m : {b->wmem, b->smem, b->xmem})
+        if (m) cudaFree(m);
+    b->wmem = b->smem = b->xmem = nullptr;
+    b->cap = 0;
+    // Grow by a quarter so that a slowly growing batch does not reallocate
+    // on every step.
+    const int c = std::max(n + n / 4, 1024);
+    const size_t wb = work_bytes(c);
+    PBF_CUDA(cudaMalloc(&b->wmem, wb));
+    PBF_CUDA(cudaMemsetAsync(b->wmem, 0, wb, b->stream));
+    bind_work(b->B, b->wmem, c);
+    const size_t sb = sort_scratch_bytes(c);
+    PBF_CUDA(cudaMalloc(&b->smem, sb));
+    PBF_CUDA(cudaMemsetAsync(b->smem, 0, sb, b->stream));
+    sort_scratch_bind(b->sort, b->smem, c);
+    b->B.err = b->sort.err;
+    const size_t xb = extra_bytes(c);
+    PBF_CUDA(cudaMalloc(&b->xmem, xb));
+    char* p = reinterpret_cast<char*>(b->xmem);
+    const size_t f1 = align_up((size_t)c * 4, 256);
+    uint32_t** arr[6] = {&b->pid, &b->spid, &b->kpid, &b->itmp, &b->perm, &b->stmp};
+    for (int k = 0; k < 6; ++k) *arr[k] = reinterpret_cast<uint32_t*>(p + k * f1);
+    b->rtmp = reinterpret_cast<unsigned long long*>(p + 6 * f1);
+    b->cap = c;
+    return PBF_OK;
+}
+
+int ensure_slots(pbf_batch* b, uint32_t nslots) {
+    if (b->off && b->off_cap >= nslots + 1) return PBF_OK;
+    drop_graph(b);
+    if (b->off) cudaFree(b->off);
+    b->off = nullptr;
+    b->off_cap = 0;
+    const uint32_t c = nslots + nslots / 4 + 1;
+    const size_t ob = align_up((size_t)(c + 1) * 4, 256);
+    PBF_CUDA(cudaMalloc(&b->off, ob + align_up(c, 256)));
+    b->off_cap = c + 1;
+    b->B.off = b->off;
+    b->B.slot_alias = reinterpret_cast<unsigned char*>(b->off) + ob;
+    return PBF_OK;
+}
+
+int ensure_tables(pbf_batch* b, int nscenes) {
+    if (b->tmem && b->tab_cap >= nscenes) return PBF_OK;
+    drop_graph(b);
+    if (b->tmem) cudaFree(b->tmem);
+    b->tmem = nullptr;
+    b->tab_cap = 0;
+    const int c = std::max(nscenes + nscenes / 4, 64);
+    b->tab_refs_at = align_up((size_t)c * sizeof(StepConsts), 256);
+    b->tab_firsts_at = b->tab_refs_at + align_up((size_t)c * sizeof(StateRef), 256);
+    b->tab_bytes = b->tab_firsts_at + align_up((size_t)(c + 1) * 4, 256);
+    PBF_CUDA(cudaMalloc(&b->tmem, b->tab_bytes));
+    b->h_tab.assign(b->tab_bytes, 0);
+    b->tab_cap = c;
+    return PBF_OK;
+}
+
+bool graphs_enabled() {
+    const char* v = std::getenv("PBF_NO_GRAPH");
+    return !(v && v[0] == '1');
+}
+
+// One step of `list` (scenes with particles, all of one arithmetic build):
+// per-scene tables uploaded, then the batch's launch sequence (from a graph).
+int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vector<float>& dts,
+               int exact, PhaseMarks* pm) {
+    const int ns = (int)list.size();
+    if (ns == 0) return PBF_OK;
+    unsigned long long n_total = 0, slots_total = 0;
+    int max_iters = 0;
+    bool any_zero = false, any_vort = false, any_plain = false, xsph_on = false;
+    std::vector<StepConsts> consts((size_t)ns);
+    for (int k = 0; k < ns; ++k) {
+        pbf_scene* s = list[k];
+        StepConsts& C = consts[k];
+        int rc = scene_consts(s, dts[k], C);
+        if (rc) return rc;
+        C.seg_begin = (uint32_t)n_total;
+        C.seg_end = (uint32_t)(n_total + (unsigned long long)s->n);
+        C.grid.base = (uint32_t)slots_total;
+        n_total += (unsigned long long)s->n;
+        slots_total += C.grid.nslots;
+        if (n_total > (1ull << 30)) return fail(PBF_ERR_CAPACITY, "at most 2^30 particles per batch");
+        if (slots_total > (1ull << 30))
+            return fail(PBF_ERR_CAPACITY, "the scenes' grids exceed 2^30 cell slots in total");
+        max_iters = std::max(max_iters, C.iters);
+        any_zero |= C.iters <= 0;
+        any_vort |= C.vort_on != 0;
+        any_plain |= C.vort_on == 0;
+        xsph_on |= C.xsph_on != 0;
+    }
+    const int n = (int)n_total;
+    int rc = ensure_particles(b, n);
+    if (!rc) rc = ensure_slots(b, (uint32_t)slots_total);
+    if (!rc) rc = ensure_tables(b, ns);
+    if (rc) return rc;
+
+    char* h = b->h_tab.data();
+    auto* htab = reinterpret_cast<StepConsts*>(h);
+    auto* hrefs = reinterpret_cast<StateRef*>(h + b->tab_refs_at);
+    auto* hfirst = reinterpret_cast<uint32_t*>(h + b->tab_firsts_at);
+    for (int k = 0; k < ns; ++k) {
+        pbf_scene* s = list[k];
+        htab[k] = consts[k];
+        hrefs[k] = StateRef{s->B.x, s->B.v, s->B.rho, s->B.lam, consts[k].seg_begin};
+        hfirst[k] = consts[k].seg_begin;
+    }
+    hfirst[ns] = (uint32_t)n;
+    // Pageable source: the copy is staged before cudaMemcpyAsync returns, so
+    // the host table may be rewritten for the next step right away.
+    PBF_CUDA(cudaMemcpyAsync(b->tmem, h, b->tab_firsts_at + (size_t)(ns + 1) * 4,
+                             cudaMemcpyHostToDevice, b->stream));
+
+    BatchDesc D{};
+    D.n = n;
+    D.nscenes = ns;
+    D.nslots = (uint32_t)slots_total;
+    D.key_bits = bits_for(slots_total);
+    D.scene_bits = bits_for((unsigned long long)ns);
+    D.max_iters = max_iters;
+    D.any_zero_iters = any_zero;
+    D.any_vort = any_vort;
+    D.any_plain = any_plain;
+    D.xsph_on = xsph_on;
+    char* t = reinterpret_cast<char*>(b->tmem);
+    D.tab = reinterpret_cast<const StepConsts*>(t);
+    D.refs = reinterpret_cast<const StateRef*>(t + b->tab_refs_at);
+    D.firsts = reinterpret_cast<const uint32_t*>(t + b->tab_firsts_at);
+    D.pid = b->pid;
+    D.spid = b->spid;
+    D.kpid = b->kpid;
+    D.rtmp = b->rtmp;
+    D.itmp = b->itmp;
+    D.perm = b->perm;
+    D.stmp = b->stmp;
+
+    auto enqueue = [&](cudaStream_t st, PhaseMarks* marks) {
+        return exact ? exact_enqueue_batch(b->B, D, b->sort, st, marks)
+                     : fast_enqueue_batch(b->B, D, b->sort, st, marks);
+    };
+    if (pm || !graphs_enabled()) {
+        cudaError_t e = enqueue(b->stream, pm);
+        if (e != cudaSuccess) return cuda_fail(e, "batch step");
+        return PBF_OK;
+    }
+    GraphKey key;
+    key.exact = exact;
+    key.n = n;
+    key.nscenes = ns;
+    key.key_bits = D.key_bits;
+    key.scene_bits = D.scene_bits;
+    key.max_iters = max_iters;
+    key.nslots = D.nslots;
+    key.any_zero = any_zero;
+    key.any_vort = any_vort;
+    key.any_plain = any_plain;
+    key.xsph_on = xsph_on;
+    if (!b->graph || !(key == b->key)) {
+        cudaGraph_t g = nullptr;
+        PBF_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t ee = enqueue(b->stream, nullptr);
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        if (ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(ee, "batch step (capture)");
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+        bool updated = false;
+        if (b->graph) {
+            // Same launch topology with new sizes: update the parameters in place.
+            cudaGraphExecUpdateResultInfo info{};
+            updated = cudaGraphExecUpdate(b->graph, g, &info) == cudaSuccess;
+            if (!updated) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(b->graph);
+                b->graph = nullptr;
+            }
+        }
+        if (!updated) {
+            ce = cudaGraphInstantiate(&b->graph, g, 0);
+            if (ce != cudaSuccess) {
+                cudaGraphDestroy(g);
+                b->graph = nullptr;
+                return cuda_fail(ce, "cudaGraphInstantiate");
+            }
+        }
+        cudaGraphDestroy(g);
+        b->key = key;
+    }
+    PBF_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    return PBF_OK;
+}
+
+// Locks the scenes (in address order, so that concurrent batches over
+// overlapping sets cannot deadlock) and checks them.
+struct SceneLocks {
+    std::vector<std::unique_lock<std::mutex>> locks;
+};
+
+int lock_scenes(const pbf_batch* b, int nscenes, pbf_scene* const* scenes, SceneLocks& L) {
+    std::vector<pbf_scene*> sorted(scenes, scenes + nscenes);
+    for (pbf_scene* s : sorted)
+        if (!s) return fail(PBF_ERR_INVALID_ARG, "a scene is NULL");
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+        return fail(PBF_ERR_INVALID_ARG, "a scene appears twice in the batch");
+    for (pbf_scene* s : sorted)
+        if (s->device != b->device) return fail(PBF_ERR_INVALID_ARG, "a scene is on another device");
+    L.locks.reserve(sorted.size());
+    for (pbf_scene* s : sorted) L.locks.emplace_back(s->mu);
+    return PBF_OK;
+}
+
+// Orders the batch stream after each scene's stream.
+int wait_for_scenes(pbf_batch* b, int nscenes, pbf_scene* const* scenes) {
+    for (int k = 0; k < nscenes; ++k) {
+        pbf_scene* s = scenes[k];
+        if (!s->ev) PBF_CUDA(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
+        PBF_CUDA(cudaEventRecord(s->ev, s->stream));
+        PBF_CUDA(cudaStreamWaitEvent(b->stream, s->ev, 0));
+    }
+    return PBF_OK;
+}
+
+// Orders each scene's later work after the batch.
+int release_scenes(pbf_batch* b, int nscenes, pbf_scene* const* scenes) {
+    PBF_CUDA(cudaEventRecord(b->done, b->stream));
+    for (int k = 0; k < nscenes; ++k) PBF_CUDA(cudaStreamWaitEvent(scenes[k]->stream, b->done, 0));
+    return PBF_OK;
+}
+
+int run_batch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
+              const int* nsteps) {
+    int max_steps = 0;
+    for (int k = 0; k < nscenes; ++k) {
+        const int m = nsteps ? nsteps[k] : 1;
+        if (m < 0) return fail(PBF_ERR_INVALID_ARG, "nsteps must be >= 0");
+        if (!(dt[k] > 0.0f) || !std::isfinite(dt[k]))
+            return fail(PBF_ERR_INVALID_ARG, "dt must be > 0");
+        max_steps = std::max(max_steps, m);
+    }
+    std::vector<pbf_scene*> list;
+    std::vector<float> dts;
+    list.reserve((size_t)nscenes);
+    dts.reserve((size_t)nscenes);
+    for (int step = 0; step < max_steps; ++step) {
+        for (int exact = 1; exact >= 0; --exact) {
+            list.clear();
+            dts.clear();
+            for (int k = 0; k < nscenes; ++k) {
+                pbf_scene* s = scenes[k];
+                const int m = nsteps ? nsteps[k] : 1;
+                if (step >= m || s->n <= 0) continue;  // pbf_solver.cpp:21
+                if ((s->settings.exact_arithmetic ? 1 : 0) != exact) continue;
+                list.push_back(s);
+                dts.push_back(dt[k]);
+            }
+            int rc = step_group(b, list, dts, exact, nullptr);
+            if (rc) return rc;
+        }
+    }
+    return PBF_OK;
+}
+
+int batch_sync(pbf_batch* b) {
+    PBF_CUDA(cudaStreamSynchronize(b->stream));
+    if (!b->sort.err) return PBF_OK;
+    uint32_t err = 0;
+    PBF_CUDA(cudaMemcpy(&err, b->sort.err, 4, cudaMemcpyDeviceToHost));
+    if (err) {
+        PBF_CUDA(cudaMemset(b->sort.err, 0, 4));
+        return fail(PBF_ERR_TIMEOUT, "device-side wait in a batch sort gave up (error word " +
+                                         std::to_string(err) + ")");
+    }
+    return PBF_OK;
+}
+
+int check_args(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt) {
+    if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+    if (nscenes < 0) return fail(PBF_ERR_INVALID_ARG, "nscenes must be >= 0");
+    if (nscenes > 0 && (!scenes || !dt)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbf_batch_create(int device, pbf_batch** out) {
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t ce = cudaGetDeviceCount(&count);
+    if (ce != cudaSuccess || count == 0)
+        return fail(PBF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(ce));
+    if (device < 0 || device >= count) return fail(PBF_ERR_INVALID_ARG, "device out of range");
+    DeviceGuard dg(device);
+    if (!dg.ok) return fail(PBF_ERR_NO_DEVICE, "cudaSetDevice failed");
+    std::unique_ptr<pbf_batch> b(new pbf_batch());
+    b->device = device;
+    PBF_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    ce = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (ce != cudaSuccess) {
+        cudaStreamDestroy(b->stream);
+        return cuda_fail(ce, "cudaEventCreate");
+    }
+    *out = b.release();
+    return PBF_OK;
+}
+
+int pbf_batch_destroy(pbf_batch* b) {
+    if (!b) return PBF_OK;
+    {
+        DeviceGuard dg(b->device);
+        if (b->stream) cudaStreamSynchronize(b->stream);
+        drop_graph(b);
+        for (void* m : {b->wmem, b->smem, b->xmem, b->tmem, static_cast<void*>(b->off)})
+            if (m) cudaFree(m);
+        if (b->done) cudaEventDestroy(b->done);
+        if (b->stream) cudaStreamDestroy(b->stream);
+    }
+    delete b;
+    return PBF_OK;
+}
+
+int pbf_batch_step(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
+                   const int* nsteps) {
+    int rc = check_args(b, nscenes, scenes, dt);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    SceneLocks L;
+    rc = lock_scenes(b, nscenes, scenes, L);
+    if (rc) return rc;
+    rc = wait_for_scenes(b, nscenes, scenes);
+    if (!rc) rc = run_batch(b, nscenes, scenes, dt, nsteps);
+    const int rc2 = release_scenes(b, nscenes, scenes);
+    return rc ? rc : rc2;
+}
+
+int pbf_batch_step_timed(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
+                         const int* nsteps, float* ms_out) {
+    int rc = check_args(b, nscenes, scenes, dt);
+    if (rc) return rc;
+    if (!ms_out) return fail(PBF_ERR_INVALID_ARG, "ms_out is NULL");
+    *ms_out = 0.0f;
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    SceneLocks L;
+    rc = lock_scenes(b, nscenes, scenes, L);
+    if (rc) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    PBF_CUDA(cudaEventCreate(&e0));
+    cudaError_t e = cudaEventCreate(&e1);
+    rc = wait_for_scenes(b, nscenes, scenes);
+    if (!rc && e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+    if (!rc && e == cudaSuccess) rc = run_batch(b, nscenes, scenes, dt, nsteps);
+    if (!rc && e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+    const int rc2 = release_scenes(b, nscenes, scenes);
+    if (!rc && e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(ms_out, e0, e1);
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (e != cudaSuccess) return cuda_fail(e, "pbf_batch_step_timed");
+    return batch_sync(b);
+}
+
+int pbf_batch_replay_timed(pbf_batch* b, int nscenes, pbf_scene* const* scenes,
+                           const pbf_snapshot* const* seeds, const float* dt, int nsteps,
+                           float* ms_out) {
+    int rc = check_args(b, nscenes, scenes, dt);
+    if (rc) return rc;
+    if (!ms_out || (nscenes > 0 && !seeds)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    if (nsteps < 0) return fail(PBF_ERR_INVALID_ARG, "nsteps must be >= 0");
+    for (int k = 0; k < nscenes; ++k)
+        if (!seeds[k]) return fail(PBF_ERR_INVALID_ARG, "a seed is NULL");
+    *ms_out = 0.0f;
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    SceneLocks L;
+    rc = lock_scenes(b, nscenes, scenes, L);
+    if (rc) return rc;
+    rc = wait_for_scenes(b, nscenes, scenes);
+    auto seeded_step = [&]() {
+        for (int k = 0; k < nscenes; ++k) {
+            const int r = restore_on(scenes[k], seeds[k], b->stream);
+            if (r) return r;
+        }
+        return run_batch(b, nscenes, scenes, dt, nullptr);
+    };
+    if (!rc) rc = seeded_step();  // builds the graph outside the timed region
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (!rc && e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+    for (int k = 0; k < nsteps && !rc && e == cudaSuccess; ++k) rc = seeded_step();
+    if (!rc && e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+    const int rc2 = release_scenes(b, nscenes, scenes);
+    if (!rc && e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(ms_out, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (e != cudaSuccess) return cuda_fail(e, "pbf_batch_replay_timed");
+    return batch_sync(b);
+}
+
+int pbf_batch_sync(pbf_batch* b) {
+    if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    return batch_sync(b);
+}
+
+int pbf_batch_device_bytes(const pbf_batch* b, size_t* out) {
+    if (!b || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    size_t t = 0;
+    if (b->wmem) t += work_bytes(b->cap) + sort_scratch_bytes(b->cap) + extra_bytes(b->cap);
+    if (b->off) t += align_up((size_t)b->off_cap * 4, 256) + align_up(b->off_cap, 256);
+    t += b->tab_bytes;
+    *out = t;
+    return PBF_OK;
+}
+
+int pbf_scene_device_bytes(const pbf_scene* s, size_t* out) {
+    if (!s || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *out = scene_device_bytes(s);
+    return PBF_OK;
+}
+
+size_t pbf_state_bytes_per_particle(void) { return kStateBytesPerParticle; }
+
+}  // extern "C"

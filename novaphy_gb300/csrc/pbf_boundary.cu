@@ -201,7 +201,8 @@ cudaError_t index_build(PointIndex& I, const float4* pos, const float* attr, int
     k_offsets<<<grid_of((int)C.grid.nslots + 1, 256), 256, 0, st>>>(I.skeys, n, I.off, C.grid.nslots);
     k_ix_gather<<<nb, kBlock, 0, st>>>(I.sidx, pos, attr, n, I.spos, I.scell, I.pos_of,
                                        I.slot_alias, C);
-    k_buckets<<<grid_of(n, 256), 256, 0, st>>>(I.rsorted, I.ridx, I.pos_of, I.scell, I.kpos, I.bend, n);
+    k_buckets<<<grid_of(n, 256), 256, 0, st>>>(I.rsorted, I.ridx, I.pos_of, I.scell, nullptr, I.kpos,
+                                               I.bend, n);
     return cudaGetLastError();
 }
 
@@ -214,8 +215,13 @@ cudaError_t index_classify(const QuerySet& Q, const float4* qpos, int nq, const 
         // Nothing to find: every neighbour bucket is empty.
         return cudaMemsetAsync(Q.qown, 0, (size_t)nq * sizeof(int), st);
     }
-    k_classify<<<grid_of(nq, kBlock), kBlock, 0, st>>>(Q.qcell, nq, I.scell, I.n, I.rsorted, I.kpos,
-                                                        I.bend, I.slot_alias, Q.btab, Q.qown, C);
+    StepConsts Cs = C;
+    Cs.seg_begin = 0;
+    Cs.seg_end = (uint32_t)I.n;
+    Cs.hash_compat = 1;  // the coupling queries always follow the reference buckets
+    k_classify<<<grid_of(nq, kBlock), kBlock, 0, st>>>(Q.qcell, nq, I.scell, I.rsorted, I.kpos,
+                                                        I.bend, I.slot_alias, Q.btab, Q.qown,
+                                                        nullptr, OneScene{Cs, StateRef{}});
     return cudaGetLastError();
 }
 

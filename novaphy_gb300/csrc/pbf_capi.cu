@@ -12,6 +12,7 @@
 
 #include "novaphy_pbf.h"
 #include "pbf_boundary.cuh"
+#include "pbf_internal.cuh"
 #include "pbf_launch.cuh"
 #include "pbf_types.cuh"
 #include "radix_sort.cuh"
@@ -21,6 +22,13 @@ using namespace pbf;
 namespace {
 
 thread_local std::string g_last_error;
+
+constexpr float kPi = 3.14159265358979323846f;  // math_utils.h:53
+
+}  // namespace
+
+namespace pbf {
+namespace capi {
 
 int fail(int code, const std::string& msg) {
     g_last_error = msg;
@@ -35,26 +43,12 @@ int cuda_fail(cudaError_t e, const char* where) {
     return fail(code, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
-#define PBF_CUDA(expr)                                  \
-    do {                                                \
-        cudaError_t e_ = (expr);                        \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #expr); \
-    } while (0)
+}  // namespace capi
+}  // namespace pbf
 
-constexpr float kPi = 3.14159265358979323846f;  // math_utils.h:53
+using namespace pbf::capi;
 
-// Sets the device for the lifetime of the guard, restoring the previous one.
-struct DeviceGuard {
-    int prev = -1;
-    bool ok = false;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        ok = cudaSetDevice(dev) == cudaSuccess;
-    }
-    ~DeviceGuard() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
+namespace {
 
 __global__ void k_expand3(const float* __restrict__ a3, float4* __restrict__ out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -82,8 +76,6 @@ __global__ void k_finite(const float4* __restrict__ x, const float4* __restrict_
     }
 }
 
-size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
-
 }  // namespace
 
 namespace pbf {
@@ -92,61 +84,6 @@ namespace pbf {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace pbf
 
-struct pbf_scene {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::mutex mu;
-    pbf_settings settings{};
-    float gravity[3] = {0.0f, -9.81f, 0.0f};  // World default (include/novaphy/sim/world.h:157)
-    float mass = 0.0f;
-    int n = 0;
-    int cap = 0;
-    // Region the grid is fitted to when the domain clamp is off.
-    bool have_bbox = false;
-    float bbox_lo[3] = {0, 0, 0}, bbox_hi[3] = {0, 0, 0};
-
-    void* pmem = nullptr;  // per-particle arrays
-    void* smem = nullptr;  // sort scratch
-    uint32_t* off = nullptr;
-    uint32_t off_cap = 0;  // entries
-    float* staging = nullptr;  // float[3 cap]
-    uint32_t* d_flag = nullptr;
-    SortScratch sort{};
-    StepBuffers B{};
-
-    // Graph of one step, re-captured when the constants change.
-    cudaGraphExec_t graph = nullptr;
-    StepConsts graph_consts{};
-    int graph_iters = -1;
-    int graph_exact = -1;
-
-    // Akinci boundary (FluidWorld coupling).
-    struct Boundary {
-        int nb = 0, nbodies = 0, needed_bodies = 0;
-        void* mem = nullptr;       // per-boundary-particle arrays
-        void* body_mem = nullptr;  // per-body arrays
-        void* sort_mem = nullptr;
-        void* fq_mem = nullptr;    // fluid-query cells (per fluid particle)
-        int fq_cap = 0;
-        float4* local = nullptr;   // w = psi
-        int* body = nullptr;
-        float4* world = nullptr;   // w = psi
-        float4* Fb = nullptr;
-        PointIndex idx;            // reference buckets over the boundary
-        QuerySet bq;               // boundary queries against the fluid index
-        int4* fq_cell = nullptr;
-        float4* body_pos = nullptr;
-        float4* body_quat = nullptr;
-        int* body_dyn = nullptr;
-        int* list_off = nullptr;
-        int* list = nullptr;
-        float* force3 = nullptr;
-        float* torque3 = nullptr;
-        SortScratch sort{};
-        uint32_t idx_slots = 0;
-    } bnd;
-};
-
 namespace {
 
 void free_particles(pbf_scene* s) {
@@ -154,67 +91,67 @@ void free_particles(pbf_scene* s) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
     }
-    if (s->pmem) cudaFree(s->pmem);
-    if (s->smem) cudaFree(s->smem);
-    s->pmem = s->smem = nullptr;
-    s->cap = 0;
+    for (void* m : {s->pmem, s->wmem, s->smem})
+        if (m) cudaFree(m);
+    s->pmem = s->wmem = s->smem = nullptr;
+    s->cap = s->work_cap = 0;
+    s->sort = SortScratch{};
     s->B = StepBuffers{};
+    s->B.off = s->off;
+    if (s->off) s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) +
+                                  align_up((size_t)s->off_cap * 4, 256);
 }
 
-// (Re)allocates the per-particle arrays for `cap` particles.
+// (Re)allocates the resident state for `cap` particles; the step scratch
+// follows on the next step (ensure_work).
 int alloc_particles(pbf_scene* s, int cap) {
     free_particles(s);
     const int c = cap > 0 ? cap : 1;
     const size_t f4 = align_up((size_t)c * 16, 256);
     const size_t f1 = align_up((size_t)c * 4, 256);
-    const size_t f2 = align_up((size_t)c * 8, 256);
     const size_t f3 = align_up((size_t)c * 12, 256);
-    const size_t f27 = align_up((size_t)c * 27 * 4, 256);
-    const size_t total = 8 * f4 + 3 * f1 + 3 * f1 + f4 + f3 + 2 * f2 + 5 * f1 + f27;
+    const size_t total = 2 * f4 + 2 * f1 + f3;
     PBF_CUDA(cudaMalloc(&s->pmem, total));
     char* p = reinterpret_cast<char*>(s->pmem);
-    auto take = [&](size_t b) {
-        char* r = p;
-        p += b;
-        return r;
-    };
-    StepBuffers& B = s->B;
-    B.x = reinterpret_cast<float4*>(take(f4));
-    B.v = reinterpret_cast<float4*>(take(f4));
-    B.sx = reinterpret_cast<float4*>(take(f4));
-    B.xa = reinterpret_cast<float4*>(take(f4));
-    B.xb = reinterpret_cast<float4*>(take(f4));
-    B.sv = reinterpret_cast<float4*>(take(f4));
-    B.sv2 = reinterpret_cast<float4*>(take(f4));
-    B.som = reinterpret_cast<float4*>(take(f4));
-    B.rho = reinterpret_cast<float*>(take(f1));
-    B.lam = reinterpret_cast<float*>(take(f1));
-    B.srho = reinterpret_cast<float*>(take(f1));
-    B.keys = reinterpret_cast<uint32_t*>(take(f1));
-    B.skeys = reinterpret_cast<uint32_t*>(take(f1));
-    B.sidx = reinterpret_cast<uint32_t*>(take(f1));
-    B.scell = reinterpret_cast<int4*>(take(f4));
-    s->staging = reinterpret_cast<float*>(take(f3));
-    B.rkeys = reinterpret_cast<unsigned long long*>(take(f2));
-    B.rsorted = reinterpret_cast<unsigned long long*>(take(f2));
-    B.ridx = reinterpret_cast<uint32_t*>(take(f1));
-    B.pos_of = reinterpret_cast<uint32_t*>(take(f1));
-    B.kpos = reinterpret_cast<uint32_t*>(take(f1));
-    B.bend = reinterpret_cast<uint32_t*>(take(f1));
-    B.sown = reinterpret_cast<int*>(take(f1));
-    B.btab = reinterpret_cast<uint32_t*>(take(f27));
+    s->B.x = reinterpret_cast<float4*>(p);
+    s->B.v = reinterpret_cast<float4*>(p + f4);
+    s->B.rho = reinterpret_cast<float*>(p + 2 * f4);
+    s->B.lam = reinterpret_cast<float*>(p + 2 * f4 + f1);
+    s->staging = reinterpret_cast<float*>(p + 2 * f4 + 2 * f1);
     PBF_CUDA(cudaMemsetAsync(s->pmem, 0, total, s->stream));
+    s->cap = c;
+    return PBF_OK;
+}
+
+// Step scratch for the scene's capacity (sorted copies, keys, buckets, sort).
+int ensure_work(pbf_scene* s) {
+    if (s->wmem && s->work_cap >= s->cap) return PBF_OK;
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    for (void* m : {s->wmem, s->smem})
+        if (m) cudaFree(m);
+    s->wmem = s->smem = nullptr;
+    s->work_cap = 0;
+    const int c = s->cap > 0 ? s->cap : 1;
+    const size_t wb = work_bytes(c);
+    PBF_CUDA(cudaMalloc(&s->wmem, wb));
+    PBF_CUDA(cudaMemsetAsync(s->wmem, 0, wb, s->stream));
+    bind_work(s->B, s->wmem, c);
     const size_t sb = sort_scratch_bytes(c);
     PBF_CUDA(cudaMalloc(&s->smem, sb));
     PBF_CUDA(cudaMemsetAsync(s->smem, 0, sb, s->stream));
     sort_scratch_bind(s->sort, s->smem, c);
-    B.err = s->sort.err;
-    B.off = s->off;
-    if (s->off) B.slot_alias = reinterpret_cast<unsigned char*>(s->off) +
-                                align_up((size_t)s->off_cap * 4, 256);
-    s->cap = c;
+    s->B.err = s->sort.err;
+    s->work_cap = c;
     return PBF_OK;
 }
+
+}  // namespace
+
+namespace pbf {
+namespace capi {
 
 int check_settings(const pbf_settings* st) {
     if (!st) return fail(PBF_ERR_INVALID_ARG, "settings is NULL");
@@ -261,7 +198,7 @@ GridDesc fit_grid(const pbf_scene* s) {
             if (g[d] > g[m]) m = d;
         g[m] = std::max(4LL, g[m] / 2);
     }
-    GridDesc G;
+    GridDesc G{};
     G.ox = (int)o[0];
     G.oy = (int)o[1];
     G.oz = (int)o[2];
@@ -274,6 +211,11 @@ GridDesc fit_grid(const pbf_scene* s) {
     G.key_bits = bits;
     return G;
 }
+
+}  // namespace capi
+}  // namespace pbf
+
+namespace {
 
 int ensure_offsets(pbf_scene* s, uint32_t nslots) {
     if (s->off && s->off_cap >= nslots + 1) return PBF_OK;
@@ -301,8 +243,13 @@ float host_poly6(float r_sq, float h) {
     return (315.0f / (64.0f * kPi * h9)) * diff * diff * diff;
 }
 
+}  // namespace
+
+namespace pbf {
+namespace capi {
+
 // Per-step constants from settings (operation order of pbf_solver.cpp).
-int make_consts(pbf_scene* s, float dt, StepConsts& C) {
+int scene_consts(const pbf_scene* s, float dt, StepConsts& C) {
     const pbf_settings& st = s->settings;
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(PBF_ERR_INVALID_ARG, "dt must be > 0");
     std::memset(&C, 0, sizeof(C));
@@ -360,8 +307,24 @@ int make_consts(pbf_scene* s, float dt, StepConsts& C) {
         C.hi[d] = st.domain_upper[d] - pr;
     }
     C.hash_compat = st.hash_compat ? 1 : 0;
+    C.iters = st.solver_iterations;
+    C.seg_begin = 0;
+    C.seg_end = (uint32_t)s->n;
     C.grid = fit_grid(s);
-    return ensure_offsets(s, C.grid.nslots);
+    return PBF_OK;
+}
+
+}  // namespace capi
+}  // namespace pbf
+
+namespace {
+
+// Constants of the scene's own step, with its offsets table and scratch.
+int make_consts(pbf_scene* s, float dt, StepConsts& C) {
+    int rc = scene_consts(s, dt, C);
+    if (!rc) rc = ensure_offsets(s, C.grid.nslots);
+    if (!rc) rc = ensure_work(s);
+    return rc;
 }
 
 void update_bbox(pbf_scene* s, const float* x3, int n) {
@@ -600,6 +563,7 @@ int pbf_scene_destroy(pbf_scene* s) {
         free_particles(s);
         if (s->off) cudaFree(s->off);
         if (s->d_flag) cudaFree(s->d_flag);
+        if (s->ev) cudaEventDestroy(s->ev);
         if (s->stream) cudaStreamDestroy(s->stream);
     }
     delete s;
@@ -681,15 +645,6 @@ int pbf_scene_step_timed(pbf_scene* s, float dt, int nsteps, float* ms_out) {
 
 }  // extern "C"
 
-struct pbf_snapshot {
-    int device = 0;
-    int n = 0;
-    pbf_settings settings{};
-    float gravity[3] = {0, 0, 0};
-    float mass = 0.0f;
-    void* mem = nullptr;  // x (float4 n) | v (float4 n) | rho (n) | lam (n)
-};
-
 namespace {
 size_t snapshot_bytes(int n) { return (size_t)n * (16 + 16 + 4 + 4); }
 }  // namespace
@@ -751,9 +706,10 @@ int pbf_snapshot_num_particles(const pbf_snapshot* snap, int* out) {
 
 }  // extern "C"
 
-namespace {
-// Copies a snapshot into the scene on its stream (asynchronous).
-int restore_async(pbf_scene* s, const pbf_snapshot* snap) {
+namespace pbf {
+namespace capi {
+
+int restore_on(pbf_scene* s, const pbf_snapshot* snap, cudaStream_t st) {
     if (snap->device != s->device) return fail(PBF_ERR_INVALID_ARG, "snapshot is on another device");
     if (snap->n > s->cap || !s->pmem) {
         int rc = alloc_particles(s, snap->n);
@@ -766,12 +722,31 @@ int restore_async(pbf_scene* s, const pbf_snapshot* snap) {
     if (snap->n == 0) return PBF_OK;
     const char* p = reinterpret_cast<const char*>(snap->mem);
     const size_t n = (size_t)snap->n;
-    PBF_CUDA(cudaMemcpyAsync(s->B.x, p, n * 16, cudaMemcpyDeviceToDevice, s->stream));
-    PBF_CUDA(cudaMemcpyAsync(s->B.v, p + n * 16, n * 16, cudaMemcpyDeviceToDevice, s->stream));
-    PBF_CUDA(cudaMemcpyAsync(s->B.rho, p + n * 32, n * 4, cudaMemcpyDeviceToDevice, s->stream));
-    PBF_CUDA(cudaMemcpyAsync(s->B.lam, p + n * 36, n * 4, cudaMemcpyDeviceToDevice, s->stream));
+    PBF_CUDA(cudaMemcpyAsync(s->B.x, p, n * 16, cudaMemcpyDeviceToDevice, st));
+    PBF_CUDA(cudaMemcpyAsync(s->B.v, p + n * 16, n * 16, cudaMemcpyDeviceToDevice, st));
+    PBF_CUDA(cudaMemcpyAsync(s->B.rho, p + n * 32, n * 4, cudaMemcpyDeviceToDevice, st));
+    PBF_CUDA(cudaMemcpyAsync(s->B.lam, p + n * 36, n * 4, cudaMemcpyDeviceToDevice, st));
     return PBF_OK;
 }
+
+size_t scene_device_bytes(const pbf_scene* s) {
+    size_t b = 0;
+    if (s->pmem) {
+        const int c = s->cap > 0 ? s->cap : 1;
+        b += 2 * align_up((size_t)c * 16, 256) + 2 * align_up((size_t)c * 4, 256) +
+             align_up((size_t)c * 12, 256);
+    }
+    if (s->wmem) b += work_bytes(s->work_cap) + sort_scratch_bytes(s->work_cap);
+    if (s->off) b += align_up((size_t)s->off_cap * 4, 256) + align_up(s->off_cap, 256);
+    return b;
+}
+
+}  // namespace capi
+}  // namespace pbf
+
+namespace {
+// Copies a snapshot into the scene on its stream (asynchronous).
+int restore_async(pbf_scene* s, const pbf_snapshot* snap) { return restore_on(s, snap, s->stream); }
 }  // namespace
 
 extern "C" {

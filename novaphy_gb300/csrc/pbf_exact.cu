@@ -13,6 +13,11 @@ cudaError_t exact_enqueue_step(const StepBuffers& B, const StepConsts& C, int it
     return exact::enqueue_step(B, C, iters, sort, st, pm);
 }
 
+cudaError_t exact_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortScratch& sort,
+                                cudaStream_t st, PhaseMarks* pm) {
+    return exact::enqueue_batch_step(B, D, sort, st, pm);
+}
+
 cudaError_t debug_cells(const StepBuffers& B, const StepConsts& C, int* d_cells3,
                         cudaStream_t st) {
     if (C.n <= 0) return cudaSuccess;

@@ -12,4 +12,9 @@ cudaError_t fast_enqueue_step(const StepBuffers& B, const StepConsts& C, int ite
     return fast::enqueue_step(B, C, iters, sort, st, pm);
 }
 
+cudaError_t fast_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortScratch& sort,
+                                cudaStream_t st, PhaseMarks* pm) {
+    return fast::enqueue_batch_step(B, D, sort, st, pm);
+}
+
 }  // namespace pbf

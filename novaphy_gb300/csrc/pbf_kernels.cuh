@@ -65,8 +65,9 @@ __device__ __forceinline__ int wrap(int c, int o, int g) {
     return t < 0 ? t + g : t;
 }
 
+// Global slot of a cell: the grid's base plus its wrapped local index.
 __device__ __forceinline__ uint32_t slot_of(int cx, int cy, int cz, const GridDesc& G) {
-    return (uint32_t)wrap(cx, G.ox, G.gx) +
+    return G.base + (uint32_t)wrap(cx, G.ox, G.gx) +
            (uint32_t)G.gx * ((uint32_t)wrap(cy, G.oy, G.gy) + (uint32_t)G.gy * (uint32_t)wrap(cz, G.oz, G.gz));
 }
 
@@ -89,10 +90,9 @@ __device__ __forceinline__ unsigned long long ref_hash(int cx, int cy, int cz) {
            ((unsigned long long)(long long)cz * 83492791ULL);
 }
 
-// lower_bound over the sorted reference keys.
+// lower_bound over the sorted reference keys in [a, b).
 __device__ __forceinline__ uint32_t key_lower_bound(const unsigned long long* __restrict__ keys,
-                                                    uint32_t n, unsigned long long k) {
-    uint32_t a = 0, b = n;
+                                                    uint32_t a, uint32_t b, unsigned long long k) {
     while (a < b) {
         const uint32_t m = (a + b) >> 1;
         if (__ldg(keys + m) < k) a = m + 1;
@@ -125,7 +125,7 @@ __device__ __forceinline__ void for_each_candidate(const int4 cell, const uint32
             const uint32_t wz = (uint32_t)wrap(cell.z + dz, G.oz, G.gz);
             for (int dy = -1; dy <= 1; ++dy) {
                 const uint32_t wy = (uint32_t)wrap(cell.y + dy, G.oy, G.gy);
-                const uint32_t row = (uint32_t)G.gx * (wy + (uint32_t)G.gy * wz);
+                const uint32_t row = G.base + (uint32_t)G.gx * (wy + (uint32_t)G.gy * wz);
                 const int wx = wrap(cell.x - 1, G.ox, G.gx);
                 if (wx + 2 < G.gx) {
                     const uint32_t q1 = __ldg(off + row + wx + 3);
@@ -152,6 +152,38 @@ __device__ __forceinline__ void for_each_candidate(const int4 cell, const uint32
 }
 
 // ---------------------------------------------------------------------------
+// Where a kernel finds its step constants and particle state.  One scene: the
+// constants and the state arrays travel by value in the kernel parameters.
+// A batch of scenes: tables with one entry per scene, indexed by the scene of
+// the particle (sid, in the order the kernel walks); batch particle i of a
+// scene whose particles start at `first` is the scene's particle i - first.
+
+struct OneScene {
+    StepConsts C;
+    StateRef S;
+    __device__ __forceinline__ const StepConsts& at(const uint32_t*, uint32_t) const { return C; }
+    __device__ __forceinline__ const StateRef& state(const uint32_t*, uint32_t) const { return S; }
+};
+
+struct SceneTable {
+    const StepConsts* __restrict__ tab;
+    const StateRef* __restrict__ refs;
+    __device__ __forceinline__ StepConsts at(const uint32_t* __restrict__ sid, uint32_t i) const {
+        return tab[__ldg(sid + i)];
+    }
+    __device__ __forceinline__ StateRef state(const uint32_t* __restrict__ sid, uint32_t i) const {
+        return refs[__ldg(sid + i)];
+    }
+};
+
+// Scene ids of a step: per particle in particle order (pid) and in the
+// cell-sorted order (spid); null for a single scene.
+struct SceneIds {
+    const uint32_t* __restrict__ pid;
+    uint32_t* __restrict__ spid;
+};
+
+// ---------------------------------------------------------------------------
 // Grid construction kernels
 
 // v' = v + g dt;  x* = x + v' dt  (pbf_solver.cpp:31-32), rounded product
@@ -167,13 +199,17 @@ __device__ __forceinline__ void predict(const float4 xi, const float4 vi, const 
 }
 
 // Predict + cell slot and reference hash key per particle (particle order).
+template <class P>
 __global__ void __launch_bounds__(kBlock)
-k_predict_key(const float4* __restrict__ x, const float4* __restrict__ v, uint32_t* __restrict__ keys,
-              unsigned long long* __restrict__ rkeys, const StepConsts C) {
+k_predict_key(uint32_t* __restrict__ keys, unsigned long long* __restrict__ rkeys, int n,
+              const SceneIds S, const P prm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= C.n) return;
+    if (i >= n) return;
+    const StepConsts& C = prm.at(S.pid, i);
+    const StateRef& R = prm.state(S.pid, i);
+    const uint32_t l = (uint32_t)i - R.first;
     float px, py, pz;
-    predict(x[i], v[i], C, px, py, pz);
+    predict(R.x[l], R.v[l], C, px, py, pz);
     int cx, cy, cz;
     cell_of(px, py, pz, C.inv_cell, cx, cy, cz);
     keys[i] = slot_of(cx, cy, cz, C.grid);
@@ -195,41 +231,48 @@ k_offsets(const uint32_t* __restrict__ skeys, int n, uint32_t* __restrict__ off,
 }
 
 // Gather particle state into cell-sorted order; recompute x* exactly as
-// predicted.  Records each particle's sorted position and flags slots that
-// receive a particle from outside the grid box (wrapped alias).
+// predicted.  Records each particle's sorted position (and scene) and flags
+// slots that receive a particle from outside the grid box (wrapped alias).
+template <class P>
 __global__ void __launch_bounds__(kBlock)
-k_gather(const uint32_t* __restrict__ sidx, const float4* __restrict__ x, const float4* __restrict__ v,
-         const float* __restrict__ rho, const float* __restrict__ lam, float4* __restrict__ sx,
-         float4* __restrict__ xa, float* __restrict__ srho, int4* __restrict__ scell,
-         uint32_t* __restrict__ pos_of, unsigned char* __restrict__ slot_alias,
-         uint32_t* __restrict__ err, const StepConsts C) {
+k_gather(const uint32_t* __restrict__ sidx, float4* __restrict__ sx, float4* __restrict__ xa,
+         float* __restrict__ srho, int4* __restrict__ scell, uint32_t* __restrict__ pos_of,
+         unsigned char* __restrict__ slot_alias, uint32_t* __restrict__ err, int n,
+         const SceneIds S, const P prm) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= C.n) return;
+    if (p >= n) return;
     uint32_t i = sidx[p];
-    if (i >= (uint32_t)C.n) {  // only after a failed sort; keep every access in range
+    if (i >= (uint32_t)n) {  // only after a failed sort; keep every access in range
         atomicOr(err, 2u);
         i = 0;
     }
-    const float4 xi = x[i];
+    const StepConsts& C = prm.at(S.pid, i);
+    const StateRef& R = prm.state(S.pid, i);
+    const uint32_t l = i - R.first;
+    const float4 xi = R.x[l];
     float px, py, pz;
-    predict(xi, v[i], C, px, py, pz);
+    predict(xi, R.v[l], C, px, py, pz);
     int cx, cy, cz;
     cell_of(px, py, pz, C.inv_cell, cx, cy, cz);
     sx[p] = make_float4(xi.x, xi.y, xi.z, __uint_as_float(i));
-    xa[p] = make_float4(px, py, pz, lam[i]);
-    srho[p] = rho[i];
+    xa[p] = make_float4(px, py, pz, R.lam[l]);
+    srho[p] = R.rho[l];
     scell[p] = make_int4(cx, cy, cz, 0);
     pos_of[i] = (uint32_t)p;
+    if (S.spid) S.spid[p] = S.pid[i];
     if (!in_grid(cx, cy, cz, C.grid)) slot_alias[slot_of(cx, cy, cz, C.grid)] = 1;
 }
 
 // Reference buckets in key-sorted order: kpos maps key-sorted positions to
 // cell-sorted ones; at each bucket start, bend holds the bucket end with
-// kImpureBit set when the bucket mixes cells (hash collision).
+// kImpureBit set when the bucket mixes cells (hash collision).  With scene
+// ids (ksid, in key-sorted order) a bucket never crosses a scene boundary:
+// every scene has its own hash grid.
 __global__ void __launch_bounds__(256)
 k_buckets(const unsigned long long* __restrict__ rsorted, const uint32_t* __restrict__ ridx,
           const uint32_t* __restrict__ pos_of, const int4* __restrict__ scell,
-          uint32_t* __restrict__ kpos, uint32_t* __restrict__ bend, int n) {
+          const uint32_t* __restrict__ ksid, uint32_t* __restrict__ kpos,
+          uint32_t* __restrict__ bend, int n) {
     const int kp = blockIdx.x * blockDim.x + threadIdx.x;
     if (kp >= n) return;
     const uint32_t i0 = ridx[kp];
@@ -237,11 +280,12 @@ k_buckets(const unsigned long long* __restrict__ rsorted, const uint32_t* __rest
     if (p0 >= (uint32_t)n) p0 = 0;
     kpos[kp] = p0;
     const unsigned long long k = rsorted[kp];
-    if (kp > 0 && rsorted[kp - 1] == k) return;
+    const uint32_t s0 = ksid ? ksid[kp] : 0u;
+    if (kp > 0 && rsorted[kp - 1] == k && (!ksid || ksid[kp - 1] == s0)) return;
     const int4 c0 = scell[p0];
     bool pure = true;
     int e = kp + 1;
-    while (e < n && rsorted[e] == k) {
+    while (e < n && rsorted[e] == k && (!ksid || ksid[e] == s0)) {
         if (pure) {
             const uint32_t ie = ridx[e];
             uint32_t pe = pos_of[ie < (uint32_t)n ? ie : 0];
@@ -258,25 +302,30 @@ k_buckets(const unsigned long long* __restrict__ rsorted, const uint32_t* __rest
 // buckets over a source point set (qown[p] = owner + 1, else 0) and stores
 // their 27 bucket starts in row `owner` of btab.  Query cells are qcell[0..nq),
 // the source's key-sorted buckets are (rsorted, kpos, bend) with cells scell
-// and slot alias flags of the source's grid.  Within a warp, one lane per
-// distinct cell does the 27 lookups; the other lanes of the cell reuse its row.
+// and slot alias flags of the source's grid; a query of scene s searches the
+// scene's key range [seg_begin, seg_end).  Within a warp, one lane per
+// distinct cell (and scene) does the 27 lookups; the other lanes reuse its row.
+template <class P>
 __global__ void __launch_bounds__(kBlock)
-k_classify(const int4* __restrict__ qcell, int nq, const int4* __restrict__ scell, int ns,
+k_classify(const int4* __restrict__ qcell, int nq, const int4* __restrict__ scell,
            const unsigned long long* __restrict__ rsorted, const uint32_t* __restrict__ kpos,
            const uint32_t* __restrict__ bend, const unsigned char* __restrict__ slot_alias,
-           uint32_t* __restrict__ btab, int* __restrict__ qown, const StepConsts C) {
+           uint32_t* __restrict__ btab, int* __restrict__ qown, const uint32_t* __restrict__ qsid,
+           const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = p < (uint32_t)nq;
     const int lane = threadIdx.x & 31;
     const int4 cell = active ? qcell[p] : make_int4(0x7fffffff, 0x7fffffff, 0x7fffffff, 0);
+    const uint32_t sc = (active && qsid) ? qsid[p] : 0xffffffffu;
     const unsigned long long kxy =
         ((unsigned long long)(unsigned)cell.x << 32) | (unsigned long long)(unsigned)cell.y;
     const uint32_t same = __match_any_sync(0xffffffffu, kxy) &
                           __match_any_sync(0xffffffffu, (unsigned)cell.z) &
-                          __ballot_sync(0xffffffffu, active);
+                          __match_any_sync(0xffffffffu, sc) & __ballot_sync(0xffffffffu, active);
     const int leader = same ? __ffs(same) - 1 : lane;
     int dirty = 0;
-    if (active && lane == leader) {
+    if (active && lane == leader && prm.at(qsid, p).hash_compat) {
+        const StepConsts& C = prm.at(qsid, p);
         uint32_t tab[27];
         int m = 0;
         for (int dz = -1; dz <= 1; ++dz)
@@ -284,8 +333,8 @@ k_classify(const int4* __restrict__ qcell, int nq, const int4* __restrict__ scel
                 for (int dx = -1; dx <= 1; ++dx, ++m) {
                     const int nx = cell.x + dx, ny = cell.y + dy, nz = cell.z + dz;
                     const unsigned long long k = ref_hash(nx, ny, nz);
-                    const uint32_t lb = key_lower_bound(rsorted, (uint32_t)ns, k);
-                    if (lb < (uint32_t)ns && __ldg(rsorted + lb) == k) {
+                    const uint32_t lb = key_lower_bound(rsorted, C.seg_begin, C.seg_end, k);
+                    if (lb < C.seg_end && __ldg(rsorted + lb) == k) {
                         tab[m] = lb;
                         const uint32_t e = __ldg(bend + lb);
                         const int4 c0 = scell[__ldg(kpos + lb)];
@@ -315,6 +364,7 @@ struct Grid {
     const uint32_t* __restrict__ kpos;
     const uint32_t* __restrict__ bend;
     const uint32_t* __restrict__ btab;
+    const uint32_t* __restrict__ spid;  // scene of each sorted particle (batches)
 };
 
 __device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
@@ -325,11 +375,15 @@ __device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
 
 // compute_density + compute_lambda (pbf_solver.cpp:129-179) in one candidate
 // pass.  Reads x* from xin, writes (x*, lambda) to xout and rho to srho.
+// Scenes whose `iters` are done by iteration `it` are left untouched.
+template <class P>
 __global__ void __launch_bounds__(kBlock)
 k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
-                 const Grid G, const StepConsts C) {
+                 int it, int n, const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)C.n) return;
+    if (p >= (uint32_t)n) return;
+    const StepConsts& C = prm.at(G.spid, p);
+    if (it >= C.iters) return;
     const float4 xi = xin[p];
     float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
@@ -376,14 +430,17 @@ __device__ __forceinline__ float4 update_velocity(float px, float py, float pz, 
 }
 
 // compute_delta_position + apply_delta (pbf_solver.cpp:181-223, :74-76).
-// Reads (x*, lambda) from xin, writes (x* + dp, lambda_i) to xout; on the last
-// iteration also the updated velocity into sv.
+// Reads (x*, lambda) from xin, writes (x* + dp, lambda_i) to xout; on the
+// scene's last iteration also the updated velocity into sv.
+template <class P>
 __global__ void __launch_bounds__(kBlock)
 k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
-        const float* __restrict__ srho, float4* __restrict__ sv, int last, const Grid G,
-        const StepConsts C) {
+        const float* __restrict__ srho, float4* __restrict__ sv, int it, int n, const Grid G,
+        const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)C.n) return;
+    if (p >= (uint32_t)n) return;
+    const StepConsts& C = prm.at(G.spid, p);
+    if (it >= C.iters) return;
     const float4 xi = xin[p];
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
@@ -413,15 +470,18 @@ k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4*
     const float py = xi.y + dy * C.inv_rho0;
     const float pz = xi.z + dz * C.inv_rho0;
     xout[p] = make_float4(px, py, pz, xi.w);
-    if (last) sv[p] = update_velocity(px, py, pz, sx[p], srho[p], C);
+    if (it == C.iters - 1) sv[p] = update_velocity(px, py, pz, sx[p], srho[p], C);
 }
 
-// Velocity update alone, for solver_iterations == 0.
+// Velocity update alone, for scenes with solver_iterations == 0.
+template <class P>
 __global__ void __launch_bounds__(kBlock)
 k_velocity(const float4* __restrict__ xin, const float4* __restrict__ sx, const float* __restrict__ srho,
-           float4* __restrict__ sv, const StepConsts C) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= C.n) return;
+           float4* __restrict__ sv, int n, const Grid G, const P prm) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)n) return;
+    const StepConsts& C = prm.at(G.spid, p);
+    if (C.iters > 0) return;
     const float4 xi = xin[p];
     sv[p] = update_velocity(xi.x, xi.y, xi.z, sx[p], srho[p], C);
 }
@@ -429,36 +489,39 @@ k_velocity(const float4* __restrict__ xin, const float4* __restrict__ sx, const 
 // Domain clamp + commit (pbf_solver.cpp:102-126), scattered to particle order.
 __device__ __forceinline__ void commit(uint32_t p, float px, float py, float pz, float vx, float vy,
                                        float vz, float lam, const float4* __restrict__ sx,
-                                       const float* __restrict__ srho, float4* __restrict__ x,
-                                       float4* __restrict__ v, float* __restrict__ rho,
-                                       float* __restrict__ lamo, const StepConsts& C) {
+                                       const float* __restrict__ srho, const StateRef& R, int n,
+                                       const StepConsts& C) {
     if (C.clamp) {
         if (px < C.lo[0]) { px = C.lo[0]; vx = 0.0f; } else if (px > C.hi[0]) { px = C.hi[0]; vx = 0.0f; }
         if (py < C.lo[1]) { py = C.lo[1]; vy = 0.0f; } else if (py > C.hi[1]) { py = C.hi[1]; vy = 0.0f; }
         if (pz < C.lo[2]) { pz = C.lo[2]; vz = 0.0f; } else if (pz > C.hi[2]) { pz = C.hi[2]; vz = 0.0f; }
     }
     uint32_t i = __float_as_uint(sx[p].w);
-    if (i >= (uint32_t)C.n) i = 0;
-    x[i] = make_float4(px, py, pz, 0.0f);
-    v[i] = make_float4(vx, vy, vz, 0.0f);
-    rho[i] = srho[p];
-    lamo[i] = lam;
+    if (i >= (uint32_t)n) i = 0;
+    const uint32_t l = i - R.first;
+    R.x[l] = make_float4(px, py, pz, 0.0f);
+    R.v[l] = make_float4(vx, vy, vz, 0.0f);
+    R.rho[l] = srho[p];
+    R.lam[l] = lam;
 }
 
 // apply_xsph_viscosity (pbf_solver.cpp:225-250) + commit, no vorticity.
+// With skip_vort set, scenes with vorticity are left to the vorticity pair.
+template <class P>
 __global__ void __launch_bounds__(kBlock)
 k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, const float4* __restrict__ sx,
-              const float* __restrict__ srho, float4* __restrict__ x, float4* __restrict__ v,
-              float* __restrict__ rho, float* __restrict__ lam, const Grid G, const StepConsts C) {
+              const float* __restrict__ srho, int n, int skip_vort, const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)C.n) return;
+    if (p >= (uint32_t)n) return;
+    const StepConsts& C = prm.at(G.spid, p);
+    if (skip_vort && C.vort_on) return;
     const float4 xi = xin[p];
     const float4 vi = sv[p];
     float vx = vi.x, vy = vi.y, vz = vi.z;
     if (C.xsph_on) {
         float cx = 0.0f, cy = 0.0f, cz = 0.0f;
         for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-                const float4 xj = __ldg(xin + q);
+            const float4 xj = __ldg(xin + q);
             const float rx = xi.x - xj.x;
             const float ry = xi.y - xj.y;
             const float rz = xi.z - xj.z;
@@ -475,18 +538,21 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
         vy = vi.y + C.xsph_c * cy;
         vz = vi.z + C.xsph_c * cz;
     }
-    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, x, v, rho, lam, C);
+    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, prm.state(G.spid, p), n, C);
 }
 
 // XSPH correction + vorticity omega in one candidate pass (vorticity path).
 // Writes the post-XSPH velocity to sv2 and (omega, |omega|) to som, with
 //   omega_i = sum_j (m/rho_j') spiky_grad(x*_i - x*_j) x (v_j - v_i),
 // the SPH curl (Macklin & Mueller 2013, section 5, with its volume factor).
+template <class P>
 __global__ void __launch_bounds__(kBlock)
 k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, float4* __restrict__ sv2,
-             float4* __restrict__ som, const Grid G, const StepConsts C) {
+             float4* __restrict__ som, int n, const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)C.n) return;
+    if (p >= (uint32_t)n) return;
+    const StepConsts& C = prm.at(G.spid, p);
+    if (!C.vort_on) return;
     const float4 xi = xin[p];
     const float4 vi = sv[p];
     float cx = 0.0f, cy = 0.0f, cz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
@@ -525,14 +591,16 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
 // Vorticity confinement (Macklin & Mueller 2013, section 5) + commit:
 //   eta_i = sum_j (m/rho_j') (|omega_j| - |omega_i|) spiky_grad(x*_i - x*_j),
 //   N = eta / |eta|,  v += dt * eps * (N x omega_i).
+template <class P>
 __global__ void __launch_bounds__(kBlock)
 k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv,
                    const float4* __restrict__ sv2, const float4* __restrict__ som,
-                   const float4* __restrict__ sx, const float* __restrict__ srho,
-                   float4* __restrict__ x, float4* __restrict__ v, float* __restrict__ rho,
-                   float* __restrict__ lam, const Grid G, const StepConsts C) {
+                   const float4* __restrict__ sx, const float* __restrict__ srho, int n,
+                   const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)C.n) return;
+    if (p >= (uint32_t)n) return;
+    const StepConsts& C = prm.at(G.spid, p);
+    if (!C.vort_on) return;
     const float4 xi = xin[p];
     const float4 wi = som[p];
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
@@ -564,7 +632,7 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     const float vx = vb.x + C.vort_scale * fx;
     const float vy = vb.y + C.vort_scale * fy;
     const float vz = vb.z + C.vort_scale * fz;
-    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, x, v, rho, lam, C);
+    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, prm.state(G.spid, p), n, C);
 }
 
 // ---------------------------------------------------------------------------
@@ -612,20 +680,25 @@ k_debug_neighbors(const float4* __restrict__ xin, const float4* __restrict__ sx,
 
 inline int grid_of(int n, int b) { return (n + b - 1) / b; }
 
-inline Grid grid_view(const StepBuffers& B) {
-    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab};
+inline Grid grid_view(const StepBuffers& B, const uint32_t* spid = nullptr) {
+    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid};
 }
 
 // predict, sort by cell and by reference key, cell offsets, gather, reference
-// buckets, classification: the neighbour structure of the step.
+// buckets, classification: the neighbour structure of one scene's step.
 inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, SortScratch& sort,
                                   cudaStream_t st, PhaseMarks* pm = nullptr) {
     const int n = C.n;
     const int nb = grid_of(n, kBlock);
+    StepConsts Cs = C;
+    Cs.seg_begin = 0;
+    Cs.seg_end = (uint32_t)n;
+    const OneScene one{Cs, StateRef{B.x, B.v, B.rho, B.lam, 0u}};
+    const SceneIds none{nullptr, nullptr};
     cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)C.grid.nslots, st);
     if (e != cudaSuccess) return e;
     if (pm) pm->mark(-1, 0, st);
-    k_predict_key<<<nb, kBlock, 0, st>>>(B.x, B.v, B.keys, B.rkeys, C);
+    k_predict_key<<<nb, kBlock, 0, st>>>(B.keys, B.rkeys, n, none, one);
     if (pm) pm->mark(kPhasePredict, 1, st);
     e = radix_sort_pairs(B.keys, B.skeys, B.sidx, n, C.grid.key_bits, sort, st);
     if (e != cudaSuccess) return e;
@@ -637,13 +710,13 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     }
     k_offsets<<<grid_of((int)C.grid.nslots + 1, 256), 256, 0, st>>>(B.skeys, n, B.off, C.grid.nslots);
     if (pm) pm->mark(kPhaseGridBuild, launches, st);
-    k_gather<<<nb, kBlock, 0, st>>>(B.sidx, B.x, B.v, B.rho, B.lam, B.sx, B.xa, B.srho, B.scell,
-                                    B.pos_of, B.slot_alias, B.err, C);
+    k_gather<<<nb, kBlock, 0, st>>>(B.sidx, B.sx, B.xa, B.srho, B.scell, B.pos_of, B.slot_alias,
+                                    B.err, n, none, one);
     if (C.hash_compat) {
-        k_buckets<<<grid_of(n, 256), 256, 0, st>>>(B.rsorted, B.ridx, B.pos_of, B.scell, B.kpos,
-                                                   B.bend, n);
-        k_classify<<<nb, kBlock, 0, st>>>(B.scell, n, B.scell, n, B.rsorted, B.kpos, B.bend,
-                                          B.slot_alias, B.btab, B.sown, C);
+        k_buckets<<<grid_of(n, 256), 256, 0, st>>>(B.rsorted, B.ridx, B.pos_of, B.scell, nullptr,
+                                                   B.kpos, B.bend, n);
+        k_classify<<<nb, kBlock, 0, st>>>(B.scell, n, B.scell, B.rsorted, B.kpos, B.bend,
+                                          B.slot_alias, B.btab, B.sown, nullptr, one);
     } else {
         e = cudaMemsetAsync(B.sown, 0, (size_t)n * 4, st);
         if (e != cudaSuccess) return e;
@@ -652,35 +725,131 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     return cudaGetLastError();
 }
 
+// The constraint, velocity, XSPH, vorticity and commit passes over n
+// cell-sorted particles for `max_iters` iterations, with constants from `prm`.
+// Scenes with vorticity take the XSPH+omega / vorticity+commit pair
+// (any_vort), the others XSPH+commit (any_plain).
+template <class P>
+inline cudaError_t enqueue_passes(const StepBuffers& B, const Grid& G, int n, int max_iters,
+                                  bool any_zero_iters, bool any_vort, bool any_plain, bool xsph_on,
+                                  const P prm, cudaStream_t st, PhaseMarks* pm) {
+    const int nb = grid_of(n, kBlock);
+    for (int it = 0; it < max_iters; ++it) {
+        k_density_lambda<<<nb, kBlock, 0, st>>>(B.xa, B.xb, B.srho, it, n, G, prm);
+        if (pm) pm->mark(kPhaseDensity, 1, st);
+        k_delta<<<nb, kBlock, 0, st>>>(B.xb, B.xa, B.sx, B.srho, B.sv, it, n, G, prm);
+        if (pm) pm->mark(kPhaseDelta, 1, st);
+    }
+    if (any_zero_iters) {
+        k_velocity<<<nb, kBlock, 0, st>>>(B.xa, B.sx, B.srho, B.sv, n, G, prm);
+        if (pm) pm->mark(kPhaseDelta, 1, st);
+    }
+    if (any_vort) {
+        k_xsph_omega<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, n, G, prm);
+        if (pm) pm->mark(kPhaseXsph, 1, st);
+        k_vorticity_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, B.sx, B.srho, n, G,
+                                                  prm);
+        if (pm) pm->mark(kPhaseCommit, 1, st);
+    }
+    if (any_plain) {
+        k_xsph_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sx, B.srho, n, any_vort ? 1 : 0, G,
+                                             prm);
+        if (pm) pm->mark(xsph_on ? kPhaseXsph : kPhaseCommit, 1, st);
+    }
+    return cudaGetLastError();
+}
+
 inline cudaError_t enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
                                 SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr) {
     const int n = C.n;
     if (n <= 0) return cudaSuccess;
-    const int nb = grid_of(n, kBlock);
-    const Grid G = grid_view(B);
     cudaError_t e = enqueue_prefix(B, C, sort, st, pm);
     if (e != cudaSuccess) return e;
-    for (int it = 0; it < iters; ++it) {
-        k_density_lambda<<<nb, kBlock, 0, st>>>(B.xa, B.xb, B.srho, G, C);
-        if (pm) pm->mark(kPhaseDensity, 1, st);
-        k_delta<<<nb, kBlock, 0, st>>>(B.xb, B.xa, B.sx, B.srho, B.sv, it == iters - 1 ? 1 : 0, G, C);
-        if (pm) pm->mark(kPhaseDelta, 1, st);
+    StepConsts Ci = C;
+    Ci.iters = iters;
+    return enqueue_passes(B, grid_view(B), n, iters, iters <= 0, C.vort_on != 0, C.vort_on == 0,
+                          C.xsph_on != 0, OneScene{Ci, StateRef{B.x, B.v, B.rho, B.lam, 0u}}, st,
+                          pm);
+}
+
+// ---------------------------------------------------------------------------
+// Batches of independent scenes: one sort and one launch per phase for all.
+
+// Reorders the key sort stably by scene: rsorted[p] = rtmp[perm[p]],
+// ridx[p] = itmp[perm[p]].
+__global__ void __launch_bounds__(256)
+k_apply_scene_perm(const unsigned long long* __restrict__ rtmp, const uint32_t* __restrict__ itmp,
+                   const uint32_t* __restrict__ perm, unsigned long long* __restrict__ rsorted,
+                   uint32_t* __restrict__ ridx, int n) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    uint32_t q = perm[p];
+    if (q >= (uint32_t)n) q = 0;
+    rsorted[p] = rtmp[q];
+    ridx[p] = itmp[q];
+}
+
+// pid[i] = the scene whose particle range holds batch particle i.
+__global__ void __launch_bounds__(256)
+k_scene_ids(const uint32_t* __restrict__ firsts, int nscenes, uint32_t* __restrict__ pid, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int a = 0, b = nscenes - 1;  // last s with firsts[s] <= i
+    while (a < b) {
+        const int m = (a + b + 1) >> 1;
+        if (__ldg(firsts + m) <= (uint32_t)i) a = m;
+        else b = m - 1;
     }
-    if (iters <= 0) {
-        k_velocity<<<nb, kBlock, 0, st>>>(B.xa, B.sx, B.srho, B.sv, C);
-        if (pm) pm->mark(kPhaseDelta, 1, st);
-    }
-    if (C.vort_on) {
-        k_xsph_omega<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, G, C);
-        if (pm) pm->mark(kPhaseXsph, 1, st);
-        k_vorticity_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, B.sx, B.srho, B.x, B.v,
-                                                  B.rho, B.lam, G, C);
-        if (pm) pm->mark(kPhaseCommit, 1, st);
-    } else {
-        k_xsph_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sx, B.srho, B.x, B.v, B.rho, B.lam, G, C);
-        if (pm) pm->mark(C.xsph_on ? kPhaseXsph : kPhaseCommit, 1, st);
-    }
-    return cudaGetLastError();
+    pid[i] = (uint32_t)a;
+}
+
+__global__ void __launch_bounds__(256)
+k_scene_of(const uint32_t* __restrict__ itmp, const uint32_t* __restrict__ pid,
+           uint32_t* __restrict__ stmp, int n) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    uint32_t i = itmp[p];
+    if (i >= (uint32_t)n) i = 0;
+    stmp[p] = pid[i];
+}
+
+inline cudaError_t enqueue_batch_step(const StepBuffers& B, const BatchDesc& D, SortScratch& sort,
+                                      cudaStream_t st, PhaseMarks* pm = nullptr) {
+    const int n = D.n;
+    if (n <= 0) return cudaSuccess;
+    const int nb = grid_of(n, kBlock);
+    const SceneTable tab{D.tab, D.refs};
+    const SceneIds ids{D.pid, D.spid};
+    cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)D.nslots, st);
+    if (e != cudaSuccess) return e;
+    if (pm) pm->mark(-1, 0, st);
+    k_scene_ids<<<grid_of(n, 256), 256, 0, st>>>(D.firsts, D.nscenes, D.pid, n);
+    k_predict_key<<<nb, kBlock, 0, st>>>(B.keys, B.rkeys, n, ids, tab);
+    if (pm) pm->mark(kPhasePredict, 2, st);
+    // Cell order: scene-major because every scene owns a slot range.
+    e = radix_sort_pairs(B.keys, B.skeys, B.sidx, n, D.key_bits, sort, st);
+    if (e != cudaSuccess) return e;
+    // Reference buckets per scene: sort by key, then stably by scene.
+    e = radix_sort_pairs64(B.rkeys, D.rtmp, D.itmp, n, 64, sort, st);
+    if (e != cudaSuccess) return e;
+    k_scene_of<<<grid_of(n, 256), 256, 0, st>>>(D.itmp, D.pid, D.stmp, n);
+    e = radix_sort_pairs(D.stmp, D.kpid, D.perm, n, D.scene_bits, sort, st);
+    if (e != cudaSuccess) return e;
+    k_apply_scene_perm<<<grid_of(n, 256), 256, 0, st>>>(D.rtmp, D.itmp, D.perm, B.rsorted, B.ridx,
+                                                        n);
+    k_offsets<<<grid_of((int)D.nslots + 1, 256), 256, 0, st>>>(B.skeys, n, B.off, D.nslots);
+    if (pm) pm->mark(kPhaseGridBuild, 14 + (D.key_bits + 7) / 8 + (D.scene_bits + 7) / 8, st);
+    k_gather<<<nb, kBlock, 0, st>>>(B.sidx, B.sx, B.xa, B.srho, B.scell, B.pos_of, B.slot_alias,
+                                    B.err, n, ids, tab);
+    k_buckets<<<grid_of(n, 256), 256, 0, st>>>(B.rsorted, B.ridx, B.pos_of, B.scell, D.kpid, B.kpos,
+                                               B.bend, n);
+    k_classify<<<nb, kBlock, 0, st>>>(B.scell, n, B.scell, B.rsorted, B.kpos, B.bend, B.slot_alias,
+                                      B.btab, B.sown, D.spid, tab);
+    if (pm) pm->mark(kPhaseNeighborQuery, 3, st);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return enqueue_passes(B, grid_view(B, D.spid), n, D.max_iters, D.any_zero_iters, D.any_vort,
+                          D.any_plain, D.xsph_on, tab, st, pm);
 }
 
 }  // namespace PBF_NS

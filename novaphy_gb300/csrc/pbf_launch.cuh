@@ -11,6 +11,13 @@ cudaError_t exact_enqueue_step(const StepBuffers& B, const StepConsts& C, int it
 cudaError_t fast_enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
                               SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr);
 
+// One step of a batch of scenes (B holds the batch's scratch; the scenes'
+// state is reached through D.refs).
+cudaError_t exact_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortScratch& sort,
+                                cudaStream_t st, PhaseMarks* pm = nullptr);
+cudaError_t fast_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortScratch& sort,
+                               cudaStream_t st, PhaseMarks* pm = nullptr);
+
 // Parity probes (exact build).
 cudaError_t debug_cells(const StepBuffers& B, const StepConsts& C, int* d_cells3,
                         cudaStream_t st);

@@ -19,6 +19,7 @@ struct GridDesc {
     int gx, gy, gz;
     uint32_t nslots;
     int key_bits;
+    uint32_t base;  // first slot of this grid in a batch's global slot space
 };
 
 // Per-step constants, all computed on the host in float32 with the
@@ -50,6 +51,9 @@ struct StepConsts {
     int clamp;
     float lo[3], hi[3];  // domain_lower + pr, domain_upper - pr (pbf_solver.cpp:105-107)
     int hash_compat;
+    int iters;           // Jacobi iterations of this scene
+    uint32_t seg_begin;  // this scene's range in the key-sorted order of a batch
+    uint32_t seg_end;
     GridDesc grid;
 };
 
@@ -118,6 +122,39 @@ struct PhaseMarks {
             ++count;
         }
     }
+};
+
+// Particle-order state of one scene of a batch; batch particle i of the
+// scene is the scene's particle i - first.
+struct StateRef {
+    float4* x;
+    float4* v;
+    float* rho;
+    float* lam;
+    uint32_t first;
+};
+
+// One step of a batch of independent scenes: particle i of the batch belongs
+// to scene pid[i]; scenes occupy consecutive particle ranges [firsts[s],
+// firsts[s+1]) and consecutive slot ranges of one global cell-slot space.
+struct BatchDesc {
+    int n;               // particles of all scenes
+    int nscenes;
+    uint32_t nslots;     // global slot space (sum of the scenes' grids)
+    int key_bits;        // bits of a global slot
+    int scene_bits;      // bits of a scene id
+    int max_iters;       // largest solver_iterations of the batch
+    bool any_zero_iters, any_vort, any_plain, xsph_on;
+    const StepConsts* tab;  // device tables, one entry per scene
+    const StateRef* refs;
+    const uint32_t* firsts;    // nscenes + 1 particle offsets
+    uint32_t* pid;             // scene of each particle (particle order)
+    uint32_t* spid;            // scene of each cell-sorted particle
+    uint32_t* kpid;            // scene of each key-sorted particle
+    unsigned long long* rtmp;  // key-sorted keys before the scene pass
+    uint32_t* itmp;            // key-sorted particles before the scene pass
+    uint32_t* perm;            // scene-pass permutation
+    uint32_t* stmp;            // scenes of the key-sorted particles before the scene pass
 };
 
 }  // namespace pbf

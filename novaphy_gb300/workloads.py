@@ -85,3 +85,31 @@ def scaled_dam_break(counts, vorticity=1e-4, seed=1) -> Workload:
     """A block of `counts` at the 1M case's density and box (same per-particle work)."""
     return dam_break(counts, 0.01, (4.0, 2.0, 2.0), dt=1.0 / 240.0, jitter=1e-5, seed=seed,
                      vorticity=vorticity, steps=200, name=f"dam_break_{np.prod(counts)}")
+
+
+def batched_scenes(nscenes=1024, seed=3, n_lo=2000, n_hi=64000, r=0.02, dt=1.0 / 120.0,
+                   steps=100, vorticity=1e-4) -> list[Workload]:
+    """Independent dam-break scenes of uneven size for batched stepping.
+
+    Per scene, from ``default_rng(seed)``: a target count N = round(exp(U(ln n_lo,
+    ln n_hi))), a block aspect a ~ U(1, 3) as a:1:1 (ny = nz = round((N/a)^(1/3)),
+    nx = round(N / (ny nz)), so the actual count follows the lattice), a box of
+    U(1.5, 3) x the block extent per axis, solver iterations ~ U{2..6}, a jitter
+    seed; r = 0.02 m, h = 4r, the other parameters as ``dam_break``.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nscenes):
+        target = int(round(float(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))))
+        aspect = float(rng.uniform(1.0, 3.0))
+        ny = max(1, int(round((target / aspect) ** (1.0 / 3.0))))
+        nx = max(1, int(round(target / (ny * ny))))
+        counts = (nx, ny, ny)
+        ext = np.array(counts, np.float64) * r
+        box = tuple(float(np.float32(e * f + r)) for e, f in zip(ext, rng.uniform(1.5, 3.0, 3)))
+        iters = int(rng.integers(2, 7))
+        w = dam_break(counts, r, box, iterations=iters, dt=dt, jitter=1e-4,
+                      seed=int(rng.integers(0, 2**31)), vorticity=vorticity, steps=steps,
+                      name=f"scene_{k}")
+        out.append(w)
+    return out
