@@ -35,6 +35,7 @@ sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import statistics
@@ -236,6 +237,7 @@ def run_batched(args, device):
         for sc, sd in zip(scenes, seeds):
             sc.restore(sd)
 
+    progress(f"batched: {len(wl)} scenes created")
     # Batched arm.
     b = capi.Batch(device)
     reseed()
@@ -249,6 +251,7 @@ def run_batched(args, device):
     reseed()
     dev_ms = b.replay_timed(scenes, seeds, dts, k)
 
+    progress("batched: plain arm")
     # Plain per-scene arm.
     reseed()
     for sc, dt in zip(scenes, dts):  # warm-up: per-scene scratch and graphs
@@ -285,6 +288,277 @@ def run_batched(args, device):
     return out
 
 
+def run_served(args, device):
+    """Serving run over workloads.served_scenes (256 clients, 1k-200k particles
+    log-uniform, dam breaks and pools, dt = 1/240).  Each client draws request
+    arrivals from its own Poisson process with mean 512 ms (so 2 ms for all
+    clients together) and asks for k in {1, 4, 16} steps.
+
+    served: requests go to the serving loop (pbf_server_*, continuous
+    batching).  Run at the full HBM budget and at a reduced budget sized to
+    half of the scenes' charged bytes, where client sessions of 8 requests
+    on average close their scene and open a fresh one so that waiting scenes
+    get admitted.  plain: each client steps its own scene with the drop-in
+    call (pbf_scene_step on the scene's stream, then wait) from its own
+    thread, requests queued per client.  Latency = arrival to completion."""
+    import threading
+
+    from novaphy_gb300 import capi
+
+    wl = workloads.served_scenes()
+    dt = np.float32(wl[0].dt)
+    T = float(args.serve_seconds)
+    rng = np.random.default_rng(44)
+    plans = []
+    for k in range(len(wl)):
+        t, p = 0.0, []
+        while True:
+            t += float(rng.exponential(0.512))
+            if t >= T:
+                break
+            p.append((t, int(rng.choice([1, 4, 16]))))
+        plans.append(p)
+    demand = sum(wl[k].n * m for k in range(len(wl)) for _, m in plans[k])
+
+    deadline_after = T + 90.0  # stop waiting for stragglers 90 s after the last arrival
+
+    def served_run(budget=None, session_mean=None, max_batch=16 << 20):
+        cfg = capi.server_config(max_batch_particles=max_batch)
+        if budget is not None:
+            cfg.hbm_budget_bytes = int(budget)
+        srv = capi.Server(cfg, device)
+        errors = []
+        lock = threading.Lock()
+        t0 = time.perf_counter() + 0.5
+        deadline = t0 + deadline_after
+
+        def wait_all(reqs):
+            for q in reqs:
+                srv.wait(q, timeout=max(0.0, deadline - time.perf_counter()))
+
+        def client(k):
+            w = wl[k]
+            st = capi.default_settings(**w.settings)
+            r = np.random.default_rng(1000 + k)
+            try:
+                sid, _ = srv.open_scene(st, w.x, w.v, w.mass, w.gravity)
+                left = int(r.geometric(1.0 / session_mean)) if session_mean else -1
+                mine = []
+                for (ta, m) in plans[k]:
+                    d = t0 + ta - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    if left == 0:
+                        wait_all(mine)
+                        mine = []
+                        srv.close_scene(sid)
+                        sid, _ = srv.open_scene(st, w.x, w.v, w.mass, w.gravity)
+                        left = int(r.geometric(1.0 / session_mean))
+                    mine.append(srv.submit(sid, float(dt), m))
+                    left -= 1
+                wait_all(mine)
+                srv.close_scene(sid)
+            except capi.PbfError as e:
+                with lock:
+                    errors.append(str(e))
+
+        th = [threading.Thread(target=client, args=(k,)) for k in range(len(wl))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        el = time.perf_counter() - t0
+        stats = srv.stats()
+        srv.close()
+        return {"value": stats["particle_steps"] / el, "unit": UNIT, "wall_s": el,
+                "particle_steps": stats["particle_steps"],
+                "step_ms_p50": stats["step_ms_p50"], "step_ms_p99": stats["step_ms_p99"],
+                "request_ms_p50": stats["request_ms_p50"],
+                "request_ms_p99": stats["request_ms_p99"],
+                "requests_done": stats["requests_done"],
+                "requests_failed": stats["requests_failed"],
+                "scenes_failed": stats["scenes_failed"],
+                "client_errors": len(errors),
+                "errors": dict(__import__("collections").Counter(errors).most_common(3)),
+                "launches": stats["launches"], "mean_launch_scenes": stats["mean_launch_scenes"],
+                "issue_ms_mean": stats["issue_ms_mean"],
+                "graph_captures": stats["graph_captures"], "graph_updates": stats["graph_updates"],
+                "graph_instantiations": stats["graph_instantiations"],
+                "mean_launch_particles": stats["mean_launch_particles"],
+                "scenes_rejected": stats["scenes_rejected"],
+                "hbm_bytes_scratch": stats["hbm_bytes_scratch"],
+                "budget_bytes": int(cfg.hbm_budget_bytes)}
+
+    def plain_run():
+        scenes = []
+        for w in wl:
+            sc = capi.Scene(capi.default_settings(**w.settings), w.x, w.v, mass=w.mass,
+                            device=device)
+            sc.set_gravity(w.gravity)
+            sc.step(float(dt), 1)  # warm-up: scratch and the step graph
+            sc.reset(w.x, w.v)
+            scenes.append(sc)
+        lat_step, lat_req = [], []
+        done = [0]
+        lock = threading.Lock()
+        t0 = time.perf_counter() + 0.5
+        deadline = t0 + deadline_after
+
+        def client(k):
+            sc = scenes[k]
+            for (ta, m) in plans[k]:
+                d = t0 + ta - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                if time.perf_counter() > deadline:
+                    break
+                prev = max(t0 + ta, time.perf_counter())
+                steps = []
+                for _ in range(m):
+                    sc.step(float(dt), 1)
+                    now = time.perf_counter()
+                    steps.append((now - prev) * 1e3)
+                    prev = now
+                with lock:
+                    lat_step.extend(steps)
+                    lat_req.append((time.perf_counter() - (t0 + ta)) * 1e3)
+                    done[0] += wl[k].n * m
+
+        th = [threading.Thread(target=client, args=(k,)) for k in range(len(wl))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        el = time.perf_counter() - t0
+        for sc in scenes:
+            sc.close()
+        return {"value": done[0] / el, "unit": UNIT, "wall_s": el, "particle_steps": done[0],
+                "step_ms_p50": percentile(lat_step, 50), "step_ms_p99": percentile(lat_step, 99),
+                "request_ms_p50": percentile(lat_req, 50),
+                "request_ms_p99": percentile(lat_req, 99)}
+
+    progress("served: full budget")
+    full = served_run()
+    total_charge = sum(w.n for w in wl) * capi.state_bytes_per_particle()
+    small_batch = 1 << 20
+    probe = capi.Server(capi.server_config(max_batch_particles=small_batch), device)
+    scratch = probe.stats()["hbm_bytes_scratch"]
+    probe.close()
+    progress("served: reduced budget")
+    reduced = served_run(budget=scratch + total_charge // 2, session_mean=8,
+                         max_batch=small_batch)
+    progress("served: plain")
+    plain = plain_run()
+    return {
+        "workload": f"served_scenes: {len(wl)} clients, {sum(w.n for w in wl)} particles "
+                    f"({min(w.n for w in wl)}-{max(w.n for w in wl)} per scene), dam breaks "
+                    f"and pools without rigid bodies, r = 0.02, h = 4r, 4 iterations, dt = 1/240, "
+                    f"s_corr k = 0.001 (PBFSettings default)",
+        "arrivals": f"per-client Poisson, mean 512 ms (2 ms aggregate) over {T:.0f} s; "
+                    f"k in {{1, 4, 16}}; {sum(len(p) for p in plans)} requests, "
+                    f"{demand} particle-steps offered",
+        "state_bytes_per_particle": capi.state_bytes_per_particle(),
+        "value": full["value"], "unit": UNIT,
+        "step_ms_p50": full["step_ms_p50"], "step_ms_p99": full["step_ms_p99"],
+        "request_ms_p50": full["request_ms_p50"], "request_ms_p99": full["request_ms_p99"],
+        "speedup_vs_plain": full["value"] / plain["value"],
+        "full_budget": full, "reduced_budget": reduced, "plain": plain,
+    }
+
+
+def run_coupled(args, device):
+    """Two-way rigid-fluid coupling through the drop-in FluidWorld: a
+    250,000-particle pool (50 x 50 x 100 lattice at r = 0.015 centred on the
+    floor of a 2 x 2 x 2 m box), 4 boxes (edge 0.2 m) and 4 spheres (radius
+    0.12 m) of density U(300, 1500) dropped from 0.5-1.0 m above the pool at
+    non-overlapping seeded x-y positions (seed 2), a floor plane; Akinci
+    boundary particles at spacing r; h = 4r, 4 iterations, dt = 1/240, s_corr
+    k = 0.1, XSPH 0.01, vorticity 1e-4.  One step = FluidWorld.step: the PBF
+    step, boundary density, coupling forces and torques reduced per body on
+    the device, the host rigid step.  Timed on the host clock over consecutive
+    steps after warm-up."""
+    import novaphy_gb300 as nv
+
+    rng = np.random.default_rng(2)
+    r = 0.015
+    counts = np.array([50, 50, 100])
+    lower = np.array([(2.0 - 50 * r) / 2, (2.0 - 50 * r) / 2, r / 2], np.float32)
+    upper = lower + (counts - 0.5).astype(np.float32) * np.float32(r)
+    mb = nv.ModelBuilder()
+    mb.add_shape(nv.CollisionShape.make_plane([0.0, 0.0, 1.0], 0.0))
+    placed = []
+    for k in range(8):
+        dens = float(rng.uniform(300.0, 1500.0))
+        while True:
+            xy = rng.uniform(lower[:2] + 0.15, upper[:2] - 0.15)
+            if all(np.linalg.norm(xy - q) > 0.3 for q in placed):
+                break
+        placed.append(xy)
+        z = float(upper[2] + rng.uniform(0.5, 1.0))
+        t = nv.Transform.from_translation([float(xy[0]), float(xy[1]), z])
+        if k < 4:
+            bi = mb.add_body(nv.RigidBody.from_box(dens * 0.2 ** 3, [0.1, 0.1, 0.1]), t)
+            mb.add_shape(nv.CollisionShape.make_box([0.1, 0.1, 0.1], bi))
+        else:
+            rad = 0.12
+            bi = mb.add_body(nv.RigidBody.from_sphere(dens * 4.0 / 3.0 * np.pi * rad ** 3, rad), t)
+            mb.add_shape(nv.CollisionShape.make_sphere(rad, bi))
+    model = mb.build()
+    blk = nv.FluidBlockDef()
+    blk.lower = lower.tolist()
+    blk.upper = upper.tolist()
+    blk.particle_spacing = r
+    st = nv.PBFSettings()
+    st.kernel_radius = float(np.float32(4 * r))
+    st.particle_radius = float(np.float32(r / 2))
+    st.solver_iterations = 4
+    st.corr_k = 0.1
+    st.corr_delta_q = 0.2
+    st.xsph_viscosity = 0.01
+    st.vorticity_epsilon = 1e-4
+    st.use_domain_bounds = True
+    st.domain_lower = [0.0, 0.0, 0.0]
+    st.domain_upper = [2.0, 2.0, 2.0]
+    world = nv.FluidWorld(model, [blk], nv.SolverSettings(), st, 1.0)
+    world.set_gravity([0.0, 0.0, -9.81])
+    dt = float(np.float32(1.0 / 240.0))
+    for _ in range(2):
+        world.step(dt)
+    k = max(1, args.coupled_steps)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        world.step(dt)
+    el = time.perf_counter() - t0
+    n, nb = world.num_particles, world.num_boundary_particles
+    return {"workload": f"coupled pool: {n} fluid + {nb} boundary particles, 8 bodies "
+                        f"(4 boxes, 4 spheres) and a floor plane, r = 0.015, h = 4r, "
+                        f"4 iterations, dt = 1/240",
+            "value": n * k / el, "unit": UNIT, "steps": k, "ms_per_step": el * 1e3 / k,
+            "fluid_particles": n, "boundary_particles": nb,
+            "step": "FluidWorld.step: PBF step, boundary density, coupling forces/torques "
+                    "(device, per-body serial reduction), host rigid step",
+            "timing": "host clock over consecutive steps after 2 warm-up steps"}
+
+
+# FP32 (non-tensor) issue peak of a GB300: 152 SMs x 128 FP32 lanes x 2 FLOP
+# (fused multiply-add) x 2.07 GHz.  Nominal: no measured FP32 peak exists.
+FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
+def fp32_roof(particle_steps_per_s, iters, candidates=1728, neighbours=250):
+    """Second roof: algorithmic FP32 work of a particle-step at h = 4r.  Every
+    candidate of the 27 cells is tested in each of the 2I + 3 neighbour passes
+    (3 subtractions + 5 for the squared norm = 8 FLOP), and each of the ~250
+    neighbours costs density+lambda 30, delta+s_corr 40 (per iteration), XSPH
+    20, omega 22 and confinement 20 FLOP."""
+    passes = 2 * iters + 3
+    flop = 8 * candidates * passes + neighbours * (70 * iters + 62)
+    achieved = particle_steps_per_s * flop / 1e12
+    return {"achieved": achieved, "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
+            "frac": achieved / FP32_PEAK_TFLOPS_NOMINAL, "flop_per_particle_step": flop,
+            "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)"}
+
+
 def run_ours(args, ws, rank, local):
     from novaphy_gb300 import capi
 
@@ -314,6 +588,7 @@ def run_ours(args, ws, rank, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    progress("single scene: warm-up")
     sc.replay_timed(seed, w.dt, max(args.warmup, 1))  # warm-up (captures the step graph)
     barrier()
     with ClockSampler(device) as clk:
@@ -343,8 +618,10 @@ def run_ours(args, ws, rank, local):
     roofline = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "alg_bytes_per_launch": alg, "launch_ms": launch_ms,
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"}
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "fp32": fp32_roof(value / ws, iters)}
 
+    progress("single scene: fast build")
     # The FMA build on the same batch.
     fast = None
     if not args.no_fast:
@@ -370,6 +647,7 @@ def run_ours(args, ws, rank, local):
                        "note": "steps 1..k of the seeded dam break; the configured s_corr "
                                "makes it explode and cells overfill"}
 
+    progress("single scene: end to end")
     # End to end through the host-array drop-in call.
     e2e = None
     if not args.no_e2e:
@@ -420,10 +698,20 @@ def run_ours(args, ws, rank, local):
 
     batched = None
     if not args.no_batched:
+        progress("batched scenes")
         batched = run_batched(args, device)
+    coupled = None
+    if not args.no_coupled:
+        progress("coupled scene")
+        coupled = run_coupled(args, device)
+    served = None
+    if not args.no_served:
+        progress("served scenes")
+        served = run_served(args, device)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        progress("cpu baseline")
         counts = (50, 50, 50)
         val, kind, n, el = time_cpu(counts, 1, 0)
         cpu = {"value": val, "unit": UNIT, "cores": 1, "kind": kind,
@@ -453,6 +741,8 @@ def run_ours(args, ws, rank, local):
             "fast": fast,
             "consecutive": consecutive,
             "batched": batched,
+            "served": served,
+            "coupled": coupled,
             "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         }
         print(json.dumps(line), flush=True)
@@ -463,7 +753,12 @@ def run_ours(args, ws, rank, local):
     return 0
 
 
+def progress(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def main():
+    faulthandler.enable()
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -477,6 +772,10 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-scenes", type=int, default=1024)
     ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-coupled", action="store_true")
+    ap.add_argument("--coupled-steps", type=int, default=10)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

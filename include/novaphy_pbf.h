@@ -271,6 +271,11 @@ int pbf_batch_replay_timed(pbf_batch* batch, int nscenes, pbf_scene* const* scen
 /* Waits for the batch's stream and checks its device status word. */
 int pbf_batch_sync(pbf_batch* batch);
 
+/* After a pbf_batch_step of nscenes scenes: out[k] = 1 when a step of
+ * scenes[k] committed a non-finite position or velocity, else 0 (waits for
+ * the batch).  nscenes must equal the last call's. */
+int pbf_batch_nonfinite(pbf_batch* batch, int nscenes, int* out);
+
 /* Device bytes held: by a batch's scratch, and by a scene's resident state
  * plus whatever scratch its own steps have allocated. */
 int pbf_batch_device_bytes(const pbf_batch* batch, size_t* out);
@@ -279,6 +284,93 @@ int pbf_scene_device_bytes(const pbf_scene* scene, size_t* out);
 /* Device bytes per particle of a scene's resident state (x, v, rho, lambda
  * and a staging buffer), the figure an admission budget counts. */
 size_t pbf_state_bytes_per_particle(void);
+
+
+/* ---- Serving loop -------------------------------------------------------
+ * No counterpart in the reference (it has no server; each FluidWorld is
+ * stepped by its owner, src/fluid/fluid_world.cpp:49).  A server keeps
+ * scenes resident on one device and steps them for many clients.  Requests
+ * (k steps of one scene, from any thread) are coalesced into batch launches
+ * by the server's scheduler, which owns the batch stream: continuous batching,
+ * so a request that arrives while launches are in flight joins the next
+ * launch, and each scene's steps run in request order.  Scenes are admitted
+ * against an HBM budget (resident state plus a grid share, and the batch
+ * scratch reserved at creation); a scene that does not fit waits in a FIFO
+ * until memory frees up, and one that can never fit is rejected.  A step
+ * that commits a non-finite position or velocity fails its scene (its
+ * requests fail with PBF_ERR_NONFINITE; a launch that fails fails its
+ * scenes with the launch's status); the other scenes are unaffected.
+ * A scene's results do not depend on what it was batched with. */
+typedef struct pbf_server pbf_server;
+
+typedef struct pbf_server_config {
+    size_t hbm_budget_bytes; /* scenes' charged bytes + batch scratch */
+    int max_batch_particles; /* particles per launch (the scratch is sized for it) */
+    int max_batch_scenes;    /* scenes per launch */
+    int max_inflight;        /* launches queued on the GPU ahead of completion, >= 1 */
+} pbf_server_config;
+
+enum pbf_scene_state {
+    PBF_SCENE_WAITING = 0,  /* queued for admission */
+    PBF_SCENE_RESIDENT = 1, /* on the device, served */
+    PBF_SCENE_FAILED = 2    /* a step went non-finite; requests fail */
+};
+
+enum pbf_request_state { PBF_REQ_PENDING = 0, PBF_REQ_DONE = 1, PBF_REQ_FAILED = 2 };
+
+typedef struct pbf_server_stats {
+    long long scenes_resident, scenes_waiting, scenes_rejected, scenes_failed;
+    long long requests_submitted, requests_done, requests_failed;
+    long long steps_done;     /* scene-steps completed */
+    long long particle_steps; /* particles x steps completed */
+    long long launches;       /* batch launches */
+    long long queue_depth;    /* requests submitted and not finished */
+    /* Step latency: from the later of a request's submission and its
+     * previous step's completion to this step's completion.  Request
+     * latency: submission to last step's completion.  Host clock, ms. */
+    double step_ms_p50, step_ms_p99;
+    double request_ms_p50, request_ms_p99;
+    double particle_steps_per_s; /* first submission to last completion */
+    double mean_launch_scenes, mean_launch_particles;
+    size_t hbm_bytes_charged;       /* admitted scenes */
+    size_t hbm_bytes_scratch;       /* batch scratch */
+    size_t state_bytes_per_particle; /* resident bytes charged per particle */
+    size_t grid_bytes_per_slot;      /* bytes charged per cell slot of a scene's grid */
+    double issue_ms_mean;            /* host time to issue one launch */
+    long long graph_captures;        /* step graphs captured (new launch shapes) */
+    long long graph_updates;         /* ... applied to the instantiated graph in place */
+    long long graph_instantiations;  /* ... instantiated anew */
+} pbf_server_stats;
+
+/* Defaults: 120 GB budget, 16M particles and 1024 scenes per launch, 2
+ * launches in flight. */
+int pbf_server_default_config(pbf_server_config* out);
+int pbf_server_create(int device, const pbf_server_config* config, pbf_server** out);
+/* Stops the scheduler after the launches in flight, frees every scene. */
+int pbf_server_destroy(pbf_server* server);
+
+/* Opens a scene (state copied from the host arrays; gravity3 may be NULL for
+ * the World default).  *state_out (may be NULL) is PBF_SCENE_RESIDENT or
+ * PBF_SCENE_WAITING.  PBF_ERR_CAPACITY when the scene can never fit. */
+int pbf_server_open_scene(pbf_server* server, const pbf_settings* settings, int n,
+                          const float* x3, const float* v3, float mass, const float* gravity3,
+                          long long* scene_id, int* state_out);
+/* Waits for the scene's requests, then frees it and admits waiting scenes. */
+int pbf_server_close_scene(pbf_server* server, long long scene_id);
+/* Queues nsteps steps of the scene with time step dt; returns at once. */
+int pbf_server_submit(pbf_server* server, long long scene_id, float dt, int nsteps,
+                      long long* request_id);
+/* Waits up to timeout_s seconds (< 0: no limit) for a request; *state_out is
+ * its pbf_request_state.  PBF_ERR_TIMEOUT if still pending; a failed request
+ * returns its failure status, with the reason in pbf_last_error(). */
+int pbf_server_wait(pbf_server* server, long long request_id, double timeout_s, int* state_out);
+/* Waits until the scene has no pending request, then reads a field
+ * (pbf_scene_read layout). */
+int pbf_server_read(pbf_server* server, long long scene_id, int field, float* host_out);
+int pbf_server_scene_state(pbf_server* server, long long scene_id, int* state_out);
+int pbf_server_get_stats(pbf_server* server, pbf_server_stats* out);
+/* Clears latency samples and counters of completed work. */
+int pbf_server_reset_stats(pbf_server* server);
 
 #ifdef __cplusplus
 }

@@ -40,7 +40,7 @@ CU_FLAGS = {
     "pbf_boundary.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
 }
 CU_SOURCES = ["radix_sort.cu", "pbf_exact.cu", "pbf_fast.cu", "pbf_boundary.cu", "pbf_capi.cu",
-              "pbf_batch.cu", "pbf_noalloc.cu"]
+              "pbf_batch.cu", "pbf_serve.cu", "pbf_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -128,6 +128,18 @@ def load() -> C.CDLL:
         "pbf_batch_device_bytes": ([vp, C.POINTER(C.c_size_t)], C.c_int),
         "pbf_scene_device_bytes": ([vp, C.POINTER(C.c_size_t)], C.c_int),
         "pbf_state_bytes_per_particle": ([], C.c_size_t),
+        "pbf_batch_nonfinite": ([vp, C.c_int, vp], C.c_int),
+        "pbf_server_default_config": ([vp], C.c_int),
+        "pbf_server_create": ([C.c_int, vp, vp], C.c_int),
+        "pbf_server_destroy": ([vp], C.c_int),
+        "pbf_server_open_scene": ([vp, vp, C.c_int, vp, vp, C.c_float, vp, vp, vp], C.c_int),
+        "pbf_server_close_scene": ([vp, C.c_longlong], C.c_int),
+        "pbf_server_submit": ([vp, C.c_longlong, C.c_float, C.c_int, vp], C.c_int),
+        "pbf_server_wait": ([vp, C.c_longlong, C.c_double, vp], C.c_int),
+        "pbf_server_read": ([vp, C.c_longlong, C.c_int, vp], C.c_int),
+        "pbf_server_scene_state": ([vp, C.c_longlong, vp], C.c_int),
+        "pbf_server_get_stats": ([vp, vp], C.c_int),
+        "pbf_server_reset_stats": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -430,6 +442,123 @@ class Batch:
         out = C.c_size_t(0)
         check(self._L.pbf_batch_device_bytes(self._h, C.byref(out)))
         return int(out.value)
+
+    def nonfinite(self, nscenes: int) -> np.ndarray:
+        out = np.zeros(max(nscenes, 1), np.int32)
+        check(self._L.pbf_batch_nonfinite(self._h, nscenes, _ptr(out)))
+        return out[:nscenes]
+
+
+SCENE_WAITING, SCENE_RESIDENT, SCENE_FAILED = 0, 1, 2
+REQ_PENDING, REQ_DONE, REQ_FAILED = 0, 1, 2
+
+
+class ServerConfig(C.Structure):
+    """pbf_server_config."""
+
+    _fields_ = [
+        ("hbm_budget_bytes", C.c_size_t),
+        ("max_batch_particles", C.c_int),
+        ("max_batch_scenes", C.c_int),
+        ("max_inflight", C.c_int),
+    ]
+
+
+class ServerStats(C.Structure):
+    """pbf_server_stats."""
+
+    _fields_ = [
+        ("scenes_resident", C.c_longlong), ("scenes_waiting", C.c_longlong),
+        ("scenes_rejected", C.c_longlong), ("scenes_failed", C.c_longlong),
+        ("requests_submitted", C.c_longlong), ("requests_done", C.c_longlong),
+        ("requests_failed", C.c_longlong), ("steps_done", C.c_longlong),
+        ("particle_steps", C.c_longlong), ("launches", C.c_longlong),
+        ("queue_depth", C.c_longlong),
+        ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
+        ("request_ms_p50", C.c_double), ("request_ms_p99", C.c_double),
+        ("particle_steps_per_s", C.c_double),
+        ("mean_launch_scenes", C.c_double), ("mean_launch_particles", C.c_double),
+        ("hbm_bytes_charged", C.c_size_t), ("hbm_bytes_scratch", C.c_size_t),
+        ("state_bytes_per_particle", C.c_size_t), ("grid_bytes_per_slot", C.c_size_t),
+        ("issue_ms_mean", C.c_double), ("graph_captures", C.c_longlong),
+        ("graph_updates", C.c_longlong), ("graph_instantiations", C.c_longlong),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def server_config(**kw) -> ServerConfig:
+    c = ServerConfig()
+    check(load().pbf_server_default_config(C.byref(c)))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Server:
+    """The serving loop (pbf_server*): device-resident scenes, continuous batching."""
+
+    def __init__(self, config: ServerConfig | None = None, device: int = 0):
+        self._L = load()
+        cfg = config if config is not None else server_config()
+        h = C.c_void_p()
+        check(self._L.pbf_server_create(device, C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._L.pbf_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def open_scene(self, settings: Settings, x, v=None, mass: float = 0.0, gravity=None):
+        x = _f32(x, (-1, 3))
+        vv = _f32(v, x.shape) if v is not None else None
+        g = _f32(gravity, (3,)) if gravity is not None else None
+        sid, st = C.c_longlong(0), C.c_int(0)
+        check(self._L.pbf_server_open_scene(self._h, C.byref(settings), len(x), _ptr(x),
+                                            _ptr(vv) if vv is not None else None, mass,
+                                            _ptr(g) if g is not None else None, C.byref(sid),
+                                            C.byref(st)))
+        return sid.value, st.value
+
+    def close_scene(self, sid: int):
+        check(self._L.pbf_server_close_scene(self._h, sid))
+
+    def submit(self, sid: int, dt: float, nsteps: int) -> int:
+        rid = C.c_longlong(0)
+        check(self._L.pbf_server_submit(self._h, sid, dt, nsteps, C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = -1.0) -> int:
+        st = C.c_int(0)
+        check(self._L.pbf_server_wait(self._h, rid, timeout, C.byref(st)))
+        return st.value
+
+    def read(self, sid: int, field: int, n: int) -> np.ndarray:
+        shape = (n, 3) if field in (FIELD_POSITIONS, FIELD_VELOCITIES) else (n,)
+        out = np.zeros(shape, np.float32)
+        check(self._L.pbf_server_read(self._h, sid, field, _ptr(out)))
+        return out
+
+    def scene_state(self, sid: int) -> int:
+        st = C.c_int(0)
+        check(self._L.pbf_server_scene_state(self._h, sid, C.byref(st)))
+        return st.value
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(self._L.pbf_server_get_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def reset_stats(self):
+        check(self._L.pbf_server_reset_stats(self._h))
 
 
 class Snapshot:

@@ -49,6 +49,8 @@ int bits_for(unsigned long long v) {
 
 struct pbf_batch {
     int device = 0;
+    // Private to the batch: only calls holding `mu` enqueue work on it, so a
+    // graph capture on it records the step's work and nothing else.
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     std::mutex mu;
@@ -69,10 +71,21 @@ struct pbf_batch {
     int tab_cap = 0;  // scenes
     void* tmem = nullptr;  // per-scene tables: StepConsts | StateRef | firsts
     size_t tab_refs_at = 0, tab_firsts_at = 0, tab_bytes = 0;
-    std::vector<char> h_tab;
+    // Pinned host copies of the tables, used in turn; each one's event marks
+    // the end of its upload, so it is rewritten only after the copy is done.
+    static constexpr int kTabRing = 4;
+    char* h_tab[kTabRing] = {};
+    cudaEvent_t h_tab_ev[kTabRing] = {};
+    bool h_tab_used[kTabRing] = {};
+    int h_tab_next = 0;
+
+    uint32_t* d_bad = nullptr;  // per-scene non-finite flags of the last call
+    int bad_cap = 0;
+    int bad_count = 0;
 
     cudaGraphExec_t graph = nullptr;
     GraphKey key{};
+    long long captures = 0, updates = 0, instantiations = 0;
 };
 
 namespace {
@@ -134,19 +147,48 @@ int ensure_slots(pbf_batch* b, uint32_t nslots) {
     return PBF_OK;
 }
 
+void free_tables(pbf_batch* b) {
+    if (b->tmem) cudaFree(b->tmem);
+    b->tmem = nullptr;
+    for (int k = 0; k < pbf_batch::kTabRing; ++k) {
+        if (b->h_tab_ev[k]) {
+            cudaEventSynchronize(b->h_tab_ev[k]);
+            cudaEventDestroy(b->h_tab_ev[k]);
+        }
+        if (b->h_tab[k]) cudaFreeHost(b->h_tab[k]);
+        b->h_tab[k] = nullptr;
+        b->h_tab_ev[k] = nullptr;
+        b->h_tab_used[k] = false;
+    }
+    b->tab_cap = 0;
+}
+
 int ensure_tables(pbf_batch* b, int nscenes) {
     if (b->tmem && b->tab_cap >= nscenes) return PBF_OK;
     drop_graph(b);
-    if (b->tmem) cudaFree(b->tmem);
-    b->tmem = nullptr;
-    b->tab_cap = 0;
+    free_tables(b);
     const int c = std::max(nscenes + nscenes / 4, 64);
     b->tab_refs_at = align_up((size_t)c * sizeof(StepConsts), 256);
     b->tab_firsts_at = b->tab_refs_at + align_up((size_t)c * sizeof(StateRef), 256);
     b->tab_bytes = b->tab_firsts_at + align_up((size_t)(c + 1) * 4, 256);
     PBF_CUDA(cudaMalloc(&b->tmem, b->tab_bytes));
-    b->h_tab.assign(b->tab_bytes, 0);
+    for (int k = 0; k < pbf_batch::kTabRing; ++k) {
+        PBF_CUDA(cudaMallocHost(&b->h_tab[k], b->tab_bytes));
+        PBF_CUDA(cudaEventCreateWithFlags(&b->h_tab_ev[k], cudaEventDisableTiming));
+    }
     b->tab_cap = c;
+    return PBF_OK;
+}
+
+int ensure_bad(pbf_batch* b, int nscenes) {
+    if (b->d_bad && b->bad_cap >= nscenes) return PBF_OK;
+    drop_graph(b);
+    if (b->d_bad) cudaFree(b->d_bad);
+    b->d_bad = nullptr;
+    b->bad_cap = 0;
+    const int c = std::max(nscenes + nscenes / 4, 64);
+    PBF_CUDA(cudaMalloc(&b->d_bad, (size_t)c * 4));
+    b->bad_cap = c;
     return PBF_OK;
 }
 
@@ -158,7 +200,7 @@ bool graphs_enabled() {
 // One step of `list` (scenes with particles, all of one arithmetic build):
 // per-scene tables uploaded, then the batch's launch sequence (from a graph).
 int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vector<float>& dts,
-               int exact, PhaseMarks* pm) {
+               const std::vector<int>& orig, int exact, PhaseMarks* pm) {
     const int ns = (int)list.size();
     if (ns == 0) return PBF_OK;
     unsigned long long n_total = 0, slots_total = 0;
@@ -190,21 +232,25 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
     if (!rc) rc = ensure_tables(b, ns);
     if (rc) return rc;
 
-    char* h = b->h_tab.data();
+    const int ring = b->h_tab_next;
+    b->h_tab_next = (ring + 1) % pbf_batch::kTabRing;
+    if (b->h_tab_used[ring]) PBF_CUDA(cudaEventSynchronize(b->h_tab_ev[ring]));
+    char* h = b->h_tab[ring];
     auto* htab = reinterpret_cast<StepConsts*>(h);
     auto* hrefs = reinterpret_cast<StateRef*>(h + b->tab_refs_at);
     auto* hfirst = reinterpret_cast<uint32_t*>(h + b->tab_firsts_at);
     for (int k = 0; k < ns; ++k) {
         pbf_scene* s = list[k];
         htab[k] = consts[k];
-        hrefs[k] = StateRef{s->B.x, s->B.v, s->B.rho, s->B.lam, consts[k].seg_begin};
+        hrefs[k] = StateRef{s->B.x, s->B.v, s->B.rho, s->B.lam, consts[k].seg_begin,
+                            b->d_bad + orig[k]};
         hfirst[k] = consts[k].seg_begin;
     }
     hfirst[ns] = (uint32_t)n;
-    // Pageable source: the copy is staged before cudaMemcpyAsync returns, so
-    // the host table may be rewritten for the next step right away.
     PBF_CUDA(cudaMemcpyAsync(b->tmem, h, b->tab_firsts_at + (size_t)(ns + 1) * 4,
                              cudaMemcpyHostToDevice, b->stream));
+    PBF_CUDA(cudaEventRecord(b->h_tab_ev[ring], b->stream));
+    b->h_tab_used[ring] = true;
 
     BatchDesc D{};
     D.n = n;
@@ -251,6 +297,7 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
     key.any_plain = any_plain;
     key.xsph_on = xsph_on;
     if (!b->graph || !(key == b->key)) {
+        ++b->captures;
         cudaGraph_t g = nullptr;
         PBF_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         const cudaError_t ee = enqueue(b->stream, nullptr);
@@ -265,6 +312,7 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
             // Same launch topology with new sizes: update the parameters in place.
             cudaGraphExecUpdateResultInfo info{};
             updated = cudaGraphExecUpdate(b->graph, g, &info) == cudaSuccess;
+            if (updated) ++b->updates;
             if (!updated) {
                 cudaGetLastError();
                 cudaGraphExecDestroy(b->graph);
@@ -272,6 +320,7 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
             }
         }
         if (!updated) {
+            ++b->instantiations;
             ce = cudaGraphInstantiate(&b->graph, g, 0);
             if (ce != cudaSuccess) {
                 cudaGraphDestroy(g);
@@ -334,14 +383,21 @@ int run_batch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* 
             return fail(PBF_ERR_INVALID_ARG, "dt must be > 0");
         max_steps = std::max(max_steps, m);
     }
+    int rc = ensure_bad(b, nscenes);
+    if (rc) return rc;
+    b->bad_count = nscenes;
+    if (nscenes > 0) PBF_CUDA(cudaMemsetAsync(b->d_bad, 0, (size_t)nscenes * 4, b->stream));
     std::vector<pbf_scene*> list;
     std::vector<float> dts;
+    std::vector<int> orig;
     list.reserve((size_t)nscenes);
     dts.reserve((size_t)nscenes);
+    orig.reserve((size_t)nscenes);
     for (int step = 0; step < max_steps; ++step) {
         for (int exact = 1; exact >= 0; --exact) {
             list.clear();
             dts.clear();
+            orig.clear();
             for (int k = 0; k < nscenes; ++k) {
                 pbf_scene* s = scenes[k];
                 const int m = nsteps ? nsteps[k] : 1;
@@ -349,8 +405,9 @@ int run_batch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* 
                 if ((s->settings.exact_arithmetic ? 1 : 0) != exact) continue;
                 list.push_back(s);
                 dts.push_back(dt[k]);
+                orig.push_back(k);
             }
-            int rc = step_group(b, list, dts, exact, nullptr);
+            rc = step_group(b, list, dts, orig, exact, nullptr);
             if (rc) return rc;
         }
     }
@@ -378,6 +435,55 @@ int check_args(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float*
 }
 
 }  // namespace
+
+namespace pbf {
+namespace capi {
+
+int batch_launch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
+                 uint32_t* flags_host, cudaEvent_t done_event) {
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    SceneLocks L;
+    int rc = lock_scenes(b, nscenes, scenes, L);
+    if (rc) return rc;
+    rc = wait_for_scenes(b, nscenes, scenes);
+    if (!rc) rc = run_batch(b, nscenes, scenes, dt, nullptr);
+    if (!rc && flags_host && nscenes > 0)
+        rc = cudaMemcpyAsync(flags_host, b->d_bad, (size_t)nscenes * 4, cudaMemcpyDeviceToHost,
+                             b->stream) == cudaSuccess
+                 ? PBF_OK
+                 : fail(PBF_ERR_CUDA, "flags copy");
+    const int rc2 = release_scenes(b, nscenes, scenes);
+    if (!rc && done_event) PBF_CUDA(cudaEventRecord(done_event, b->stream));
+    return rc ? rc : rc2;
+}
+
+void batch_counters(const pbf_batch* b, long long* captures, long long* updates,
+                    long long* instantiations) {
+    *captures = b->captures;
+    *updates = b->updates;
+    *instantiations = b->instantiations;
+}
+
+int batch_reserve(pbf_batch* b, int particles, int scenes) {
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    int rc = ensure_particles(b, particles);
+    if (!rc) rc = ensure_tables(b, scenes);
+    if (!rc) rc = ensure_bad(b, scenes);
+    return rc;
+}
+
+size_t batch_bytes(const pbf_batch* b) {
+    size_t t = 0;
+    if (b->wmem) t += work_bytes(b->cap) + sort_scratch_bytes(b->cap) + extra_bytes(b->cap);
+    if (b->off) t += align_up((size_t)b->off_cap * 4, 256) + align_up(b->off_cap, 256);
+    t += b->tab_bytes + (size_t)b->bad_cap * 4;
+    return t;
+}
+
+}  // namespace capi
+}  // namespace pbf
 
 extern "C" {
 
@@ -409,7 +515,9 @@ int pbf_batch_destroy(pbf_batch* b) {
         DeviceGuard dg(b->device);
         if (b->stream) cudaStreamSynchronize(b->stream);
         drop_graph(b);
-        for (void* m : {b->wmem, b->smem, b->xmem, b->tmem, static_cast<void*>(b->off)})
+        free_tables(b);
+        for (void* m : {b->wmem, b->smem, b->xmem, static_cast<void*>(b->off),
+                        static_cast<void*>(b->d_bad)})
             if (m) cudaFree(m);
         if (b->done) cudaEventDestroy(b->done);
         if (b->stream) cudaStreamDestroy(b->stream);
@@ -512,11 +620,22 @@ int pbf_batch_sync(pbf_batch* b) {
 
 int pbf_batch_device_bytes(const pbf_batch* b, size_t* out) {
     if (!b || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
-    size_t t = 0;
-    if (b->wmem) t += work_bytes(b->cap) + sort_scratch_bytes(b->cap) + extra_bytes(b->cap);
-    if (b->off) t += align_up((size_t)b->off_cap * 4, 256) + align_up(b->off_cap, 256);
-    t += b->tab_bytes;
-    *out = t;
+    *out = batch_bytes(b);
+    return PBF_OK;
+}
+
+int pbf_batch_nonfinite(pbf_batch* b, int nscenes, int* out) {
+    if (!b || (nscenes > 0 && !out)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    if (nscenes != b->bad_count)
+        return fail(PBF_ERR_INVALID_ARG, "nscenes differs from the last batch call");
+    if (nscenes == 0) return PBF_OK;
+    std::vector<uint32_t> h((size_t)nscenes);
+    PBF_CUDA(cudaMemcpyAsync(h.data(), b->d_bad, (size_t)nscenes * 4, cudaMemcpyDeviceToHost,
+                             b->stream));
+    PBF_CUDA(cudaStreamSynchronize(b->stream));
+    for (int k = 0; k < nscenes; ++k) out[k] = h[k] ? 1 : 0;
     return PBF_OK;
 }
 

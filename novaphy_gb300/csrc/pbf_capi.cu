@@ -84,6 +84,46 @@ namespace pbf {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace pbf
 
+namespace pbf {
+namespace capi {
+
+// One stream-ordered memory pool per device for scene state and scratch.
+// Freed blocks stay in the pool (release threshold: never), so opening and
+// closing scenes neither synchronizes the device, as cudaMalloc/cudaFree
+// would, nor hands memory back to the driver between scenes.
+cudaMemPool_t scene_pool(int device) {
+    static std::mutex mu;
+    static std::vector<cudaMemPool_t> pools;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)pools.size() <= device) pools.resize((size_t)device + 1, nullptr);
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return nullptr;
+        unsigned long long keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        pools[device] = pool;
+    }
+    return pools[device];
+}
+
+int pool_alloc(void** p, size_t bytes, int device, cudaStream_t st) {
+    cudaMemPool_t pool = scene_pool(device);
+    if (!pool) return fail(PBF_ERR_CUDA, "cudaMemPoolCreate failed");
+    PBF_CUDA(cudaMallocFromPoolAsync(p, bytes, pool, st));
+    return PBF_OK;
+}
+
+void pool_free(void* p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
+}
+
+}  // namespace capi
+}  // namespace pbf
+
 namespace {
 
 void free_particles(pbf_scene* s) {
@@ -91,8 +131,7 @@ void free_particles(pbf_scene* s) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
     }
-    for (void* m : {s->pmem, s->wmem, s->smem})
-        if (m) cudaFree(m);
+    for (void* m : {s->pmem, s->wmem, s->smem}) pool_free(m, s->stream);
     s->pmem = s->wmem = s->smem = nullptr;
     s->cap = s->work_cap = 0;
     s->sort = SortScratch{};
@@ -111,7 +150,8 @@ int alloc_particles(pbf_scene* s, int cap) {
     const size_t f1 = align_up((size_t)c * 4, 256);
     const size_t f3 = align_up((size_t)c * 12, 256);
     const size_t total = 2 * f4 + 2 * f1 + f3;
-    PBF_CUDA(cudaMalloc(&s->pmem, total));
+    int rc = pool_alloc(&s->pmem, total, s->device, s->stream);
+    if (rc) return rc;
     char* p = reinterpret_cast<char*>(s->pmem);
     s->B.x = reinterpret_cast<float4*>(p);
     s->B.v = reinterpret_cast<float4*>(p + f4);
@@ -130,17 +170,18 @@ int ensure_work(pbf_scene* s) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
     }
-    for (void* m : {s->wmem, s->smem})
-        if (m) cudaFree(m);
+    for (void* m : {s->wmem, s->smem}) pool_free(m, s->stream);
     s->wmem = s->smem = nullptr;
     s->work_cap = 0;
     const int c = s->cap > 0 ? s->cap : 1;
     const size_t wb = work_bytes(c);
-    PBF_CUDA(cudaMalloc(&s->wmem, wb));
+    int rc = pool_alloc(&s->wmem, wb, s->device, s->stream);
+    if (rc) return rc;
     PBF_CUDA(cudaMemsetAsync(s->wmem, 0, wb, s->stream));
     bind_work(s->B, s->wmem, c);
     const size_t sb = sort_scratch_bytes(c);
-    PBF_CUDA(cudaMalloc(&s->smem, sb));
+    rc = pool_alloc(&s->smem, sb, s->device, s->stream);
+    if (rc) return rc;
     PBF_CUDA(cudaMemsetAsync(s->smem, 0, sb, s->stream));
     sort_scratch_bind(s->sort, s->smem, c);
     s->B.err = s->sort.err;
@@ -534,11 +575,12 @@ int pbf_scene_create(int device, const pbf_settings* settings, int n, const floa
     s->device = device;
     s->settings = *settings;
     s->mass = mass;
-    ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    ce = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) {
         delete s;
         return cuda_fail(ce, "cudaStreamCreate");
     }
+    s->stream = s->own_stream;
     rc = set_state(s, n, x3, v3);
     if (rc == PBF_OK) {
         ce = cudaStreamSynchronize(s->stream);
@@ -564,7 +606,10 @@ int pbf_scene_destroy(pbf_scene* s) {
         if (s->off) cudaFree(s->off);
         if (s->d_flag) cudaFree(s->d_flag);
         if (s->ev) cudaEventDestroy(s->ev);
-        if (s->stream) cudaStreamDestroy(s->stream);
+        if (s->own_stream) {
+            cudaStreamSynchronize(s->own_stream);
+            cudaStreamDestroy(s->own_stream);
+        }
     }
     delete s;
     return PBF_OK;
@@ -727,6 +772,13 @@ int restore_on(pbf_scene* s, const pbf_snapshot* snap, cudaStream_t st) {
     PBF_CUDA(cudaMemcpyAsync(s->B.rho, p + n * 32, n * 4, cudaMemcpyDeviceToDevice, st));
     PBF_CUDA(cudaMemcpyAsync(s->B.lam, p + n * 36, n * 4, cudaMemcpyDeviceToDevice, st));
     return PBF_OK;
+}
+
+uint32_t grid_slots_for(const pbf_settings& st, const float* x3, int n) {
+    pbf_scene tmp;
+    tmp.settings = st;
+    if (!st.use_domain_bounds) update_bbox(&tmp, x3, n);
+    return fit_grid(&tmp).nslots;
 }
 
 size_t scene_device_bytes(const pbf_scene* s) {

@@ -91,7 +91,8 @@ inline void bind_work(StepBuffers& B, void* mem, int c) {
 
 struct pbf_scene {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // where the scene's work is ordered
+    cudaStream_t own_stream = nullptr;  // the stream created with the scene
     std::mutex mu;
     pbf_settings settings{};
     float gravity[3] = {0.0f, -9.81f, 0.0f};  // World default (include/novaphy/sim/world.h:157)
@@ -165,10 +166,36 @@ int check_settings(const pbf_settings* st);
 GridDesc fit_grid(const pbf_scene* s);
 // Per-step constants of the scene with time step dt (no allocation).
 int scene_consts(const pbf_scene* s, float dt, StepConsts& C);
+// Stream-ordered allocation of scene buffers from the device's scene pool.
+int pool_alloc(void** p, size_t bytes, int device, cudaStream_t st);
+void pool_free(void* p, cudaStream_t st);
 // Copies a snapshot into the scene on stream `st` (asynchronous).
 int restore_on(pbf_scene* s, const pbf_snapshot* snap, cudaStream_t st);
 // Device bytes the scene holds (state, step scratch, offsets table).
 size_t scene_device_bytes(const pbf_scene* s);
+// Cell slots of the grid a scene with these settings and positions steps on.
+uint32_t grid_slots_for(const pbf_settings& st, const float* x3, int n);
+
+}  // namespace capi
+}  // namespace pbf
+
+struct pbf_batch;
+
+namespace pbf {
+namespace capi {
+
+// One step of each scene (distinct, unlocked by the caller) as one batch
+// launch, asynchronous on the batch's stream.  When flags_host is given
+// (pinned, nscenes words), it receives each scene's non-finite flag once the
+// launch completes; done_event (if given) is recorded after the launch.
+int batch_launch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
+                 uint32_t* flags_host, cudaEvent_t done_event);
+// Step graphs captured, updated in place and instantiated so far.
+void batch_counters(const pbf_batch* b, long long* captures, long long* updates,
+                    long long* instantiations);
+// Grows the batch's scratch for `particles` particles and `scenes` scenes.
+int batch_reserve(pbf_batch* b, int particles, int scenes);
+size_t batch_bytes(const pbf_batch* b);
 
 }  // namespace capi
 }  // namespace pbf

@@ -499,6 +499,9 @@ __device__ __forceinline__ void commit(uint32_t p, float px, float py, float pz,
     uint32_t i = __float_as_uint(sx[p].w);
     if (i >= (uint32_t)n) i = 0;
     const uint32_t l = i - R.first;
+    if (R.bad && !(isfinite(px) && isfinite(py) && isfinite(pz) && isfinite(vx) && isfinite(vy) &&
+                   isfinite(vz)))
+        atomicOr(R.bad, 1u);
     R.x[l] = make_float4(px, py, pz, 0.0f);
     R.v[l] = make_float4(vx, vy, vz, 0.0f);
     R.rho[l] = srho[p];
@@ -693,7 +696,7 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     StepConsts Cs = C;
     Cs.seg_begin = 0;
     Cs.seg_end = (uint32_t)n;
-    const OneScene one{Cs, StateRef{B.x, B.v, B.rho, B.lam, 0u}};
+    const OneScene one{Cs, StateRef{B.x, B.v, B.rho, B.lam, 0u, nullptr}};
     const SceneIds none{nullptr, nullptr};
     cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)C.grid.nslots, st);
     if (e != cudaSuccess) return e;
@@ -768,7 +771,7 @@ inline cudaError_t enqueue_step(const StepBuffers& B, const StepConsts& C, int i
     StepConsts Ci = C;
     Ci.iters = iters;
     return enqueue_passes(B, grid_view(B), n, iters, iters <= 0, C.vort_on != 0, C.vort_on == 0,
-                          C.xsph_on != 0, OneScene{Ci, StateRef{B.x, B.v, B.rho, B.lam, 0u}}, st,
+                          C.xsph_on != 0, OneScene{Ci, StateRef{B.x, B.v, B.rho, B.lam, 0u, nullptr}}, st,
                           pm);
 }
 

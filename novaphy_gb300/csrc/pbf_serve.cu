@@ -1,0 +1,689 @@
+// Serving loop (include/novaphy_pbf.h, "Serving loop"): device-resident
+// scenes stepped for many clients by a scheduler that coalesces pending
+// requests into batch launches on one stream.
+//
+// Scheduling.  Every resident scene has a FIFO of requests; its issuable
+// request is the first one with steps not yet issued.  A launch takes one
+// step of every scene with an issuable request, oldest request first, up to
+// the per-launch particle and scene caps.  Up to max_inflight launches are
+// queued on the batch stream; while they run, the scheduler builds the next
+// one from whatever is pending then (continuous batching), and a scene can
+// be in several queued launches at once because the stream orders them.
+// A second thread waits on the oldest launch's event and retires its steps,
+// which frees its slot for the next launch.
+//
+// Admission.  A scene is charged state_bytes * n + grid_bytes * slots of its
+// grid (the share of the batch's offset table a launch holding it can use).
+// The batch scratch for max_batch_particles is reserved at creation.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "pbf_internal.cuh"
+
+using namespace pbf;
+using namespace pbf::capi;
+
+namespace {
+
+constexpr size_t kGridBytesPerSlot = 5;  // one offset word + one alias byte
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct SceneRec {
+    long long id = 0;
+    pbf_scene* s = nullptr;
+    int state = PBF_SCENE_WAITING;
+    int n = 0;
+    size_t charge = 0;
+    bool busy = false;  // device copy being made or read outside the lock
+    // Host copy while waiting for admission.
+    pbf_settings settings{};
+    std::vector<float> x, v;
+    float mass = 0.0f;
+    float gravity[3] = {0.0f, -9.81f, 0.0f};
+    std::deque<long long> reqs;  // FIFO
+    int inflight = 0;            // steps issued, not completed
+    std::string why;             // why the scene failed
+    int code = PBF_OK;           // and the status its requests fail with
+};
+
+struct ReqRec {
+    long long id = 0, scene = 0;
+    float dt = 0.0f;
+    int nsteps = 0, issued = 0, done = 0;
+    int state = PBF_REQ_PENDING;
+    double t_submit = 0.0, t_prev = 0.0;
+    std::string why;  // why the request failed
+    int code = PBF_OK;
+};
+
+struct Launch {
+    int slot = 0;
+    std::vector<std::pair<long long, long long>> items;  // (scene, request)
+    long long particles = 0;
+};
+
+double pct(std::vector<double> v, double q) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double pos = q / 100.0 * (double)(v.size() - 1);
+    const size_t lo = (size_t)std::floor(pos), hi = std::min(lo + 1, v.size() - 1);
+    return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
+}
+
+}  // namespace
+
+struct pbf_server {
+    int device = 0;
+    pbf_server_config cfg{};
+    pbf_batch* batch = nullptr;
+    size_t scratch = 0;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_retire, cv_done;
+    bool stop = false;
+    std::thread issuer, retirer;
+
+    std::map<long long, SceneRec> scenes;
+    std::deque<long long> admit_queue;
+    std::unordered_map<long long, ReqRec> reqs;
+    long long next_scene = 1, next_req = 1;
+    size_t charged = 0;
+
+    std::deque<Launch> inflight;
+    std::vector<cudaEvent_t> events;
+    uint32_t* flags = nullptr;  // pinned, max_inflight x max_batch_scenes
+    int next_slot = 0;
+
+    // statistics
+    long long rejected = 0, failed_scenes = 0, submitted = 0, done_reqs = 0, failed_reqs = 0;
+    long long steps_done = 0, particle_steps = 0, launches = 0, launch_scenes = 0,
+              launch_particles = 0;
+    double t_first = -1.0, t_last = 0.0;
+    double issue_ms = 0.0;  // host time spent issuing launches
+    std::vector<double> step_ms, req_ms;
+};
+
+namespace {
+
+// Charged bytes of a scene with n particles on a grid of `slots` cells.
+size_t charge_of(int n, uint32_t slots) {
+    return (size_t)n * kStateBytesPerParticle + (size_t)slots * kGridBytesPerSlot;
+}
+
+void fail_request(pbf_server* sv, ReqRec& r, const std::string& why, int code) {
+    if (r.state != PBF_REQ_PENDING) return;
+    r.state = PBF_REQ_FAILED;
+    r.why = why;
+    r.code = code;
+    ++sv->failed_reqs;
+}
+
+// code: PBF_ERR_NONFINITE for a non-finite state, else the failing call's.
+void fail_scene(pbf_server* sv, SceneRec& sc, const std::string& why, int code) {
+    if (sc.state == PBF_SCENE_FAILED) return;
+    sc.state = PBF_SCENE_FAILED;
+    sc.why = why;
+    sc.code = code;
+    ++sv->failed_scenes;
+    for (long long rid : sc.reqs) {
+        auto it = sv->reqs.find(rid);
+        if (it != sv->reqs.end()) fail_request(sv, it->second, "its scene failed: " + why, code);
+    }
+    sc.reqs.clear();
+}
+
+// Marks completed steps of a finished launch; called with the lock held.
+void complete_launch(pbf_server* sv, const Launch& L, double t) {
+    const uint32_t* fl = sv->flags + (size_t)L.slot * sv->cfg.max_batch_scenes;
+    for (size_t k = 0; k < L.items.size(); ++k) {
+        auto sit = sv->scenes.find(L.items[k].first);
+        if (sit == sv->scenes.end()) continue;
+        SceneRec& sc = sit->second;
+        --sc.inflight;
+        if (fl[k])
+            fail_scene(sv, sc, "a step committed a non-finite position or velocity",
+                       PBF_ERR_NONFINITE);
+        auto rit = sv->reqs.find(L.items[k].second);
+        if (rit == sv->reqs.end()) continue;
+        ReqRec& r = rit->second;
+        if (r.state != PBF_REQ_PENDING) continue;
+        ++r.done;
+        ++sv->steps_done;
+        sv->particle_steps += sc.n;
+        sv->step_ms.push_back(t - r.t_prev);
+        r.t_prev = t;
+        sv->t_last = t;
+        if (r.done == r.nsteps) {
+            r.state = PBF_REQ_DONE;
+            ++sv->done_reqs;
+            sv->req_ms.push_back(t - r.t_submit);
+            if (!sc.reqs.empty() && sc.reqs.front() == r.id) sc.reqs.pop_front();
+        }
+    }
+}
+
+// Builds the next launch from issuable requests; called with the lock held.
+bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
+                  std::vector<float>& dts) {
+    struct Cand {
+        double t;
+        SceneRec* sc;
+        ReqRec* r;
+    };
+    std::vector<Cand> cand;
+    for (auto& kv : sv->scenes) {
+        SceneRec& sc = kv.second;
+        if (sc.state != PBF_SCENE_RESIDENT || !sc.s || sc.busy) continue;
+        for (long long rid : sc.reqs) {
+            ReqRec& r = sv->reqs[rid];
+            if (r.state == PBF_REQ_PENDING && r.issued < r.nsteps) {
+                cand.push_back({r.t_submit, &sc, &r});
+                break;
+            }
+        }
+    }
+    if (cand.empty()) return false;
+    std::sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.t < b.t; });
+    L.items.clear();
+    L.particles = 0;
+    ptrs.clear();
+    dts.clear();
+    for (const Cand& c : cand) {
+        if ((int)L.items.size() >= sv->cfg.max_batch_scenes) break;
+        if (!L.items.empty() && L.particles + c.sc->n > sv->cfg.max_batch_particles) continue;
+        L.items.push_back({c.sc->id, c.r->id});
+        L.particles += c.sc->n;
+        ptrs.push_back(c.sc->s);
+        dts.push_back(c.r->dt);
+        ++c.r->issued;
+        ++c.sc->inflight;
+    }
+    return !L.items.empty();
+}
+
+// Issues launches while slots are free and requests are pending.
+void issue_main(pbf_server* sv) {
+    cudaSetDevice(sv->device);
+    std::vector<pbf_scene*> ptrs;
+    std::vector<float> dts;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        if (sv->stop) break;
+        Launch L;
+        if ((int)sv->inflight.size() >= sv->cfg.max_inflight || !build_launch(sv, L, ptrs, dts)) {
+            sv->cv_work.wait(lk);
+            continue;
+        }
+        L.slot = sv->next_slot;
+        sv->next_slot = (sv->next_slot + 1) % sv->cfg.max_inflight;
+        uint32_t* fl = sv->flags + (size_t)L.slot * sv->cfg.max_batch_scenes;
+        lk.unlock();
+        const double t_issue = now_ms();
+        const int rc = batch_launch(sv->batch, (int)ptrs.size(), ptrs.data(), dts.data(), fl,
+                                    sv->events[L.slot]);
+        const double issued = now_ms() - t_issue;
+        lk.lock();
+        sv->issue_ms += issued;
+        ++sv->launches;
+        sv->launch_scenes += (long long)L.items.size();
+        sv->launch_particles += L.particles;
+        if (rc) {
+            // The launch did not run: its scenes cannot be trusted.
+            const std::string why = std::string("a batch launch failed: ") + pbf_last_error();
+            for (auto& it : L.items) {
+                auto sit = sv->scenes.find(it.first);
+                if (sit == sv->scenes.end()) continue;
+                --sit->second.inflight;
+                fail_scene(sv, sit->second, why, rc);
+            }
+            sv->next_slot = L.slot;  // the slot was not used
+            sv->cv_done.notify_all();
+        } else {
+            sv->inflight.push_back(std::move(L));
+            sv->cv_retire.notify_one();
+        }
+    }
+}
+
+// Waits for the oldest launch and retires its steps.
+void retire_main(pbf_server* sv) {
+    cudaSetDevice(sv->device);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        sv->cv_retire.wait(lk, [&] { return !sv->inflight.empty() || sv->stop; });
+        if (sv->inflight.empty()) {
+            if (sv->stop) break;
+            continue;
+        }
+        const int slot = sv->inflight.front().slot;
+        lk.unlock();
+        const cudaError_t e = cudaEventSynchronize(sv->events[slot]);
+        const double t = now_ms();
+        lk.lock();
+        Launch L = std::move(sv->inflight.front());
+        sv->inflight.pop_front();
+        if (e != cudaSuccess) {
+            const std::string why =
+                std::string("a batch launch did not complete: ") + cudaGetErrorString(e);
+            for (auto& it : L.items) {
+                auto sit = sv->scenes.find(it.first);
+                if (sit == sv->scenes.end()) continue;
+                --sit->second.inflight;
+                fail_scene(sv, sit->second, why, PBF_ERR_CUDA);
+            }
+        } else {
+            complete_launch(sv, L, t);
+        }
+        sv->cv_work.notify_one();
+        sv->cv_done.notify_all();
+    }
+}
+
+// Creates the device copy of an admitted scene (outside the lock).
+int materialize(pbf_server* sv, SceneRec& rec) {
+    pbf_scene* s = nullptr;
+    int rc = pbf_scene_create(sv->device, &rec.settings, rec.n, rec.x.data(),
+                              rec.v.empty() ? nullptr : rec.v.data(), rec.mass, &s);
+    if (rc) return rc;
+    rc = pbf_scene_set_gravity(s, rec.gravity);
+    if (rc) {
+        pbf_scene_destroy(s);
+        return rc;
+    }
+    // The scene keeps its own stream: launches order themselves against it
+    // with events, and client threads (reads, closes) never put work on the
+    // batch stream, which the scheduler may be capturing into a graph.
+    rec.s = s;
+    return PBF_OK;
+}
+
+// Admits waiting scenes in FIFO order while they fit; the caller holds the
+// lock, which is released around device allocation.
+void admit_waiting(pbf_server* sv, std::unique_lock<std::mutex>& lk) {
+    while (!sv->admit_queue.empty()) {
+        const long long id = sv->admit_queue.front();
+        auto it = sv->scenes.find(id);
+        if (it == sv->scenes.end()) {
+            sv->admit_queue.pop_front();
+            continue;
+        }
+        SceneRec& rec = it->second;
+        if (sv->charged + rec.charge + sv->scratch > sv->cfg.hbm_budget_bytes) break;
+        sv->admit_queue.pop_front();
+        sv->charged += rec.charge;
+        rec.busy = true;
+        rec.state = PBF_SCENE_RESIDENT;
+        lk.unlock();
+        const int rc = materialize(sv, rec);
+        lk.lock();
+        rec.busy = false;
+        sv->cv_done.notify_all();
+        rec.x.clear();
+        rec.x.shrink_to_fit();
+        rec.v.clear();
+        rec.v.shrink_to_fit();
+        if (rc) fail_scene(sv, rec, std::string("its device copy failed: ") + pbf_last_error(), rc);
+        sv->cv_work.notify_one();
+        sv->cv_done.notify_all();
+    }
+}
+
+int check_server(pbf_server* sv) {
+    if (!sv) return fail(PBF_ERR_INVALID_ARG, "server is NULL");
+    return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbf_server_default_config(pbf_server_config* out) {
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+    out->hbm_budget_bytes = (size_t)120 << 30;
+    out->max_batch_particles = 16 << 20;
+    out->max_batch_scenes = 1024;
+    out->max_inflight = 2;
+    return PBF_OK;
+}
+
+int pbf_server_create(int device, const pbf_server_config* cfg, pbf_server** out) {
+    if (!cfg || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (cfg->max_batch_particles < 1 || cfg->max_batch_scenes < 1 || cfg->max_inflight < 1 ||
+        cfg->max_inflight > 16)
+        return fail(PBF_ERR_INVALID_ARG,
+                    "max_batch_particles, max_batch_scenes >= 1 and max_inflight in [1, 16]");
+    pbf_batch* b = nullptr;
+    int rc = pbf_batch_create(device, &b);
+    if (rc) return rc;
+    std::unique_ptr<pbf_server> sv(new pbf_server());
+    sv->device = device;
+    sv->cfg = *cfg;
+    sv->batch = b;
+    {
+        DeviceGuard dg(device);
+        rc = batch_reserve(b, cfg->max_batch_particles, cfg->max_batch_scenes);
+        if (!rc) {
+            sv->scratch = batch_bytes(b);
+            if (sv->scratch > cfg->hbm_budget_bytes)
+                rc = fail(PBF_ERR_CAPACITY, "the batch scratch alone exceeds the HBM budget");
+        }
+        sv->events.assign((size_t)cfg->max_inflight, nullptr);
+        for (auto& e : sv->events)
+            if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                rc = fail(PBF_ERR_CUDA, "cudaEventCreate");
+        if (!rc && cudaMallocHost(&sv->flags, (size_t)cfg->max_inflight * cfg->max_batch_scenes *
+                                                  sizeof(uint32_t)) != cudaSuccess)
+            rc = fail(PBF_ERR_OOM, "pinned flags");
+    }
+    if (rc) {
+        for (auto e : sv->events)
+            if (e) cudaEventDestroy(e);
+        if (sv->flags) cudaFreeHost(sv->flags);
+        pbf_batch_destroy(b);
+        return rc;
+    }
+    pbf_server* p = sv.release();
+    p->issuer = std::thread(issue_main, p);
+    p->retirer = std::thread(retire_main, p);
+    *out = p;
+    return PBF_OK;
+}
+
+int pbf_server_destroy(pbf_server* sv) {
+    if (!sv) return PBF_OK;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    if (sv->issuer.joinable()) sv->issuer.join();
+    sv->cv_retire.notify_all();  // the retirer drains the launches in flight, then stops
+    if (sv->retirer.joinable()) sv->retirer.join();
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        for (auto& kv : sv->reqs) fail_request(sv, kv.second, "the server stopped", PBF_ERR_INVALID_ARG);
+    }
+    sv->cv_done.notify_all();
+    {
+        DeviceGuard dg(sv->device);
+        for (auto& kv : sv->scenes)
+            if (kv.second.s) pbf_scene_destroy(kv.second.s);
+        sv->scenes.clear();
+        for (auto e : sv->events)
+            if (e) cudaEventDestroy(e);
+        if (sv->flags) cudaFreeHost(sv->flags);
+        pbf_batch_destroy(sv->batch);
+    }
+    delete sv;
+    return PBF_OK;
+}
+
+int pbf_server_open_scene(pbf_server* sv, const pbf_settings* st, int n, const float* x3,
+                          const float* v3, float mass, const float* g3, long long* id_out,
+                          int* state_out) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    if (!st || !id_out || (n > 0 && !x3)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n must be >= 0");
+    rc = check_settings(st);
+    if (rc) return rc;
+    const size_t charge = charge_of(n, grid_slots_for(*st, x3, n));
+    std::unique_lock<std::mutex> lk(sv->mu);
+    if (charge + sv->scratch > sv->cfg.hbm_budget_bytes) {
+        ++sv->rejected;
+        return fail(PBF_ERR_CAPACITY, "the scene can never fit the HBM budget (" +
+                                          std::to_string(charge) + " bytes charged)");
+    }
+    if (n > sv->cfg.max_batch_particles)
+        return fail(PBF_ERR_CAPACITY, "the scene exceeds max_batch_particles");
+    const long long id = sv->next_scene++;
+    SceneRec& rec = sv->scenes[id];
+    rec.id = id;
+    rec.n = n;
+    rec.charge = charge;
+    rec.settings = *st;
+    rec.mass = mass;
+    if (g3)
+        for (int d = 0; d < 3; ++d) rec.gravity[d] = g3[d];
+    rec.x.assign(x3, x3 + (size_t)3 * n);
+    if (v3) rec.v.assign(v3, v3 + (size_t)3 * n);
+    sv->admit_queue.push_back(id);
+    admit_waiting(sv, lk);
+    auto it = sv->scenes.find(id);
+    const int state = it == sv->scenes.end() ? PBF_SCENE_FAILED : it->second.state;
+    *id_out = id;
+    if (state_out) *state_out = state;
+    return PBF_OK;
+}
+
+int pbf_server_close_scene(pbf_server* sv, long long id) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->scenes.find(id);
+    if (it == sv->scenes.end()) return fail(PBF_ERR_INVALID_ARG, "no such scene");
+    // Let queued requests finish (a waiting scene has none running).
+    sv->cv_done.wait(lk, [&] {
+        auto i2 = sv->scenes.find(id);
+        if (i2 == sv->scenes.end()) return true;
+        const SceneRec& sc = i2->second;
+        if (sc.busy) return false;
+        if (sc.state == PBF_SCENE_WAITING) return true;
+        bool pending = false;
+        for (long long rid : sc.reqs) {
+            auto r = sv->reqs.find(rid);
+            if (r != sv->reqs.end() && r->second.state == PBF_REQ_PENDING) pending = true;
+        }
+        return !pending && sc.inflight == 0;
+    });
+    it = sv->scenes.find(id);
+    if (it == sv->scenes.end()) return PBF_OK;
+    SceneRec rec = std::move(it->second);
+    sv->scenes.erase(it);
+    for (long long rid : rec.reqs) {
+        auto r = sv->reqs.find(rid);
+        if (r != sv->reqs.end()) fail_request(sv, r->second, "its scene was closed", PBF_ERR_INVALID_ARG);
+    }
+    if (rec.state == PBF_SCENE_WAITING) {
+        sv->admit_queue.erase(std::remove(sv->admit_queue.begin(), sv->admit_queue.end(), id),
+                              sv->admit_queue.end());
+    } else {
+        sv->charged -= rec.charge;
+    }
+    lk.unlock();
+    if (rec.s) pbf_scene_destroy(rec.s);
+    lk.lock();
+    admit_waiting(sv, lk);
+    sv->cv_done.notify_all();
+    return PBF_OK;
+}
+
+int pbf_server_submit(pbf_server* sv, long long scene, float dt, int nsteps, long long* req_out) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    if (!req_out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(PBF_ERR_INVALID_ARG, "dt must be > 0");
+    if (nsteps < 0) return fail(PBF_ERR_INVALID_ARG, "nsteps must be >= 0");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->scenes.find(scene);
+    if (it == sv->scenes.end()) return fail(PBF_ERR_INVALID_ARG, "no such scene");
+    SceneRec& sc = it->second;
+    if (sc.state == PBF_SCENE_FAILED) return fail(sc.code, "the scene failed: " + sc.why);
+    const double t = now_ms();
+    const long long id = sv->next_req++;
+    ReqRec& r = sv->reqs[id];
+    r.id = id;
+    r.scene = scene;
+    r.dt = dt;
+    r.nsteps = nsteps;
+    r.t_submit = r.t_prev = t;
+    ++sv->submitted;
+    if (sv->t_first < 0.0) sv->t_first = t;
+    if (nsteps == 0 || sc.n == 0) {  // nothing to run (pbf_solver.cpp:21)
+        r.state = PBF_REQ_DONE;
+        ++sv->done_reqs;
+        sv->req_ms.push_back(0.0);
+        sv->cv_done.notify_all();
+    } else {
+        sc.reqs.push_back(id);
+        sv->cv_work.notify_one();
+    }
+    *req_out = id;
+    return PBF_OK;
+}
+
+int pbf_server_wait(pbf_server* sv, long long rid, double timeout_s, int* state_out) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(rid);
+    if (it == sv->reqs.end()) return fail(PBF_ERR_INVALID_ARG, "no such request");
+    auto done = [&] { return sv->reqs[rid].state != PBF_REQ_PENDING; };
+    if (timeout_s < 0.0) {
+        sv->cv_done.wait(lk, done);
+    } else if (!sv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
+        if (state_out) *state_out = PBF_REQ_PENDING;
+        return fail(PBF_ERR_TIMEOUT, "the request is still pending");
+    }
+    const ReqRec& r = sv->reqs[rid];
+    if (state_out) *state_out = r.state;
+    if (r.state == PBF_REQ_FAILED) return fail(r.code, "the request failed: " + r.why);
+    return PBF_OK;
+}
+
+int pbf_server_read(pbf_server* sv, long long id, int field, float* out) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    pbf_scene* s = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(sv->mu);
+        auto idle = [&] {
+            auto i2 = sv->scenes.find(id);
+            if (i2 == sv->scenes.end()) return true;
+            const SceneRec& sc = i2->second;
+            if (sc.busy) return false;
+            for (long long r : sc.reqs)
+                if (sv->reqs[r].state == PBF_REQ_PENDING) return false;
+            return sc.inflight == 0;
+        };
+        sv->cv_done.wait(lk, idle);
+        auto it = sv->scenes.find(id);
+        if (it == sv->scenes.end()) return fail(PBF_ERR_INVALID_ARG, "no such scene");
+        if (it->second.state == PBF_SCENE_WAITING) {
+            // Not on the device yet: the state is the host copy.
+            const SceneRec& sc = it->second;
+            const size_t n = (size_t)sc.n;
+            if (field == PBF_FIELD_POSITIONS) {
+                std::memcpy(out, sc.x.data(), n * 12);
+            } else if (field == PBF_FIELD_VELOCITIES) {
+                if (sc.v.empty()) std::memset(out, 0, n * 12);
+                else std::memcpy(out, sc.v.data(), n * 12);
+            } else if (field == PBF_FIELD_DENSITIES || field == PBF_FIELD_LAMBDAS) {
+                std::memset(out, 0, n * 4);
+            } else {
+                return fail(PBF_ERR_INVALID_ARG, "unknown field");
+            }
+            return PBF_OK;
+        }
+        s = it->second.s;
+        // No launch of this scene is pending; the busy flag keeps new launches
+        // and close_scene away until the read is done.
+        it->second.busy = true;
+    }
+    rc = s ? pbf_scene_read(s, field, out) : fail(PBF_ERR_INVALID_ARG, "scene has no device copy");
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        auto it = sv->scenes.find(id);
+        if (it != sv->scenes.end()) it->second.busy = false;
+    }
+    sv->cv_done.notify_all();
+    return rc;
+}
+
+int pbf_server_scene_state(pbf_server* sv, long long id, int* state_out) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    if (!state_out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->scenes.find(id);
+    if (it == sv->scenes.end()) return fail(PBF_ERR_INVALID_ARG, "no such scene");
+    *state_out = it->second.state;
+    return PBF_OK;
+}
+
+int pbf_server_get_stats(pbf_server* sv, pbf_server_stats* out) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    pbf_server_stats s{};
+    for (auto& kv : sv->scenes) {
+        if (kv.second.state == PBF_SCENE_WAITING) ++s.scenes_waiting;
+        else if (kv.second.state == PBF_SCENE_RESIDENT) ++s.scenes_resident;
+    }
+    s.scenes_rejected = sv->rejected;
+    s.scenes_failed = sv->failed_scenes;
+    s.requests_submitted = sv->submitted;
+    s.requests_done = sv->done_reqs;
+    s.requests_failed = sv->failed_reqs;
+    s.steps_done = sv->steps_done;
+    s.particle_steps = sv->particle_steps;
+    s.launches = sv->launches;
+    s.queue_depth = sv->submitted - sv->done_reqs - sv->failed_reqs;
+    s.step_ms_p50 = pct(sv->step_ms, 50.0);
+    s.step_ms_p99 = pct(sv->step_ms, 99.0);
+    s.request_ms_p50 = pct(sv->req_ms, 50.0);
+    s.request_ms_p99 = pct(sv->req_ms, 99.0);
+    const double span = sv->t_last - sv->t_first;
+    s.particle_steps_per_s = (sv->t_first >= 0.0 && span > 0.0)
+                                 ? (double)sv->particle_steps / (span / 1e3)
+                                 : 0.0;
+    s.mean_launch_scenes = sv->launches ? (double)sv->launch_scenes / sv->launches : 0.0;
+    s.mean_launch_particles = sv->launches ? (double)sv->launch_particles / sv->launches : 0.0;
+    s.hbm_bytes_charged = sv->charged;
+    s.hbm_bytes_scratch = sv->scratch;
+    s.state_bytes_per_particle = kStateBytesPerParticle;
+    s.grid_bytes_per_slot = kGridBytesPerSlot;
+    s.issue_ms_mean = sv->launches ? sv->issue_ms / sv->launches : 0.0;
+    batch_counters(sv->batch, &s.graph_captures, &s.graph_updates, &s.graph_instantiations);
+    *out = s;
+    return PBF_OK;
+}
+
+int pbf_server_reset_stats(pbf_server* sv) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->submitted -= sv->done_reqs + sv->failed_reqs;
+    sv->done_reqs = sv->failed_reqs = 0;
+    sv->steps_done = sv->particle_steps = sv->launches = 0;
+    sv->launch_scenes = sv->launch_particles = 0;
+    sv->issue_ms = 0.0;
+    sv->rejected = 0;
+    sv->t_first = -1.0;
+    sv->t_last = 0.0;
+    sv->step_ms.clear();
+    sv->req_ms.clear();
+    for (auto it = sv->reqs.begin(); it != sv->reqs.end();) {
+        if (it->second.state != PBF_REQ_PENDING) it = sv->reqs.erase(it);
+        else ++it;
+    }
+    return PBF_OK;
+}
+
+}  // extern "C"

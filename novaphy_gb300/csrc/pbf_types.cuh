@@ -132,6 +132,7 @@ struct StateRef {
     float* rho;
     float* lam;
     uint32_t first;
+    uint32_t* bad;  // set to 1 when a committed x or v is not finite (null: no check)
 };
 
 // One step of a batch of independent scenes: particle i of the batch belongs

@@ -113,3 +113,39 @@ def batched_scenes(nscenes=1024, seed=3, n_lo=2000, n_hi=64000, r=0.02, dt=1.0 /
                       name=f"scene_{k}")
         out.append(w)
     return out
+
+
+def served_scenes(nclients=256, seed=4, n_lo=1000, n_hi=200_000, r=0.02, dt=1.0 / 240.0,
+                  vorticity=1e-4) -> list[Workload]:
+    """One scene per client of a serving run, from ``default_rng(seed)``: a
+    target count N = round(exp(U(ln n_lo, ln n_hi))); half dam breaks (a 1:1:2
+    block in the corner of a box 3x its footprint and 1.5x its height), half
+    pools (a 2:2:1 block covering the floor of a box 2x its height).  h = 4r,
+    4 iterations, XSPH 0.01, vorticity 1e-4, and the s_corr defaults of
+    PBFSettings (k = 0.001, dq = 0.3 h, n = 4): served scenes run hundreds of
+    consecutive steps, and with k = 0.1 the fluid collapses into a few
+    overfull cells within ~100 steps."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nclients):
+        target = int(round(float(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))))
+        if rng.uniform() < 0.5:
+            a = max(1, int(round((target / 2.0) ** (1.0 / 3.0))))
+            counts = (a, a, max(1, int(round(target / (a * a)))))
+            ext = np.array(counts, np.float64) * r
+            box = (3.0 * ext[0] + r, 3.0 * ext[1] + r, 1.5 * ext[2] + r)
+            kind = "dam"
+        else:
+            c = max(1, int(round((target / 4.0) ** (1.0 / 3.0))))
+            a = max(1, int(round((target / c) ** 0.5)))
+            counts = (a, a, c)
+            ext = np.array(counts, np.float64) * r
+            box = (ext[0] + r, ext[1] + r, 2.0 * ext[2] + r)
+            kind = "pool"
+        box = tuple(float(np.float32(b)) for b in box)
+        w = dam_break(counts, r, box, iterations=4, dt=dt, jitter=1e-4,
+                      seed=int(rng.integers(0, 2**31)), vorticity=vorticity, steps=16,
+                      name=f"client_{k}_{kind}")
+        w.settings.update(corr_k=0.001, corr_delta_q=0.3)
+        out.append(w)
+    return out

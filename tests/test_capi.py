@@ -1,6 +1,7 @@
 """The C-ABI library loads and exports what include/novaphy_pbf.h declares
 (CPU: no compute calls)."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -52,4 +53,47 @@ def test_no_device_is_reported_not_faked(capi):
     x = np.zeros((4, 3), np.float32)
     with pytest.raises(capi.PbfError) as e:
         capi.Scene(s, x, mass=1.0)
+    assert e.value.code == capi.PBF_ERR_NO_DEVICE
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """sizeof/offsetof of the C ABI structs, from gcc on include/novaphy_pbf.h."""
+    import shutil
+    import subprocess
+
+    from novaphy_gb300 import capi as c
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"pbf_settings": c.Settings, "pbf_server_config": c.ServerConfig,
+               "pbf_server_stats": c.ServerStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "novaphy_pbf.h"',
+             "int main(void) {"]
+    for name, py in structs.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = dict(line.rsplit(" ", 1) for line in subprocess.run(
+        [str(exe)], check=True, capture_output=True, text=True).stdout.splitlines())
+    for name, py in structs.items():
+        assert int(out[name]) == ctypes.sizeof(py), name
+        for f, _ in py._fields_:
+            assert int(out[f"{name}.{f}"]) == getattr(py, f).offset, (name, f)
+
+
+def test_server_defaults_and_no_device(capi):
+    cfg = capi.server_config()
+    assert cfg.hbm_budget_bytes == 120 << 30 and cfg.max_inflight == 2
+    assert capi.state_bytes_per_particle() == 52
+    if capi.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(capi.PbfError) as e:
+        capi.Server(cfg)
     assert e.value.code == capi.PBF_ERR_NO_DEVICE

@@ -1,0 +1,227 @@
+"""The serving loop (pbf_server_*): continuous batching over device-resident
+scenes, HBM-budget admission, failure isolation.
+
+The equality bar: a scene served among others (its requests coalesced into
+batch launches with whatever else is pending, from several client threads)
+ends bit for bit where the same sequence of steps leaves it when stepped
+alone with pbf_scene_step (exact arithmetic, the default).
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from novaphy_gb300 import capi, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def small_scenes(k=6, seed=31, lo=500, hi=4000):
+    return workloads.batched_scenes(nscenes=k, seed=seed, n_lo=lo, n_hi=hi)
+
+
+def settings_of(w, **kw):
+    st = dict(w.settings)
+    st.update(kw)
+    return capi.default_settings(**st)
+
+
+def alone(w, dts):
+    sc = capi.Scene(settings_of(w), w.x, w.v, mass=w.mass)
+    sc.set_gravity(w.gravity)
+    for dt in dts:
+        sc.step(np.float32(dt), 1)
+    out = [sc.read(f) for f in (capi.FIELD_POSITIONS, capi.FIELD_VELOCITIES,
+                                capi.FIELD_DENSITIES, capi.FIELD_LAMBDAS)]
+    sc.close()
+    return out
+
+
+def served(srv, sid, n):
+    return [srv.read(sid, f, n) for f in (capi.FIELD_POSITIONS, capi.FIELD_VELOCITIES,
+                                          capi.FIELD_DENSITIES, capi.FIELD_LAMBDAS)]
+
+
+def same(a, b):
+    return all(np.array_equal(x.view(np.uint32), y.view(np.uint32)) for x, y in zip(a, b))
+
+
+def test_alone_equals_mix_under_concurrent_clients():
+    ws = small_scenes()
+    srv = capi.Server()
+    ids = []
+    for w in ws:
+        sid, st = srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)
+        assert st == capi.SCENE_RESIDENT
+        ids.append(sid)
+    rng = np.random.default_rng(5)
+    plans = [[(float(np.float32(w.dt * rng.choice([1.0, 0.5]))), int(rng.choice([1, 2, 4])))
+              for _ in range(4)] for w in ws]
+
+    def client(k):
+        r = np.random.default_rng(100 + k)
+        reqs = []
+        for dt, m in plans[k]:
+            time.sleep(float(r.uniform(0, 0.01)))
+            reqs.append(srv.submit(ids[k], dt, m))
+        for q in reqs:
+            assert srv.wait(q) == capi.REQ_DONE
+
+    th = [threading.Thread(target=client, args=(k,)) for k in range(len(ws))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    st = srv.stats()
+    assert st["requests_done"] == sum(len(p) for p in plans)
+    assert st["steps_done"] == sum(m for p in plans for _, m in p)
+    for k, w in enumerate(ws):
+        dts = [dt for dt, m in plans[k] for _ in range(m)]
+        assert same(served(srv, ids[k], w.n), alone(w, dts)), k
+    srv.close()
+
+
+def test_requests_are_batched_together():
+    ws = small_scenes(k=4, seed=7)
+    srv = capi.Server()
+    ids = [srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)[0] for w in ws]
+    reqs = [srv.submit(sid, ws[0].dt, 16) for sid in ids]
+    for q in reqs:
+        srv.wait(q)
+    st = srv.stats()
+    assert st["steps_done"] == 64
+    assert st["mean_launch_scenes"] > 1.0, st
+    assert st["launches"] < 64
+    assert 0.0 < st["step_ms_p50"] <= st["step_ms_p99"]
+    assert 0.0 < st["request_ms_p50"] <= st["request_ms_p99"]
+    assert st["particle_steps"] == 16 * sum(w.n for w in ws)
+    srv.close()
+
+
+def test_budget_admission_waits_fifo_and_admits_on_close():
+    ws = small_scenes(k=3, seed=9, lo=2000, hi=3000)
+    probe = capi.Server()
+    charges = []
+    for w in ws:
+        before = probe.stats()["hbm_bytes_charged"]
+        probe.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)
+        charges.append(probe.stats()["hbm_bytes_charged"] - before)
+    scratch = probe.stats()["hbm_bytes_scratch"]
+    probe.close()
+    # The first two fit, the third does not until the first is closed.
+    budget = scratch + max(charges[0] + charges[1], charges[1] + charges[2])
+    srv = capi.Server(capi.server_config(hbm_budget_bytes=budget))
+    a, sa = srv.open_scene(settings_of(ws[0]), ws[0].x, ws[0].v, ws[0].mass, ws[0].gravity)
+    b, sb = srv.open_scene(settings_of(ws[1]), ws[1].x, ws[1].v, ws[1].mass, ws[1].gravity)
+    c, sc = srv.open_scene(settings_of(ws[2]), ws[2].x, ws[2].v, ws[2].mass, ws[2].gravity)
+    assert (sa, sb, sc) == (capi.SCENE_RESIDENT, capi.SCENE_RESIDENT, capi.SCENE_WAITING)
+    assert srv.stats()["scenes_waiting"] == 1
+    q = srv.submit(c, ws[2].dt, 2)  # queued behind admission
+    with pytest.raises(capi.PbfError) as e:
+        srv.wait(q, timeout=0.2)
+    assert e.value.code == capi.PBF_ERR_TIMEOUT
+    srv.close_scene(a)
+    assert srv.wait(q, timeout=30.0) == capi.REQ_DONE
+    assert srv.scene_state(c) == capi.SCENE_RESIDENT
+    assert same(served(srv, c, ws[2].n), alone(ws[2], [ws[2].dt, ws[2].dt]))
+    srv.close()
+
+
+def test_scene_that_never_fits_is_rejected():
+    w = small_scenes(k=1, seed=3)[0]
+    probe = capi.Server()
+    scratch = probe.stats()["hbm_bytes_scratch"]
+    probe.close()
+    srv = capi.Server(capi.server_config(hbm_budget_bytes=scratch + 1000))
+    with pytest.raises(capi.PbfError) as e:
+        srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)
+    assert e.value.code == capi.PBF_ERR_CAPACITY
+    assert srv.stats()["scenes_rejected"] == 1
+    srv.close()
+
+
+def test_nonfinite_scene_fails_alone():
+    ws = small_scenes(k=2, seed=13)
+    srv = capi.Server()
+    bad_x = ws[0].x.copy()
+    bad_x[7] = np.nan
+    a, _ = srv.open_scene(settings_of(ws[0]), bad_x, ws[0].v, ws[0].mass, ws[0].gravity)
+    b, _ = srv.open_scene(settings_of(ws[1]), ws[1].x, ws[1].v, ws[1].mass, ws[1].gravity)
+    qa = srv.submit(a, ws[0].dt, 3)
+    qb = srv.submit(b, ws[1].dt, 3)
+    with pytest.raises(capi.PbfError) as e:
+        srv.wait(qa)
+    assert e.value.code == capi.PBF_ERR_NONFINITE
+    assert srv.wait(qb) == capi.REQ_DONE
+    assert srv.scene_state(a) == capi.SCENE_FAILED
+    with pytest.raises(capi.PbfError) as e:
+        srv.submit(a, ws[0].dt, 1)
+    assert e.value.code == capi.PBF_ERR_NONFINITE
+    assert same(served(srv, b, ws[1].n), alone(ws[1], [ws[1].dt] * 3))
+    st = srv.stats()
+    assert st["scenes_failed"] == 1 and st["requests_failed"] == 1
+    srv.close()
+
+
+def test_close_waits_for_pending_requests():
+    w = small_scenes(k=1, seed=17)[0]
+    srv = capi.Server()
+    sid, _ = srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)
+    qs = [srv.submit(sid, w.dt, 2) for _ in range(3)]
+    srv.close_scene(sid)
+    for q in qs:
+        assert srv.wait(q) == capi.REQ_DONE
+    assert srv.stats()["steps_done"] == 6
+    srv.close()
+
+
+def test_batch_reports_nonfinite_scenes():
+    ws = small_scenes(k=3, seed=19)
+    bad_x = ws[1].x.copy()
+    bad_x[0] = np.nan
+    scenes = []
+    for k, w in enumerate(ws):
+        sc = capi.Scene(settings_of(w), bad_x if k == 1 else w.x, w.v, mass=w.mass)
+        sc.set_gravity(w.gravity)
+        scenes.append(sc)
+    b = capi.Batch()
+    b.step(scenes, ws[0].dt)
+    assert list(b.nonfinite(3)) == [0, 1, 0]
+
+
+def test_reads_and_closes_while_other_scenes_run():
+    """Client threads read and close their scenes while other scenes' launches
+    are queued and being captured; every scene still matches its lone run."""
+    ws = small_scenes(k=8, seed=41, lo=1000, hi=6000)
+    srv = capi.Server()
+    ids = [srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)[0] for w in ws]
+    results = {}
+    errors = []
+
+    def client(k):
+        try:
+            w, sid = ws[k], ids[k]
+            steps = 0
+            for m in (4, 1, 16, 2):
+                srv.wait(srv.submit(sid, w.dt, m))
+                steps += m
+                served(srv, sid, w.n)  # read between requests
+            results[k] = (served(srv, sid, w.n), steps)
+            if k % 2 == 0:
+                srv.close_scene(sid)
+        except Exception as e:  # noqa: BLE001
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=client, args=(k,)) for k in range(len(ws))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    st = srv.stats()
+    assert st["scenes_failed"] == 0 and st["requests_failed"] == 0
+    for k, w in enumerate(ws):
+        got, steps = results[k]
+        assert same(got, alone(w, [w.dt] * steps)), k
+    srv.close()
