@@ -210,6 +210,39 @@ def percentile(xs, q):
     return float(np.percentile(np.asarray(xs, np.float64), q)) if len(xs) else None
 
 
+def _cpu_scene_step(item):
+    """One reference CPU step of one scene from its seeded state (pool worker)."""
+    from oracle.oracle import Port, Settings
+
+    settings, x, v, dt, g, mass = item
+    port = Port()
+    z = np.zeros(len(x), np.float32)
+    t0 = time.perf_counter()
+    port.steps(Settings.make(**settings), x, v, z, z, dt, g, mass, 1)
+    return len(x), time.perf_counter() - t0
+
+
+def cpu_scene_pool(sample):
+    """Reference CPU throughput for independent scenes, one process per host
+    core (spawned), each running one seeded step of a scene of `sample`.
+    Returns particle-steps/s per core (scene-weighted) and that figure times
+    the core count, the aggregate of a host running one scene per core."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    items = [(w.settings, w.x, w.v, w.dt, w.gravity, w.mass) for w in sample]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_cpu_scene_step, items, chunksize=1)
+    n = sum(r[0] for r in res)
+    busy = sum(r[1] for r in res)
+    per_core = n / busy
+    return {"value": per_core * cores, "unit": UNIT, "cores": cores, "kind": "port",
+            "per_core": per_core,
+            "sample": f"one seeded step of each of {len(sample)} scenes of the workload "
+                      f"({n} particles), one spawned process per core; value = per-core "
+                      f"throughput x {cores} cores"}
+
+
 def run_batched(args, device):
     """Independent dam-break scenes of uneven size (workloads.batched_scenes:
     1,024 scenes, 2,000-64,000 particles log-uniform, 2-6 iterations) stepped
@@ -250,6 +283,17 @@ def run_batched(args, device):
     t_batch = time.perf_counter() - t0
     reseed()
     dev_ms = b.replay_timed(scenes, seeds, dts, k)
+    # The same with the Jacobi loop as one persistent cooperative launch.
+    b.set_persistent(True)
+    reseed()
+    b.step(scenes, dts)  # graph with the persistent loop
+    reseed()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        b.step(scenes, dts, sync=False)
+    b.sync()
+    t_persist = time.perf_counter() - t0
+    b.set_persistent(False)
 
     progress("batched: plain arm")
     # Plain per-scene arm.
@@ -267,6 +311,17 @@ def run_batched(args, device):
         sc.sync()
     t_plain = time.perf_counter() - t0
 
+    # Plain per-scene arm, synchronous: each scene's step returns after it is
+    # done, as a loop over worlds calling the drop-in step does.
+    progress("batched: plain synchronous arm")
+    reseed()
+    ks = min(k, 2)
+    t0 = time.perf_counter()
+    for _ in range(ks):
+        for sc, dt in zip(scenes, dts):
+            sc.step(float(dt), 1)
+    t_plain_sync = time.perf_counter() - t0
+
     out = {
         "workload": f"batched_scenes: {len(wl)} dam-break scenes, {total} particles "
                     f"({min(w.n for w in wl)}-{max(w.n for w in wl)} per scene), r = 0.02, "
@@ -275,8 +330,11 @@ def run_batched(args, device):
         "value": total * k / t_batch, "unit": UNIT,
         "plain_value": total * k / t_plain,
         "speedup_vs_plain": t_plain / t_batch,
+        "plain_sync_value": total * ks / t_plain_sync, "plain_sync_steps": ks,
+        "speedup_vs_plain_sync": (t_plain_sync / ks) / (t_batch / k),
         "step_ms_p50": percentile(lat, 50), "step_ms_p99": percentile(lat, 99),
         "seeded_device_value": total * k / (dev_ms / 1e3),
+        "persistent_value": total * k / t_persist,
         "batch_scratch_bytes": b.device_bytes(),
         "timing": "host clock over k consecutive steps from the seeded states, both arms",
     }
@@ -285,6 +343,9 @@ def run_batched(args, device):
         sd.close()
     for sc in scenes:
         sc.close()
+    if not args.no_cpu_baseline:
+        progress("batched: cpu baseline")
+        out["cpu_baseline"] = cpu_scene_pool(wl[:: max(1, len(wl) // (2 * (os.cpu_count() or 1)))])
     return out
 
 
@@ -438,7 +499,10 @@ def run_served(args, device):
                 "request_ms_p99": percentile(lat_req, 99)}
 
     progress("served: full budget")
-    full = served_run()
+    full = served_run(max_batch=args.served_max_batch)
+    if args.served_full_only:
+        return {"value": full["value"], "unit": UNIT, "full_budget": full,
+                "max_batch_particles": args.served_max_batch}
     total_charge = sum(w.n for w in wl) * capi.state_bytes_per_particle()
     small_batch = 1 << 20
     probe = capi.Server(capi.server_config(max_batch_particles=small_batch), device)
@@ -449,6 +513,10 @@ def run_served(args, device):
                          max_batch=small_batch)
     progress("served: plain")
     plain = plain_run()
+    cpu = None
+    if not args.no_cpu_baseline:
+        progress("served: cpu baseline")
+        cpu = cpu_scene_pool(wl[:: max(1, len(wl) // (2 * (os.cpu_count() or 1)))])
     return {
         "workload": f"served_scenes: {len(wl)} clients, {sum(w.n for w in wl)} particles "
                     f"({min(w.n for w in wl)}-{max(w.n for w in wl)} per scene), dam breaks "
@@ -463,6 +531,7 @@ def run_served(args, device):
         "request_ms_p50": full["request_ms_p50"], "request_ms_p99": full["request_ms_p99"],
         "speedup_vs_plain": full["value"] / plain["value"],
         "full_budget": full, "reduced_budget": reduced, "plain": plain,
+        "cpu_baseline": cpu,
     }
 
 
@@ -470,8 +539,9 @@ def run_coupled(args, device):
     """Two-way rigid-fluid coupling through the drop-in FluidWorld: a
     250,000-particle pool (50 x 50 x 100 lattice at r = 0.015 centred on the
     floor of a 2 x 2 x 2 m box), 4 boxes (edge 0.2 m) and 4 spheres (radius
-    0.12 m) of density U(300, 1500) dropped from 0.5-1.0 m above the pool at
-    non-overlapping seeded x-y positions (seed 2), a floor plane; Akinci
+    0.12 m) of density U(300, 1500) dropped from 0.5-1.0 m above the pool, at
+    x-y positions in 8 of the 9 cells of a 3 x 3 grid over the pool (seed 2),
+    a floor plane; Akinci
     boundary particles at spacing r; h = 4r, 4 iterations, dt = 1/240, s_corr
     k = 0.1, XSPH 0.01, vorticity 1e-4.  One step = FluidWorld.step: the PBF
     step, boundary density, coupling forces and torques reduced per body on
@@ -486,14 +556,13 @@ def run_coupled(args, device):
     upper = lower + (counts - 0.5).astype(np.float32) * np.float32(r)
     mb = nv.ModelBuilder()
     mb.add_shape(nv.CollisionShape.make_plane([0.0, 0.0, 1.0], 0.0))
-    placed = []
+    # x-y: 8 of the 9 cells (0.25 m) of a 3 x 3 grid over the pool footprint,
+    # chosen and jittered from the seed, so no two bodies overlap.
+    cells = rng.permutation(9)[:8]
     for k in range(8):
         dens = float(rng.uniform(300.0, 1500.0))
-        while True:
-            xy = rng.uniform(lower[:2] + 0.15, upper[:2] - 0.15)
-            if all(np.linalg.norm(xy - q) > 0.3 for q in placed):
-                break
-        placed.append(xy)
+        cx, cy = divmod(int(cells[k]), 3)
+        xy = lower[:2] + (np.array([cx, cy]) + 0.5) * 0.25 + rng.uniform(-0.005, 0.005, 2)
         z = float(upper[2] + rng.uniform(0.5, 1.0))
         t = nv.Transform.from_translation([float(xy[0]), float(xy[1]), z])
         if k < 4:
@@ -776,6 +845,10 @@ def main():
     ap.add_argument("--no-coupled", action="store_true")
     ap.add_argument("--coupled-steps", type=int, default=10)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--served-max-batch", type=int, default=16 << 20,
+                    help="particles per launch of the full-budget serving run")
+    ap.add_argument("--served-full-only", action="store_true",
+                    help="run only the full-budget serving arm")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

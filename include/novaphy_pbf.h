@@ -268,7 +268,14 @@ int pbf_batch_replay_timed(pbf_batch* batch, int nscenes, pbf_scene* const* scen
                            const pbf_snapshot* const* seeds, const float* dt, int nsteps,
                            float* ms_out);
 
-/* Waits for the batch's stream and checks its device status word. */
+/* on != 0: run the Jacobi iterations of each batch step as one persistent
+ * cooperative launch (a grid sized to stay resident loops over the particles
+ * and meets at a bounded grid barrier after every pass) instead of one launch
+ * per pass.  Results are identical either way.  Off by default. */
+int pbf_batch_set_persistent(pbf_batch* batch, int on);
+
+/* Waits for the batch's stream and checks its device status word (a grid
+ * barrier that gave up is reported as PBF_ERR_TIMEOUT). */
 int pbf_batch_sync(pbf_batch* batch);
 
 /* After a pbf_batch_step of nscenes scenes: out[k] = 1 when a step of

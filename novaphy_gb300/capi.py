@@ -129,6 +129,7 @@ def load() -> C.CDLL:
         "pbf_scene_device_bytes": ([vp, C.POINTER(C.c_size_t)], C.c_int),
         "pbf_state_bytes_per_particle": ([], C.c_size_t),
         "pbf_batch_nonfinite": ([vp, C.c_int, vp], C.c_int),
+        "pbf_batch_set_persistent": ([vp, C.c_int], C.c_int),
         "pbf_server_default_config": ([vp], C.c_int),
         "pbf_server_create": ([C.c_int, vp, vp], C.c_int),
         "pbf_server_destroy": ([vp], C.c_int),
@@ -437,6 +438,9 @@ class Batch:
 
     def sync(self):
         check(self._L.pbf_batch_sync(self._h))
+
+    def set_persistent(self, on: bool = True):
+        check(self._L.pbf_batch_set_persistent(self._h, 1 if on else 0))
 
     def device_bytes(self) -> int:
         out = C.c_size_t(0)

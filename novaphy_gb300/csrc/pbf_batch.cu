@@ -28,11 +28,12 @@ namespace {
 // The launch sequence of a batch step depends on these; a cached graph is
 // reused (with updated kernel parameters) while they stay the same.
 struct GraphKey {
-    int exact = -1, n = 0, nscenes = 0, key_bits = 0, scene_bits = 0, max_iters = 0;
+    int exact = -1, persist = 0, n = 0, nscenes = 0, key_bits = 0, scene_bits = 0, max_iters = 0;
     uint32_t nslots = 0;
     bool any_zero = false, any_vort = false, any_plain = false, xsph_on = false;
     bool operator==(const GraphKey& o) const {
-        return exact == o.exact && n == o.n && nscenes == o.nscenes && key_bits == o.key_bits &&
+        return exact == o.exact && persist == o.persist && n == o.n && nscenes == o.nscenes &&
+               key_bits == o.key_bits &&
                scene_bits == o.scene_bits && max_iters == o.max_iters && nslots == o.nslots &&
                any_zero == o.any_zero && any_vort == o.any_vort && any_plain == o.any_plain &&
                xsph_on == o.xsph_on;
@@ -82,6 +83,11 @@ struct pbf_batch {
     uint32_t* d_bad = nullptr;  // per-scene non-finite flags of the last call
     int bad_cap = 0;
     int bad_count = 0;
+
+    // Persistent Jacobi loop (one cooperative launch per step) when set.
+    bool persistent = false;
+    int persist_blocks[2] = {-1, -1};  // co-resident grid per build (fast, exact)
+    unsigned int* barrier = nullptr;   // grid barrier words
 
     cudaGraphExec_t graph = nullptr;
     GraphKey key{};
@@ -274,6 +280,13 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
     D.itmp = b->itmp;
     D.perm = b->perm;
     D.stmp = b->stmp;
+    D.persist_blocks = 0;
+    D.barrier = b->barrier;
+    if (b->persistent && max_iters > 0) {
+        int& pb = b->persist_blocks[exact];
+        if (pb < 0) pb = exact ? exact_persist_blocks() : fast_persist_blocks();
+        D.persist_blocks = pb;
+    }
 
     auto enqueue = [&](cudaStream_t st, PhaseMarks* marks) {
         return exact ? exact_enqueue_batch(b->B, D, b->sort, st, marks)
@@ -286,6 +299,7 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
     }
     GraphKey key;
     key.exact = exact;
+    key.persist = D.persist_blocks;
     key.n = n;
     key.nscenes = ns;
     key.key_bits = D.key_bits;
@@ -421,7 +435,7 @@ int batch_sync(pbf_batch* b) {
     PBF_CUDA(cudaMemcpy(&err, b->sort.err, 4, cudaMemcpyDeviceToHost));
     if (err) {
         PBF_CUDA(cudaMemset(b->sort.err, 0, 4));
-        return fail(PBF_ERR_TIMEOUT, "device-side wait in a batch sort gave up (error word " +
+        return fail(PBF_ERR_TIMEOUT, "a device-side wait of a batch step gave up (error word " +
                                          std::to_string(err) + ")");
     }
     return PBF_OK;
@@ -501,9 +515,13 @@ int pbf_batch_create(int device, pbf_batch** out) {
     b->device = device;
     PBF_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     ce = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->barrier, 256);
+    if (ce == cudaSuccess) ce = cudaMemset(b->barrier, 0, 256);
     if (ce != cudaSuccess) {
+        if (b->done) cudaEventDestroy(b->done);
+        if (b->barrier) cudaFree(b->barrier);
         cudaStreamDestroy(b->stream);
-        return cuda_fail(ce, "cudaEventCreate");
+        return cuda_fail(ce, "pbf_batch_create");
     }
     *out = b.release();
     return PBF_OK;
@@ -517,7 +535,7 @@ int pbf_batch_destroy(pbf_batch* b) {
         drop_graph(b);
         free_tables(b);
         for (void* m : {b->wmem, b->smem, b->xmem, static_cast<void*>(b->off),
-                        static_cast<void*>(b->d_bad)})
+                        static_cast<void*>(b->d_bad), static_cast<void*>(b->barrier)})
             if (m) cudaFree(m);
         if (b->done) cudaEventDestroy(b->done);
         if (b->stream) cudaStreamDestroy(b->stream);
@@ -609,6 +627,13 @@ int pbf_batch_replay_timed(pbf_batch* b, int nscenes, pbf_scene* const* scenes,
     if (rc2) return rc2;
     if (e != cudaSuccess) return cuda_fail(e, "pbf_batch_replay_timed");
     return batch_sync(b);
+}
+
+int pbf_batch_set_persistent(pbf_batch* b, int on) {
+    if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+    std::lock_guard<std::mutex> lk(b->mu);
+    b->persistent = on != 0;
+    return PBF_OK;
 }
 
 int pbf_batch_sync(pbf_batch* b) {

@@ -18,6 +18,8 @@ cudaError_t exact_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortSc
     return exact::enqueue_batch_step(B, D, sort, st, pm);
 }
 
+int exact_persist_blocks() { return exact::persist_blocks_max(); }
+
 cudaError_t debug_cells(const StepBuffers& B, const StepConsts& C, int* d_cells3,
                         cudaStream_t st) {
     if (C.n <= 0) return cudaSuccess;

@@ -17,4 +17,6 @@ cudaError_t fast_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortScr
     return fast::enqueue_batch_step(B, D, sort, st, pm);
 }
 
+int fast_persist_blocks() { return fast::persist_blocks_max(); }
+
 }  // namespace pbf

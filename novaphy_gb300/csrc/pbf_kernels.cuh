@@ -373,21 +373,30 @@ __device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
     return c;
 }
 
+// Load of a step array that the Jacobi loop rewrites.  Per-pass kernels read
+// it through the read-only cache (nothing writes it during their launch); the
+// persistent loop, whose other blocks rewrite it between its passes, uses
+// plain loads, which its grid barrier orders after those writes.
+template <bool kPersist, class T>
+__device__ __forceinline__ T ld_step(const T* p) {
+    if constexpr (kPersist) return *p;
+    else return __ldg(p);
+}
+
 // compute_density + compute_lambda (pbf_solver.cpp:129-179) in one candidate
-// pass.  Reads x* from xin, writes (x*, lambda) to xout and rho to srho.
-// Scenes whose `iters` are done by iteration `it` are left untouched.
-template <class P>
-__global__ void __launch_bounds__(kBlock)
-k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
-                 int it, int n, const Grid G, const P prm) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)n) return;
+// pass for sorted particle p.  Reads x* from xin, writes (x*, lambda) to xout
+// and rho to srho.  Scenes whose `iters` are done by iteration `it` are left
+// untouched.
+template <bool kPersist, class P>
+__device__ __forceinline__ void density_lambda_at(uint32_t p, const float4* xin, float4* xout,
+                                                  float* __restrict__ srho, int it, const Grid& G,
+                                                  const P& prm) {
     const StepConsts& C = prm.at(G.spid, p);
     if (it >= C.iters) return;
     const float4 xi = xin[p];
     float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        const float4 xj = __ldg(xin + q);
+        const float4 xj = ld_step<kPersist>(xin + q);
         const float rx = xi.x - xj.x;
         const float ry = xi.y - xj.y;
         const float rz = xi.z - xj.z;
@@ -411,6 +420,15 @@ k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, floa
     xout[p] = make_float4(xi.x, xi.y, xi.z, lam);
 }
 
+template <class P>
+__global__ void __launch_bounds__(kBlock)
+k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
+                 int it, int n, const Grid G, const P prm) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)n) return;
+    density_lambda_at<false>(p, xin, xout, srho, it, G, prm);
+}
+
 // Velocity update with speed clamp (pbf_solver.cpp:81-93) for sorted p; w is
 // the XSPH weight m / rho' (pbf_solver.cpp:240-241).
 __device__ __forceinline__ float4 update_velocity(float px, float py, float pz, const float4 x0,
@@ -429,22 +447,20 @@ __device__ __forceinline__ float4 update_velocity(float px, float py, float pz, 
     return make_float4(a, b, c, C.mass / rho_j);
 }
 
-// compute_delta_position + apply_delta (pbf_solver.cpp:181-223, :74-76).
-// Reads (x*, lambda) from xin, writes (x* + dp, lambda_i) to xout; on the
-// scene's last iteration also the updated velocity into sv.
-template <class P>
-__global__ void __launch_bounds__(kBlock)
-k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
-        const float* __restrict__ srho, float4* __restrict__ sv, int it, int n, const Grid G,
-        const P prm) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)n) return;
+// compute_delta_position + apply_delta (pbf_solver.cpp:181-223, :74-76) for
+// sorted particle p.  Reads (x*, lambda) from xin, writes (x* + dp, lambda_i)
+// to xout; on the scene's last iteration also the updated velocity into sv.
+template <bool kPersist, class P>
+__device__ __forceinline__ void delta_at(uint32_t p, const float4* xin, float4* xout,
+                                         const float4* __restrict__ sx,
+                                         const float* __restrict__ srho, float4* __restrict__ sv,
+                                         int it, const Grid& G, const P& prm) {
     const StepConsts& C = prm.at(G.spid, p);
     if (it >= C.iters) return;
     const float4 xi = xin[p];
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        const float4 xj = __ldg(xin + q);
+        const float4 xj = ld_step<kPersist>(xin + q);
         const float rx = xi.x - xj.x;
         const float ry = xi.y - xj.y;
         const float rz = xi.z - xj.z;
@@ -471,6 +487,86 @@ k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4*
     const float pz = xi.z + dz * C.inv_rho0;
     xout[p] = make_float4(px, py, pz, xi.w);
     if (it == C.iters - 1) sv[p] = update_velocity(px, py, pz, sx[p], srho[p], C);
+}
+
+template <class P>
+__global__ void __launch_bounds__(kBlock)
+k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
+        const float* __restrict__ srho, float4* __restrict__ sv, int it, int n, const Grid G,
+        const P prm) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)n) return;
+    delta_at<false>(p, xin, xout, sx, srho, sv, it, G, prm);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent Jacobi loop: all iterations of a step in one cooperative launch.
+// Every thread keeps the same particles (grid stride) in both passes, and the
+// grid meets at a barrier after each pass.
+
+// Grid barrier for a cooperative launch (all blocks resident).  `count` must
+// be 0 when the launch starts.  Every wait is bounded: after kBarrierSpins
+// polls or kBarrierNs of global time a block records bit 4 in *err and the
+// loop returns, so a barrier that cannot complete ends the launch instead of
+// hanging it.
+struct GridSync {
+    unsigned int* count;
+    unsigned int* gen;
+    uint32_t* err;
+};
+
+constexpr uint32_t kBarrierSpins = 1u << 24;
+constexpr unsigned long long kBarrierNs = 10ull * 1000 * 1000 * 1000;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool grid_sync(const GridSync& S) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const unsigned int g = *(volatile unsigned int*)S.gen;
+        __threadfence();  // this block's writes before its arrival
+        if (atomicAdd(S.count, 1u) == gridDim.x - 1u) {
+            atomicExch(S.count, 0u);
+            __threadfence();
+            atomicAdd(S.gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            for (uint32_t k = 0; *(volatile unsigned int*)S.gen == g; ++k) {
+                if (k > kBarrierSpins || global_ns() - t0 > kBarrierNs) {
+                    atomicOr(S.err, 4u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(128);
+            }
+        }
+        __threadfence();  // the other blocks' writes before this block's reads
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kBlock)
+k_iterate(float4* xa, float4* xb, float* __restrict__ srho, const float4* __restrict__ sx,
+          float4* __restrict__ sv, int max_iters, int n, const Grid G, const P prm,
+          const GridSync S) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t p0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int it = 0; it < max_iters; ++it) {
+        for (uint32_t p = p0; p < (uint32_t)n; p += stride)
+            density_lambda_at<true>(p, xa, xb, srho, it, G, prm);
+        if (!grid_sync(S)) return;
+        for (uint32_t p = p0; p < (uint32_t)n; p += stride)
+            delta_at<true>(p, xb, xa, sx, srho, sv, it, G, prm);
+        if (it + 1 < max_iters && !grid_sync(S)) return;
+    }
 }
 
 // Velocity update alone, for scenes with solver_iterations == 0.
@@ -735,13 +831,34 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
 template <class P>
 inline cudaError_t enqueue_passes(const StepBuffers& B, const Grid& G, int n, int max_iters,
                                   bool any_zero_iters, bool any_vort, bool any_plain, bool xsph_on,
-                                  const P prm, cudaStream_t st, PhaseMarks* pm) {
+                                  const P prm, cudaStream_t st, PhaseMarks* pm,
+                                  int persist_blocks = 0, unsigned int* barrier = nullptr) {
     const int nb = grid_of(n, kBlock);
-    for (int it = 0; it < max_iters; ++it) {
-        k_density_lambda<<<nb, kBlock, 0, st>>>(B.xa, B.xb, B.srho, it, n, G, prm);
+    if (persist_blocks > 0 && barrier && max_iters > 0) {
+        // The whole Jacobi loop as one cooperative launch.
+        cudaError_t e = cudaMemsetAsync(barrier, 0, sizeof(unsigned int), st);
+        if (e != cudaSuccess) return e;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)persist_blocks);
+        cfg.blockDim = dim3(kBlock);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, k_iterate<P>, B.xa, B.xb, B.srho,
+                               static_cast<const float4*>(B.sx), B.sv, max_iters, n, G, prm,
+                               GridSync{barrier, barrier + 1, B.err});
+        if (e != cudaSuccess) return e;
         if (pm) pm->mark(kPhaseDensity, 1, st);
-        k_delta<<<nb, kBlock, 0, st>>>(B.xb, B.xa, B.sx, B.srho, B.sv, it, n, G, prm);
-        if (pm) pm->mark(kPhaseDelta, 1, st);
+    } else {
+        for (int it = 0; it < max_iters; ++it) {
+            k_density_lambda<<<nb, kBlock, 0, st>>>(B.xa, B.xb, B.srho, it, n, G, prm);
+            if (pm) pm->mark(kPhaseDensity, 1, st);
+            k_delta<<<nb, kBlock, 0, st>>>(B.xb, B.xa, B.sx, B.srho, B.sv, it, n, G, prm);
+            if (pm) pm->mark(kPhaseDelta, 1, st);
+        }
     }
     if (any_zero_iters) {
         k_velocity<<<nb, kBlock, 0, st>>>(B.xa, B.sx, B.srho, B.sv, n, G, prm);
@@ -852,7 +969,18 @@ inline cudaError_t enqueue_batch_step(const StepBuffers& B, const BatchDesc& D, 
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return enqueue_passes(B, grid_view(B, D.spid), n, D.max_iters, D.any_zero_iters, D.any_vort,
-                          D.any_plain, D.xsph_on, tab, st, pm);
+                          D.any_plain, D.xsph_on, tab, st, pm, D.persist_blocks, D.barrier);
+}
+
+// Blocks of the persistent Jacobi loop that fit on the device at once.
+inline int persist_blocks_max() {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_iterate<SceneTable>, kBlock, 0) !=
+        cudaSuccess)
+        return 0;
+    return sms * per_sm;
 }
 
 }  // namespace PBF_NS

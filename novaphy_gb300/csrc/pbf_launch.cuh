@@ -17,6 +17,9 @@ cudaError_t exact_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortSc
                                 cudaStream_t st, PhaseMarks* pm = nullptr);
 cudaError_t fast_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortScratch& sort,
                                cudaStream_t st, PhaseMarks* pm = nullptr);
+// Largest co-resident grid of the persistent Jacobi loop on the current device.
+int exact_persist_blocks();
+int fast_persist_blocks();
 
 // Parity probes (exact build).
 cudaError_t debug_cells(const StepBuffers& B, const StepConsts& C, int* d_cells3,

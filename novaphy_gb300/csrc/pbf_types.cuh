@@ -156,6 +156,8 @@ struct BatchDesc {
     uint32_t* itmp;            // key-sorted particles before the scene pass
     uint32_t* perm;            // scene-pass permutation
     uint32_t* stmp;            // scenes of the key-sorted particles before the scene pass
+    int persist_blocks;        // > 0: the Jacobi loop as one cooperative launch of this grid
+    unsigned int* barrier;     // its grid barrier (count, generation)
 };
 
 }  // namespace pbf

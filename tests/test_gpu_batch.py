@@ -174,3 +174,34 @@ def test_invalid_batches():
         b.step([sc], w.dt, nsteps=[-1])
     assert e.value.code == capi.PBF_ERR_INVALID_ARG
     b.step([], w.dt)  # nothing to do
+
+
+def test_persistent_loop_equals_per_pass_launches():
+    """The Jacobi loop as one cooperative launch (grid-stride, bounded grid
+    barrier) gives the same bits as one launch per pass, with scenes of
+    different iteration counts (0 to 7) in one batch."""
+    ws, variants = mixed_scenes()
+    alone = [make_scene(w, **kw) for w, kw in zip(ws, variants)]
+    inbatch = [make_scene(w, **kw) for w, kw in zip(ws, variants)]
+    for sc, w in zip(alone, ws):
+        sc.step(w.dt, 3)
+    b = capi.Batch()
+    b.set_persistent(True)
+    for _ in range(3):
+        b.step(inbatch, [w.dt for w in ws])
+    b.sync()
+    for k, (a, c) in enumerate(zip(alone, inbatch)):
+        assert_same(state(a), state(c), f"scene {k} {variants[k]}")
+
+
+def test_persistent_loop_on_a_large_batch():
+    ws = workloads.batched_scenes(nscenes=24, seed=6, n_lo=2000, n_hi=64000)
+    a = [make_scene(w) for w in ws]
+    c = [make_scene(w) for w in ws]
+    b1, b2 = capi.Batch(), capi.Batch()
+    b2.set_persistent(True)
+    b1.step(a, ws[0].dt, nsteps=2)
+    b2.step(c, ws[0].dt, nsteps=2)
+    b2.sync()
+    for k in range(len(ws)):
+        assert_same(state(a[k]), state(c[k]), f"scene {k}")
