@@ -271,10 +271,14 @@ def run_batched(args, device):
             sc.restore(sd)
 
     progress(f"batched: {len(wl)} scenes created")
-    # Batched arm.
+    # Batched arm, autotuned: the warm-up steps try the block sizes and the
+    # persistent loop, the timed steps run the fastest.
     b = capi.Batch(device)
-    reseed()
-    b.step(scenes, dts)  # warm-up: scratch, graph
+    b.set_autotune(True)
+    for _ in range(5):
+        reseed()
+        b.step(scenes, dts)
+    tuning = b.tuning()
     reseed()
     lat = []
     t0 = time.perf_counter()
@@ -284,6 +288,7 @@ def run_batched(args, device):
     reseed()
     dev_ms = b.replay_timed(scenes, seeds, dts, k)
     # The same with the Jacobi loop as one persistent cooperative launch.
+    b.set_autotune(False)
     b.set_persistent(True)
     reseed()
     b.step(scenes, dts)  # graph with the persistent loop
@@ -295,32 +300,35 @@ def run_batched(args, device):
     t_persist = time.perf_counter() - t0
     b.set_persistent(False)
 
-    progress("batched: plain arm")
-    # Plain per-scene arm.
-    reseed()
-    for sc, dt in zip(scenes, dts):  # warm-up: per-scene scratch and graphs
-        sc.step(float(dt), 1, sync=False)
-    for sc in scenes:
-        sc.sync()
-    reseed()
-    t0 = time.perf_counter()
-    for _ in range(k):
-        for sc, dt in zip(scenes, dts):
+    t_plain = t_plain_sync = ks = None
+    if not args.no_batched_plain:
+        # Plain per-scene arm.
+        progress("batched: plain arm")
+        reseed()
+        for sc, dt in zip(scenes, dts):  # warm-up: per-scene scratch and graphs
             sc.step(float(dt), 1, sync=False)
-    for sc in scenes:
-        sc.sync()
-    t_plain = time.perf_counter() - t0
+        for sc in scenes:
+            sc.sync()
+        reseed()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            for sc, dt in zip(scenes, dts):
+                sc.step(float(dt), 1, sync=False)
+        for sc in scenes:
+            sc.sync()
+        t_plain = time.perf_counter() - t0
 
-    # Plain per-scene arm, synchronous: each scene's step returns after it is
-    # done, as a loop over worlds calling the drop-in step does.
-    progress("batched: plain synchronous arm")
-    reseed()
-    ks = min(k, 2)
-    t0 = time.perf_counter()
-    for _ in range(ks):
-        for sc, dt in zip(scenes, dts):
-            sc.step(float(dt), 1)
-    t_plain_sync = time.perf_counter() - t0
+        # Plain per-scene arm, synchronous: each scene's step returns after it is
+        # done, as a loop over worlds calling the drop-in step does.
+        progress("batched: plain synchronous arm")
+        reseed()
+        ks = min(k, 2)
+        t0 = time.perf_counter()
+        for _ in range(ks):
+            for sc, dt in zip(scenes, dts):
+                sc.step(float(dt), 1)
+        t_plain_sync = time.perf_counter() - t0
+
 
     out = {
         "workload": f"batched_scenes: {len(wl)} dam-break scenes, {total} particles "
@@ -328,13 +336,15 @@ def run_batched(args, device):
                     f"h = 4r, 2-6 iterations, dt = 1/120",
         "particles": total, "scenes": len(wl), "steps": k,
         "value": total * k / t_batch, "unit": UNIT,
-        "plain_value": total * k / t_plain,
-        "speedup_vs_plain": t_plain / t_batch,
-        "plain_sync_value": total * ks / t_plain_sync, "plain_sync_steps": ks,
-        "speedup_vs_plain_sync": (t_plain_sync / ks) / (t_batch / k),
+        "plain_value": total * k / t_plain if t_plain else None,
+        "speedup_vs_plain": t_plain / t_batch if t_plain else None,
+        "plain_sync_value": total * ks / t_plain_sync if t_plain_sync else None,
+        "plain_sync_steps": ks,
+        "speedup_vs_plain_sync": (t_plain_sync / ks) / (t_batch / k) if t_plain_sync else None,
         "step_ms_p50": percentile(lat, 50), "step_ms_p99": percentile(lat, 99),
         "seeded_device_value": total * k / (dev_ms / 1e3),
         "persistent_value": total * k / t_persist,
+        "autotuned": {"block": tuning[0], "persistent": bool(tuning[1])},
         "batch_scratch_bytes": b.device_bytes(),
         "timing": "host clock over k consecutive steps from the seeded states, both arms",
     }
@@ -343,7 +353,7 @@ def run_batched(args, device):
         sd.close()
     for sc in scenes:
         sc.close()
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and not args.no_batched_plain:
         progress("batched: cpu baseline")
         out["cpu_baseline"] = cpu_scene_pool(wl[:: max(1, len(wl) // (2 * (os.cpu_count() or 1)))])
     return out
@@ -841,6 +851,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-scenes", type=int, default=1024)
     ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--no-batched-plain", action="store_true",
+                    help="skip the plain per-scene arms and CPU pool of the batched run")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-coupled", action="store_true")
     ap.add_argument("--coupled-steps", type=int, default=10)

@@ -274,6 +274,19 @@ int pbf_batch_replay_timed(pbf_batch* batch, int nscenes, pbf_scene* const* scen
  * per pass.  Results are identical either way.  Off by default. */
 int pbf_batch_set_persistent(pbf_batch* batch, int on);
 
+/* on != 0: autotune each class of batch shape (arithmetic build,
+ * particle-count octave, largest iteration count, vorticity).  The first four
+ * steps of a class each run one choice of {block size of the neighbour passes
+ * 128, 64, 256; persistent Jacobi loop} timed with events on the batch's
+ * stream; later steps use the fastest.  Results are identical under every
+ * choice.  Decisions are appended to a JSON-lines file keyed by GPU name
+ * ($PBF_AUTOTUNE_CACHE, default ~/.cache/novaphy_gb300/autotune.jsonl) and
+ * read back when autotuning is switched on.  Off by default. */
+int pbf_batch_set_autotune(pbf_batch* batch, int on);
+
+/* Block size and persistent flag the batch's last step ran with. */
+int pbf_batch_tuning(const pbf_batch* batch, int* block, int* persistent);
+
 /* Waits for the batch's stream and checks its device status word (a grid
  * barrier that gave up is reported as PBF_ERR_TIMEOUT). */
 int pbf_batch_sync(pbf_batch* batch);

@@ -130,6 +130,8 @@ def load() -> C.CDLL:
         "pbf_state_bytes_per_particle": ([], C.c_size_t),
         "pbf_batch_nonfinite": ([vp, C.c_int, vp], C.c_int),
         "pbf_batch_set_persistent": ([vp, C.c_int], C.c_int),
+        "pbf_batch_set_autotune": ([vp, C.c_int], C.c_int),
+        "pbf_batch_tuning": ([vp, vp, vp], C.c_int),
         "pbf_server_default_config": ([vp], C.c_int),
         "pbf_server_create": ([C.c_int, vp, vp], C.c_int),
         "pbf_server_destroy": ([vp], C.c_int),
@@ -441,6 +443,14 @@ class Batch:
 
     def set_persistent(self, on: bool = True):
         check(self._L.pbf_batch_set_persistent(self._h, 1 if on else 0))
+
+    def set_autotune(self, on: bool = True):
+        check(self._L.pbf_batch_set_autotune(self._h, 1 if on else 0))
+
+    def tuning(self) -> tuple[int, int]:
+        blk, per = C.c_int(0), C.c_int(0)
+        check(self._L.pbf_batch_tuning(self._h, C.byref(blk), C.byref(per)))
+        return blk.value, per.value
 
     def device_bytes(self) -> int:
         out = C.c_size_t(0)

@@ -11,11 +11,18 @@
 // the scene alone: results do not depend on what else is in the batch.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
 #include <memory>
 #include <mutex>
+#include <sstream>
+#include <string>
 #include <vector>
+
+#include <sys/stat.h>
 
 #include "pbf_internal.cuh"
 #include "pbf_launch.cuh"
@@ -28,11 +35,13 @@ namespace {
 // The launch sequence of a batch step depends on these; a cached graph is
 // reused (with updated kernel parameters) while they stay the same.
 struct GraphKey {
-    int exact = -1, persist = 0, n = 0, nscenes = 0, key_bits = 0, scene_bits = 0, max_iters = 0;
+    int exact = -1, persist = 0, block = 0, n = 0, nscenes = 0, key_bits = 0, scene_bits = 0,
+        max_iters = 0;
     uint32_t nslots = 0;
     bool any_zero = false, any_vort = false, any_plain = false, xsph_on = false;
     bool operator==(const GraphKey& o) const {
-        return exact == o.exact && persist == o.persist && n == o.n && nscenes == o.nscenes &&
+        return exact == o.exact && persist == o.persist && block == o.block && n == o.n &&
+               nscenes == o.nscenes &&
                key_bits == o.key_bits &&
                scene_bits == o.scene_bits && max_iters == o.max_iters && nslots == o.nslots &&
                any_zero == o.any_zero && any_vort == o.any_vort && any_plain == o.any_plain &&
@@ -45,6 +54,27 @@ int bits_for(unsigned long long v) {
     while ((1ull << b) < v) ++b;
     return b;
 }
+
+// Autotuning.  A choice is the block size of the neighbour passes and
+// whether the Jacobi loop runs as one persistent launch.  A class of batch
+// shapes tries each choice once, on its next steps, and keeps the fastest.
+struct Choice {
+    int block = 128;
+    int persist = 0;
+};
+
+const Choice kChoices[] = {{128, 0}, {64, 0}, {256, 0}, {128, 1}};
+constexpr int kNumChoices = (int)(sizeof(kChoices) / sizeof(kChoices[0]));
+
+struct TuneState {
+    bool done = false;
+    Choice best;
+    double best_ms = 0.0;
+    int next = 0;              // next choice to try
+    int pending = -1;          // choice whose timing is in flight
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double ms[kNumChoices] = {};
+};
 
 }  // namespace
 
@@ -92,6 +122,13 @@ struct pbf_batch {
     cudaGraphExec_t graph = nullptr;
     GraphKey key{};
     long long captures = 0, updates = 0, instantiations = 0;
+
+    // Autotuner (off by default): per class of batch shape.
+    bool autotune = false;
+    std::string gpu;
+    std::string cache_path;
+    std::map<std::string, TuneState> tune;
+    Choice last{};
 };
 
 namespace {
@@ -203,6 +240,101 @@ bool graphs_enabled() {
     return !(v && v[0] == '1');
 }
 
+// Where tuning decisions are kept: $PBF_AUTOTUNE_CACHE, else
+// ~/.cache/novaphy_gb300/autotune.jsonl.  One JSON object per line.
+std::string cache_file() {
+    if (const char* p = std::getenv("PBF_AUTOTUNE_CACHE")) return p;
+    const char* home = std::getenv("HOME");
+    return std::string(home ? home : ".") + "/.cache/novaphy_gb300/autotune.jsonl";
+}
+
+// Value of "key": in one of our own cache lines (string or number).
+std::string json_field(const std::string& line, const std::string& key) {
+    const std::string k = "\"" + key + "\": ";
+    const size_t at = line.find(k);
+    if (at == std::string::npos) return {};
+    size_t b = at + k.size();
+    if (b < line.size() && line[b] == '"') {
+        const size_t e = line.find('"', b + 1);
+        return e == std::string::npos ? std::string() : line.substr(b + 1, e - b - 1);
+    }
+    size_t e = line.find_first_of(",}", b);
+    return line.substr(b, e == std::string::npos ? std::string::npos : e - b);
+}
+
+void load_tuning(pbf_batch* b) {
+    std::ifstream in(b->cache_path);
+    std::string line;
+    while (std::getline(in, line)) {
+        if (json_field(line, "gpu") != b->gpu) continue;
+        const std::string cls = json_field(line, "class");
+        const std::string block = json_field(line, "block"), persist = json_field(line, "persistent");
+        if (cls.empty() || block.empty() || persist.empty()) continue;
+        TuneState& t = b->tune[cls];
+        t.done = true;
+        t.best.block = std::atoi(block.c_str());
+        t.best.persist = std::atoi(persist.c_str());
+        t.best_ms = std::atof(json_field(line, "ms").c_str());
+    }
+}
+
+void save_tuning(const pbf_batch* b, const std::string& cls, const TuneState& t) {
+    const std::string& path = b->cache_path;
+    const size_t slash = path.find_last_of('/');
+    if (slash != std::string::npos) {
+        // mkdir -p of the cache directory, one level at a time
+        for (size_t at = path.find('/', 1); at != std::string::npos && at <= slash;
+             at = path.find('/', at + 1))
+            (void)mkdir(path.substr(0, at).c_str(), 0755);
+    }
+    std::ofstream out(path, std::ios::app);
+    if (!out) return;  // a cache that cannot be written only costs re-tuning
+    out << "{\"gpu\": \"" << b->gpu << "\", \"class\": \"" << cls << "\", \"block\": "
+        << t.best.block << ", \"persistent\": " << t.best.persist << ", \"ms\": " << t.best_ms
+        << "}\n";
+}
+
+// Class of a batch shape: arithmetic build, particle-count octave, largest
+// iteration count, vorticity on any scene.
+std::string tune_class(int exact, int n, int max_iters, bool any_vort) {
+    std::ostringstream o;
+    o << (exact ? "exact" : "fast") << " n2^" << bits_for((unsigned long long)n) << " it"
+      << max_iters << (any_vort ? " vort" : "");
+    return o.str();
+}
+
+// The choice for this step of class `cls`; collects the timing of the
+// previous trial first.
+Choice pick_choice(pbf_batch* b, const std::string& cls, int* trial) {
+    *trial = -1;
+    TuneState& t = b->tune[cls];
+    if (t.pending >= 0) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(t.e1) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, t.e0, t.e1) == cudaSuccess)
+            t.ms[t.pending] = ms;
+        else
+            t.ms[t.pending] = 1e30;
+        t.pending = -1;
+        if (t.next >= kNumChoices) {
+            int best = 0;
+            for (int k = 1; k < kNumChoices; ++k)
+                if (t.ms[k] < t.ms[best]) best = k;
+            t.done = true;
+            t.best = kChoices[best];
+            t.best_ms = t.ms[best];
+            save_tuning(b, cls, t);
+        }
+    }
+    if (t.done) return t.best;
+    if (!t.e0) {
+        cudaEventCreate(&t.e0);
+        cudaEventCreate(&t.e1);
+    }
+    *trial = t.next++;
+    return kChoices[*trial];
+}
+
 // One step of `list` (scenes with particles, all of one arithmetic build):
 // per-scene tables uploaded, then the batch's launch sequence (from a graph).
 int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vector<float>& dts,
@@ -282,24 +414,41 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
     D.stmp = b->stmp;
     D.persist_blocks = 0;
     D.barrier = b->barrier;
-    if (b->persistent && max_iters > 0) {
+    Choice choice;
+    choice.persist = b->persistent ? 1 : 0;
+    int trial = -1;
+    std::string cls;
+    if (b->autotune && !pm) {
+        cls = tune_class(exact, n, max_iters, any_vort);
+        choice = pick_choice(b, cls, &trial);
+    }
+    D.block = choice.block;
+    if (choice.persist && max_iters > 0) {
         int& pb = b->persist_blocks[exact];
         if (pb < 0) pb = exact ? exact_persist_blocks() : fast_persist_blocks();
         D.persist_blocks = pb;
     }
+    b->last = choice;
+    TuneState* ts = trial >= 0 ? &b->tune[cls] : nullptr;
 
     auto enqueue = [&](cudaStream_t st, PhaseMarks* marks) {
         return exact ? exact_enqueue_batch(b->B, D, b->sort, st, marks)
                      : fast_enqueue_batch(b->B, D, b->sort, st, marks);
     };
     if (pm || !graphs_enabled()) {
+        if (ts) PBF_CUDA(cudaEventRecord(ts->e0, b->stream));
         cudaError_t e = enqueue(b->stream, pm);
         if (e != cudaSuccess) return cuda_fail(e, "batch step");
+        if (ts) {
+            PBF_CUDA(cudaEventRecord(ts->e1, b->stream));
+            ts->pending = trial;
+        }
         return PBF_OK;
     }
     GraphKey key;
     key.exact = exact;
     key.persist = D.persist_blocks;
+    key.block = D.block;
     key.n = n;
     key.nscenes = ns;
     key.key_bits = D.key_bits;
@@ -345,7 +494,12 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
         cudaGraphDestroy(g);
         b->key = key;
     }
+    if (ts) PBF_CUDA(cudaEventRecord(ts->e0, b->stream));
     PBF_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    if (ts) {
+        PBF_CUDA(cudaEventRecord(ts->e1, b->stream));
+        ts->pending = trial;
+    }
     return PBF_OK;
 }
 
@@ -534,6 +688,10 @@ int pbf_batch_destroy(pbf_batch* b) {
         if (b->stream) cudaStreamSynchronize(b->stream);
         drop_graph(b);
         free_tables(b);
+        for (auto& kv : b->tune) {
+            if (kv.second.e0) cudaEventDestroy(kv.second.e0);
+            if (kv.second.e1) cudaEventDestroy(kv.second.e1);
+        }
         for (void* m : {b->wmem, b->smem, b->xmem, static_cast<void*>(b->off),
                         static_cast<void*>(b->d_bad), static_cast<void*>(b->barrier)})
             if (m) cudaFree(m);
@@ -633,6 +791,28 @@ int pbf_batch_set_persistent(pbf_batch* b, int on) {
     if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
     std::lock_guard<std::mutex> lk(b->mu);
     b->persistent = on != 0;
+    return PBF_OK;
+}
+
+int pbf_batch_set_autotune(pbf_batch* b, int on) {
+    if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceGuard dg(b->device);
+    b->autotune = on != 0;
+    if (b->autotune && b->gpu.empty()) {
+        cudaDeviceProp prop{};
+        PBF_CUDA(cudaGetDeviceProperties(&prop, b->device));
+        b->gpu = prop.name;
+        b->cache_path = cache_file();
+        load_tuning(b);
+    }
+    return PBF_OK;
+}
+
+int pbf_batch_tuning(const pbf_batch* b, int* block, int* persistent) {
+    if (!b || !block || !persistent) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    *block = b->last.block;
+    *persistent = b->last.persist;
     return PBF_OK;
 }
 

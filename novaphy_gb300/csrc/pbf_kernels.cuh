@@ -11,6 +11,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "pbf_types.cuh"
 #include "radix_sort.cuh"
@@ -420,8 +421,8 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, const float4* xin,
     xout[p] = make_float4(xi.x, xi.y, xi.z, lam);
 }
 
-template <class P>
-__global__ void __launch_bounds__(kBlock)
+template <int BS, class P>
+__global__ void __launch_bounds__(BS)
 k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
                  int it, int n, const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -489,8 +490,8 @@ __device__ __forceinline__ void delta_at(uint32_t p, const float4* xin, float4* 
     if (it == C.iters - 1) sv[p] = update_velocity(px, py, pz, sx[p], srho[p], C);
 }
 
-template <class P>
-__global__ void __launch_bounds__(kBlock)
+template <int BS, class P>
+__global__ void __launch_bounds__(BS)
 k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
         const float* __restrict__ srho, float4* __restrict__ sv, int it, int n, const Grid G,
         const P prm) {
@@ -570,8 +571,8 @@ k_iterate(float4* xa, float4* xb, float* __restrict__ srho, const float4* __rest
 }
 
 // Velocity update alone, for scenes with solver_iterations == 0.
-template <class P>
-__global__ void __launch_bounds__(kBlock)
+template <int BS, class P>
+__global__ void __launch_bounds__(BS)
 k_velocity(const float4* __restrict__ xin, const float4* __restrict__ sx, const float* __restrict__ srho,
            float4* __restrict__ sv, int n, const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -606,8 +607,8 @@ __device__ __forceinline__ void commit(uint32_t p, float px, float py, float pz,
 
 // apply_xsph_viscosity (pbf_solver.cpp:225-250) + commit, no vorticity.
 // With skip_vort set, scenes with vorticity are left to the vorticity pair.
-template <class P>
-__global__ void __launch_bounds__(kBlock)
+template <int BS, class P>
+__global__ void __launch_bounds__(BS)
 k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, const float4* __restrict__ sx,
               const float* __restrict__ srho, int n, int skip_vort, const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -644,8 +645,8 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
 // Writes the post-XSPH velocity to sv2 and (omega, |omega|) to som, with
 //   omega_i = sum_j (m/rho_j') spiky_grad(x*_i - x*_j) x (v_j - v_i),
 // the SPH curl (Macklin & Mueller 2013, section 5, with its volume factor).
-template <class P>
-__global__ void __launch_bounds__(kBlock)
+template <int BS, class P>
+__global__ void __launch_bounds__(BS)
 k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, float4* __restrict__ sv2,
              float4* __restrict__ som, int n, const Grid G, const P prm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -690,8 +691,8 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
 // Vorticity confinement (Macklin & Mueller 2013, section 5) + commit:
 //   eta_i = sum_j (m/rho_j') (|omega_j| - |omega_i|) spiky_grad(x*_i - x*_j),
 //   N = eta / |eta|,  v += dt * eps * (N x omega_i).
-template <class P>
-__global__ void __launch_bounds__(kBlock)
+template <int BS, class P>
+__global__ void __launch_bounds__(BS)
 k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv,
                    const float4* __restrict__ sv2, const float4* __restrict__ som,
                    const float4* __restrict__ sx, const float* __restrict__ srho, int n,
@@ -828,12 +829,12 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
 // cell-sorted particles for `max_iters` iterations, with constants from `prm`.
 // Scenes with vorticity take the XSPH+omega / vorticity+commit pair
 // (any_vort), the others XSPH+commit (any_plain).
-template <class P>
-inline cudaError_t enqueue_passes(const StepBuffers& B, const Grid& G, int n, int max_iters,
-                                  bool any_zero_iters, bool any_vort, bool any_plain, bool xsph_on,
-                                  const P prm, cudaStream_t st, PhaseMarks* pm,
-                                  int persist_blocks = 0, unsigned int* barrier = nullptr) {
-    const int nb = grid_of(n, kBlock);
+template <int BS, class P>
+inline cudaError_t enqueue_passes_bs(const StepBuffers& B, const Grid& G, int n, int max_iters,
+                                     bool any_zero_iters, bool any_vort, bool any_plain,
+                                     bool xsph_on, const P prm, cudaStream_t st, PhaseMarks* pm,
+                                     int persist_blocks, unsigned int* barrier) {
+    const int nb = grid_of(n, BS);
     if (persist_blocks > 0 && barrier && max_iters > 0) {
         // The whole Jacobi loop as one cooperative launch.
         cudaError_t e = cudaMemsetAsync(barrier, 0, sizeof(unsigned int), st);
@@ -854,29 +855,53 @@ inline cudaError_t enqueue_passes(const StepBuffers& B, const Grid& G, int n, in
         if (pm) pm->mark(kPhaseDensity, 1, st);
     } else {
         for (int it = 0; it < max_iters; ++it) {
-            k_density_lambda<<<nb, kBlock, 0, st>>>(B.xa, B.xb, B.srho, it, n, G, prm);
+            k_density_lambda<BS><<<nb, BS, 0, st>>>(B.xa, B.xb, B.srho, it, n, G, prm);
             if (pm) pm->mark(kPhaseDensity, 1, st);
-            k_delta<<<nb, kBlock, 0, st>>>(B.xb, B.xa, B.sx, B.srho, B.sv, it, n, G, prm);
+            k_delta<BS><<<nb, BS, 0, st>>>(B.xb, B.xa, B.sx, B.srho, B.sv, it, n, G, prm);
             if (pm) pm->mark(kPhaseDelta, 1, st);
         }
     }
     if (any_zero_iters) {
-        k_velocity<<<nb, kBlock, 0, st>>>(B.xa, B.sx, B.srho, B.sv, n, G, prm);
+        k_velocity<BS><<<nb, BS, 0, st>>>(B.xa, B.sx, B.srho, B.sv, n, G, prm);
         if (pm) pm->mark(kPhaseDelta, 1, st);
     }
     if (any_vort) {
-        k_xsph_omega<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, n, G, prm);
+        k_xsph_omega<BS><<<nb, BS, 0, st>>>(B.xa, B.sv, B.sv2, B.som, n, G, prm);
         if (pm) pm->mark(kPhaseXsph, 1, st);
-        k_vorticity_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sv2, B.som, B.sx, B.srho, n, G,
+        k_vorticity_commit<BS><<<nb, BS, 0, st>>>(B.xa, B.sv, B.sv2, B.som, B.sx, B.srho, n, G,
                                                   prm);
         if (pm) pm->mark(kPhaseCommit, 1, st);
     }
     if (any_plain) {
-        k_xsph_commit<<<nb, kBlock, 0, st>>>(B.xa, B.sv, B.sx, B.srho, n, any_vort ? 1 : 0, G,
+        k_xsph_commit<BS><<<nb, BS, 0, st>>>(B.xa, B.sv, B.sx, B.srho, n, any_vort ? 1 : 0, G,
                                              prm);
         if (pm) pm->mark(xsph_on ? kPhaseXsph : kPhaseCommit, 1, st);
     }
     return cudaGetLastError();
+}
+
+// The constraint, velocity, XSPH, vorticity and commit passes over n
+// cell-sorted particles for `max_iters` iterations, with constants from `prm`.
+// Scenes with vorticity take the XSPH+omega / vorticity+commit pair
+// (any_vort), the others XSPH+commit (any_plain).  Batches (SceneTable) may
+// pick the block size of the neighbour passes (64, 128 or 256 threads); a
+// single scene always uses kBlock.
+template <class P>
+inline cudaError_t enqueue_passes(const StepBuffers& B, const Grid& G, int n, int max_iters,
+                                  bool any_zero_iters, bool any_vort, bool any_plain, bool xsph_on,
+                                  const P prm, cudaStream_t st, PhaseMarks* pm,
+                                  int persist_blocks = 0, unsigned int* barrier = nullptr,
+                                  int block = kBlock) {
+    if constexpr (std::is_same<P, SceneTable>::value) {
+        if (block == 64)
+            return enqueue_passes_bs<64>(B, G, n, max_iters, any_zero_iters, any_vort, any_plain,
+                                         xsph_on, prm, st, pm, persist_blocks, barrier);
+        if (block == 256)
+            return enqueue_passes_bs<256>(B, G, n, max_iters, any_zero_iters, any_vort, any_plain,
+                                          xsph_on, prm, st, pm, persist_blocks, barrier);
+    }
+    return enqueue_passes_bs<kBlock>(B, G, n, max_iters, any_zero_iters, any_vort, any_plain,
+                                     xsph_on, prm, st, pm, persist_blocks, barrier);
 }
 
 inline cudaError_t enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
@@ -969,7 +994,8 @@ inline cudaError_t enqueue_batch_step(const StepBuffers& B, const BatchDesc& D, 
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return enqueue_passes(B, grid_view(B, D.spid), n, D.max_iters, D.any_zero_iters, D.any_vort,
-                          D.any_plain, D.xsph_on, tab, st, pm, D.persist_blocks, D.barrier);
+                          D.any_plain, D.xsph_on, tab, st, pm, D.persist_blocks, D.barrier,
+                          D.block);
 }
 
 // Blocks of the persistent Jacobi loop that fit on the device at once.

@@ -158,6 +158,7 @@ struct BatchDesc {
     uint32_t* stmp;            // scenes of the key-sorted particles before the scene pass
     int persist_blocks;        // > 0: the Jacobi loop as one cooperative launch of this grid
     unsigned int* barrier;     // its grid barrier (count, generation)
+    int block;                 // threads per block of the neighbour passes (64, 128, 256)
 };
 
 }  // namespace pbf

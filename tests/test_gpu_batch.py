@@ -205,3 +205,33 @@ def test_persistent_loop_on_a_large_batch():
     b2.sync()
     for k in range(len(ws)):
         assert_same(state(a[k]), state(c[k]), f"scene {k}")
+
+
+def test_autotuner_keeps_results_and_caches_its_choice(tmp_path, monkeypatch):
+    """Autotuning tries four choices on the first steps of a batch shape
+    (block size 128/64/256, persistent loop) without changing any result,
+    then keeps the fastest and records it; a new batch reads it back."""
+    cache = tmp_path / "autotune.jsonl"
+    monkeypatch.setenv("PBF_AUTOTUNE_CACHE", str(cache))
+    ws, variants = mixed_scenes()
+    alone = [make_scene(w, **kw) for w, kw in zip(ws, variants)]
+    inbatch = [make_scene(w, **kw) for w, kw in zip(ws, variants)]
+    nsteps = 6
+    for sc, w in zip(alone, ws):
+        sc.step(w.dt, nsteps)
+    b = capi.Batch()
+    b.set_autotune(True)
+    seen = set()
+    for _ in range(nsteps):
+        b.step(inbatch, [w.dt for w in ws])
+        seen.add(b.tuning())
+    assert {(128, 0), (64, 0), (256, 0), (128, 1)} <= seen
+    for k, (a, c) in enumerate(zip(alone, inbatch)):
+        assert_same(state(a), state(c), f"scene {k}")
+    lines = cache.read_text().splitlines()
+    assert len(lines) >= 1 and '"block": ' in lines[0]
+    best = b.tuning()
+    b2 = capi.Batch()
+    b2.set_autotune(True)
+    b2.step(inbatch, [w.dt for w in ws])
+    assert b2.tuning() == best
