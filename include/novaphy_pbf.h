@@ -174,6 +174,15 @@ int pbf_scene_set_bodies(pbf_scene* scene, int nbodies, const float* pos3, const
  * The rigid step that follows stays with the caller. */
 int pbf_scene_step_coupled(pbf_scene* scene, float dt, float* force3, float* torque3);
 
+/* The coupling half of pbf_scene_step_coupled, for a scene whose PBF step ran
+ * elsewhere (for instance in a pbf_batch_step with other scenes): boundary
+ * world positions from the current body poses, boundary density added to the
+ * densities, coupling forces / torques accumulated into force3 / torque3.
+ * pbf_scene_step(dt) followed by pbf_scene_couple(dt) equals
+ * pbf_scene_step_coupled(dt) bit for bit (the PBF step never reads the
+ * boundary).  dt must be the step's time step. */
+int pbf_scene_couple(pbf_scene* scene, float dt, float* force3, float* torque3);
+
 /* World positions of the boundary particles used by the last coupled step. */
 int pbf_scene_read_boundary(pbf_scene* scene, float* world3);
 

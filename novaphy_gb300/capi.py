@@ -116,6 +116,7 @@ def load() -> C.CDLL:
         "pbf_scene_set_boundary": ([vp, C.c_int, vp, vp, vp], C.c_int),
         "pbf_scene_set_bodies": ([vp, C.c_int, vp, vp, vp], C.c_int),
         "pbf_scene_step_coupled": ([vp, C.c_float, vp, vp], C.c_int),
+        "pbf_scene_couple": ([vp, C.c_float, vp, vp], C.c_int),
         "pbf_scene_read_boundary": ([vp, vp], C.c_int),
         "pbf_boundary_volumes": ([C.c_int, C.c_int, vp, C.c_float, vp], C.c_int),
         "pbf_scene_step_profiled": ([vp, C.c_float, vp, vp], C.c_int),
@@ -278,6 +279,14 @@ class Scene:
         f = _f32(force, (-1, 3)).copy()
         t = _f32(torque, (-1, 3)).copy()
         check(self._L.pbf_scene_step_coupled(self._h, dt, _ptr(f), _ptr(t)))
+        return f, t
+
+    def couple(self, dt, force, torque):
+        """The coupling half of step_coupled, after a step that ran elsewhere
+        (e.g. in a batch); returns (force, torque) accumulated onto the inputs."""
+        f = _f32(force, (-1, 3)).copy()
+        t = _f32(torque, (-1, 3)).copy()
+        check(self._L.pbf_scene_couple(self._h, dt, _ptr(f), _ptr(t)))
         return f, t
 
     def read_boundary(self):

@@ -1240,41 +1240,35 @@ int pbf_scene_set_bodies(pbf_scene* s, int nbodies, const float* pos3, const flo
     return PBF_OK;
 }
 
-int pbf_scene_step_coupled(pbf_scene* s, float dt, float* force3, float* torque3) {
-    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
-    std::lock_guard<std::mutex> lk(s->mu);
-    DeviceGuard dg(s->device);
+}  // extern "C"
+
+namespace {
+
+// Boundary world positions from the current body poses, boundary density
+// added to the final densities, coupling forces and torques accumulated onto
+// force3 / torque3 (fluid_world.cpp:57-81 after the PBF step).  C are the
+// constants of the step that produced the current state.
+int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* torque3) {
     auto& b = s->bnd;
     const int nbodies = b.nbodies;
-    if (b.nb > 0 && b.nbodies < b.needed_bodies)
-        return fail(PBF_ERR_INVALID_ARG, "set the bodies first");
-    if (nbodies > 0 && (!force3 || !torque3)) return fail(PBF_ERR_INVALID_ARG, "NULL force/torque");
-    if (s->n == 0) return PBF_OK;  // fluid_world.cpp:57
-    StepConsts C;
-    int rc = make_consts(s, dt, C);
-    if (rc) return rc;
     cudaStream_t st = s->stream;
-    // 1. boundary world positions from the step-start transforms
-    if (b.nb > 0) {
-        cudaError_t e = boundary_xform(b.local, b.body, b.nb, b.body_pos, b.body_quat, nbodies,
-                                       b.world, st);
-        if (e != cudaSuccess) return cuda_fail(e, "boundary_xform");
-    }
-    // 2. the PBF step
-    rc = run_steps(s, dt, 1);
-    if (rc) return rc;
     if (b.nb == 0) return sync_and_check(s);
-    // 3. boundary density on the final positions (fluid_world.cpp:101-123)
-    rc = ensure_boundary_grid(s, C.grid.nslots);
+    // 1. boundary world positions from the step-start transforms (unchanged
+    //    by the PBF step, which never reads the boundary)
+    cudaError_t e = boundary_xform(b.local, b.body, b.nb, b.body_pos, b.body_quat, nbodies,
+                                   b.world, st);
+    if (e != cudaSuccess) return cuda_fail(e, "boundary_xform");
+    // 2. boundary density on the final positions (fluid_world.cpp:101-123)
+    int rc = ensure_boundary_grid(s, C.grid.nslots);
     if (rc) return rc;
     rc = ensure_fluid_queries(s);
     if (rc) return rc;
-    cudaError_t e = index_build(b.idx, b.world, nullptr, b.nb, C, b.sort, st);
+    e = index_build(b.idx, b.world, nullptr, b.nb, C, b.sort, st);
     QuerySet fq{b.fq_cell, s->B.sown, s->B.btab};
     if (e == cudaSuccess) e = index_classify(fq, s->B.x, s->n, b.idx, C, st);
     if (e == cudaSuccess) e = boundary_density(s->B.x, s->n, fq, b.idx, s->B.rho, C, st);
     if (e != cudaSuccess) return cuda_fail(e, "boundary density");
-    // 4. coupling forces from a fresh fluid grid on the final positions
+    // 3. coupling forces from a fresh fluid grid on the final positions
     //    (fluid_world.cpp:125-174); the step's sorted buffers are free now.
     PointIndex fidx;
     fidx.keys = s->B.keys;
@@ -1309,6 +1303,47 @@ int pbf_scene_step_coupled(pbf_scene* s, float dt, float* force3, float* torque3
     }
     if (e != cudaSuccess) return cuda_fail(e, "coupling forces");
     return sync_and_check(s);
+}
+
+int check_coupling_args(pbf_scene* s, float* force3, float* torque3) {
+    auto& b = s->bnd;
+    if (b.nb > 0 && b.nbodies < b.needed_bodies)
+        return fail(PBF_ERR_INVALID_ARG, "set the bodies first");
+    if (b.nbodies > 0 && (!force3 || !torque3))
+        return fail(PBF_ERR_INVALID_ARG, "NULL force/torque");
+    return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbf_scene_step_coupled(pbf_scene* s, float dt, float* force3, float* torque3) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = check_coupling_args(s, force3, torque3);
+    if (rc) return rc;
+    if (s->n == 0) return PBF_OK;  // fluid_world.cpp:57
+    StepConsts C;
+    rc = make_consts(s, dt, C);
+    if (rc) return rc;
+    rc = run_steps(s, dt, 1);
+    if (rc) return rc;
+    return couple_after_step(s, C, force3, torque3);
+}
+
+int pbf_scene_couple(pbf_scene* s, float dt, float* force3, float* torque3) {
+    if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    int rc = check_coupling_args(s, force3, torque3);
+    if (rc) return rc;
+    if (s->n == 0) return PBF_OK;
+    StepConsts C;
+    rc = make_consts(s, dt, C);
+    if (rc) return rc;
+    return couple_after_step(s, C, force3, torque3);
 }
 
 int pbf_scene_read_boundary(pbf_scene* s, float* world3) {

@@ -100,3 +100,37 @@ def test_coupled_step_without_boundary_is_plain_step():
     b.step_coupled(w.dt, np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32))
     for u, v in zip(a.state(), b.state()):
         assert np.array_equal(u, v)
+
+
+def test_batched_step_then_couple_equals_coupled_step(port):
+    """Coupled worlds stepped together: one batch step of their fluids, then
+    each world's coupling (pbf_scene_couple) gives the bits of its own
+    pbf_scene_step_coupled, with a plain scene in the same batch."""
+    w, local, body, psi, bp, bq, dyn, world0 = coupled_scene(port)
+    f0 = np.array([[0.1, -0.2, 0.3], [0.0, 0.0, 0.0]], np.float32)
+    t0 = np.array([[0.01, 0.02, -0.03], [0.0, 0.0, 0.0]], np.float32)
+
+    def make():
+        sc = capi.Scene(capi.default_settings(**w.settings), w.x, w.v, mass=w.mass)
+        sc.set_gravity(w.gravity)
+        sc.set_boundary(local, body, psi)
+        sc.set_bodies(bp, bq, dyn)
+        return sc
+
+    ref = make()
+    rf, rt = f0, t0
+    for _ in range(2):
+        rf, rt = ref.step_coupled(w.dt, rf, rt)
+    other_w = workloads.batched_scenes(nscenes=1, seed=4, n_lo=800, n_hi=1200)[0]
+    other = capi.Scene(capi.default_settings(**other_w.settings), other_w.x, other_w.v,
+                       mass=other_w.mass)
+    other.set_gravity(other_w.gravity)
+    sc = make()
+    b = capi.Batch()
+    f, t = f0, t0
+    for _ in range(2):
+        b.step([other, sc], [other_w.dt, w.dt])
+        f, t = sc.couple(w.dt, f, t)
+    for a, c in zip(ref.state(), sc.state()):
+        assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
+    assert np.array_equal(f, rf) and np.array_equal(t, rt)
