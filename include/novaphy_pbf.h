@@ -393,6 +393,38 @@ int pbf_server_submit(pbf_server* server, long long scene_id, float dt, int nste
  * its pbf_request_state.  PBF_ERR_TIMEOUT if still pending; a failed request
  * returns its failure status, with the reason in pbf_last_error(). */
 int pbf_server_wait(pbf_server* server, long long request_id, double timeout_s, int* state_out);
+/* A rigid body of a served coupled scene: the state the host rigid step of
+ * World integrates (free bodies, no contacts; src/dynamics/integrator.cpp).
+ * inv_mass 0 marks a static body; inv_inertia is RigidBody::inv_inertia,
+ * row-major. */
+typedef struct pbf_rigid_body {
+    float pos[3];
+    float quat[4]; /* w, x, y, z */
+    float lin_vel[3];
+    float ang_vel[3];
+    float inv_mass;
+    float inv_inertia[9];
+} pbf_rigid_body;
+
+/* Opens a coupled scene: the fluid of pbf_server_open_scene plus nb Akinci
+ * boundary particles (pbf_scene_set_boundary layout; psi from
+ * pbf_boundary_volumes) owned by nbodies rigid bodies.  Each served step of
+ * it is FluidWorld::step (src/fluid/fluid_world.cpp:46-99): the PBF step,
+ * batched with the other scenes; the coupling (pbf_scene_couple); then the
+ * host rigid step of the bodies under gravity and the coupling forces, before
+ * the scene's next step.  The scene is charged its own step scratch too,
+ * which the coupling uses. */
+int pbf_server_open_coupled_scene(pbf_server* server, const pbf_settings* settings, int n,
+                                  const float* x3, const float* v3, float mass,
+                                  const float* gravity3, int nb, const float* local3,
+                                  const int* body, const float* psi, int nbodies,
+                                  const pbf_rigid_body* bodies, long long* scene_id,
+                                  int* state_out);
+
+/* The bodies of a coupled scene after its completed steps (waits until the
+ * scene has no pending request). */
+int pbf_server_read_bodies(pbf_server* server, long long scene_id, pbf_rigid_body* out);
+
 /* Waits until the scene has no pending request, then reads a field
  * (pbf_scene_read layout). */
 int pbf_server_read(pbf_server* server, long long scene_id, int field, float* host_out);

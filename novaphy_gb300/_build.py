@@ -123,7 +123,7 @@ def build_core(verbose: bool = False) -> str | None:
         return None
     os.makedirs(BUILD, exist_ok=True)
     out = core_path()
-    incs = [f"-I{p}" for p in _pybind_includes()] + [f"-I{INCLUDE}", f"-I{HOST}"]
+    incs = [f"-I{p}" for p in _pybind_includes()] + [f"-I{INCLUDE}", f"-I{HOST}", f"-I{CSRC}"]
     flags = ["-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden"]
 
     def comp(src: str) -> str:

@@ -144,6 +144,9 @@ def load() -> C.CDLL:
         "pbf_server_scene_state": ([vp, C.c_longlong, vp], C.c_int),
         "pbf_server_get_stats": ([vp, vp], C.c_int),
         "pbf_server_reset_stats": ([vp], C.c_int),
+        "pbf_server_open_coupled_scene": ([vp, vp, C.c_int, vp, vp, C.c_float, vp, C.c_int, vp, vp,
+                                           vp, C.c_int, vp, vp, vp], C.c_int),
+        "pbf_server_read_bodies": ([vp, C.c_longlong, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -476,6 +479,19 @@ SCENE_WAITING, SCENE_RESIDENT, SCENE_FAILED = 0, 1, 2
 REQ_PENDING, REQ_DONE, REQ_FAILED = 0, 1, 2
 
 
+class RigidBody(C.Structure):
+    """pbf_rigid_body: pose (quaternion w, x, y, z), velocities, inverse mass and inertia."""
+
+    _fields_ = [
+        ("pos", C.c_float * 3),
+        ("quat", C.c_float * 4),
+        ("lin_vel", C.c_float * 3),
+        ("ang_vel", C.c_float * 3),
+        ("inv_mass", C.c_float),
+        ("inv_inertia", C.c_float * 9),
+    ]
+
+
 class ServerConfig(C.Structure):
     """pbf_server_config."""
 
@@ -550,6 +566,29 @@ class Server:
                                             _ptr(g) if g is not None else None, C.byref(sid),
                                             C.byref(st)))
         return sid.value, st.value
+
+    def open_coupled_scene(self, settings: Settings, x, v, mass, gravity, local, body, psi,
+                           bodies):
+        """A FluidWorld-like scene: boundary particles (local, body, psi) owned by
+        `bodies` (a sequence of RigidBody) that the server advances after each step."""
+        x = _f32(x, (-1, 3))
+        vv = _f32(v, x.shape) if v is not None else None
+        g = _f32(gravity, (3,))
+        local = _f32(local, (-1, 3))
+        body = np.ascontiguousarray(body, np.int32)
+        psi = _f32(psi)
+        arr = (RigidBody * max(len(bodies), 1))(*bodies)
+        sid, st = C.c_longlong(0), C.c_int(0)
+        check(self._L.pbf_server_open_coupled_scene(
+            self._h, C.byref(settings), len(x), _ptr(x), _ptr(vv) if vv is not None else None,
+            mass, _ptr(g), len(local), _ptr(local), _ptr(body), _ptr(psi), len(bodies), arr,
+            C.byref(sid), C.byref(st)))
+        return sid.value, st.value
+
+    def read_bodies(self, sid: int, nbodies: int):
+        arr = (RigidBody * max(nbodies, 1))()
+        check(self._L.pbf_server_read_bodies(self._h, sid, arr))
+        return list(arr)[:nbodies]
 
     def close_scene(self, sid: int):
         check(self._L.pbf_server_close_scene(self._h, sid))

@@ -117,6 +117,10 @@ PYBIND11_MODULE(_core, m) {
         .def_readwrite("mass", &RigidBody::mass)
         .def_readwrite("com", &RigidBody::com)
         .def("inv_mass", &RigidBody::inv_mass)
+        .def("inv_inertia", [](const RigidBody& b) {
+            const auto a = b.inv_inertia();
+            return std::vector<float>(a.begin(), a.end());
+        })
         .def("is_static", &RigidBody::is_static)
         .def_static("from_box", &RigidBody::from_box, py::arg("mass"), py::arg("half_extents"))
         .def_static("from_sphere", &RigidBody::from_sphere, py::arg("mass"), py::arg("radius"))

@@ -1,6 +1,7 @@
 // Host layer implementation (see novaphy_host.hpp).  Compiled with
 // -ffp-contract=off so that host float arithmetic rounds like the reference.
 #include "novaphy_host.hpp"
+#include "rigid_step.hpp"
 
 #include <algorithm>
 #include <cstdlib>
@@ -431,14 +432,15 @@ void World::step_rigid_pipeline(float dt) {
             if (b.is_static()) continue;
             Vec3& v = state_.linear_velocities[(size_t)i];
             Vec3& w = state_.angular_velocities[(size_t)i];
-            v += (gravity_ + state_.forces[(size_t)i] * b.inv_mass()) * dt;
-            const auto ii = b.inv_inertia();
+            const float g[3] = {gravity_.x, gravity_.y, gravity_.z};
+            const Vec3& f = state_.forces[(size_t)i];
             const Vec3& t = state_.torques[(size_t)i];
-            const Vec3 it(ii[0] * t.x + (ii[1] * t.y + ii[2] * t.z),
-                          ii[3] * t.x + (ii[4] * t.y + ii[5] * t.z),
-                          ii[6] * t.x + (ii[7] * t.y + ii[8] * t.z));
-            w += it * dt;
-            w = w * 0.999f;
+            const float fa[3] = {f.x, f.y, f.z}, ta[3] = {t.x, t.y, t.z};
+            float va[3] = {v.x, v.y, v.z}, wa[3] = {w.x, w.y, w.z};
+            const auto ii = b.inv_inertia();
+            pbf_rigid::integrate_velocity(va, wa, g, fa, b.inv_mass(), ii.data(), ta, dt);
+            v = Vec3(va[0], va[1], va[2]);
+            w = Vec3(wa[0], wa[1], wa[2]);
         }
     }
     { Scope s(monitor_, "world.broadphase.sap"); }  // contacts are not modelled on this path
@@ -449,18 +451,12 @@ void World::step_rigid_pipeline(float dt) {
             Transform& tr = state_.transforms[(size_t)i];
             const Vec3& v = state_.linear_velocities[(size_t)i];
             const Vec3& w = state_.angular_velocities[(size_t)i];
-            tr.position += v * dt;
-            Quat& q = tr.rotation;
-            Quat dq;
-            dq.w = 0.5f * (-w.x * q.x - w.y * q.y - w.z * q.z);
-            dq.x = 0.5f * (w.x * q.w + w.z * q.y - w.y * q.z);
-            dq.y = 0.5f * (w.y * q.w - w.z * q.x + w.x * q.z);
-            dq.z = 0.5f * (w.z * q.w + w.y * q.x - w.x * q.y);
-            q.w += dq.w * dt;
-            q.x += dq.x * dt;
-            q.y += dq.y * dt;
-            q.z += dq.z * dt;
-            q = q.normalized();
+            float p[3] = {tr.position.x, tr.position.y, tr.position.z};
+            float q[4] = {tr.rotation.w, tr.rotation.x, tr.rotation.y, tr.rotation.z};
+            const float va[3] = {v.x, v.y, v.z}, wa[3] = {w.x, w.y, w.z};
+            pbf_rigid::integrate_position(p, q, va, wa, dt);
+            tr.position = Vec3(p[0], p[1], p[2]);
+            tr.rotation = Quat{q[0], q[1], q[2], q[3]};
         }
     }
     {

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "pbf_internal.cuh"
+#include "rigid_step.hpp"
 
 using namespace pbf;
 using namespace pbf::capi;
@@ -36,6 +37,9 @@ using namespace pbf::capi;
 namespace {
 
 constexpr size_t kGridBytesPerSlot = 5;  // one offset word + one alias byte
+// Device bytes per boundary particle of a coupled scene: local, world and force
+// float4s, body index, query cell and classification row, boundary index.
+constexpr size_t kBoundaryBytes = 256;
 
 double now_ms() {
     using namespace std::chrono;
@@ -58,6 +62,18 @@ struct SceneRec {
     int inflight = 0;            // steps issued, not completed
     std::string why;             // why the scene failed
     int code = PBF_OK;           // and the status its requests fail with
+    // Coupled scenes (FluidWorld): Akinci boundary owned by rigid bodies that
+    // the host rigid step advances after each step of the scene.
+    bool coupled = false;
+    std::vector<float> local, psi;  // until the device copy is made
+    std::vector<int> body;
+    std::vector<pbf_rigid_body> bodies;
+    bool post = false;  // coupling and rigid step of its last step still to run
+};
+
+struct PostItem {
+    long long scene, req;
+    float dt;
 };
 
 struct ReqRec {
@@ -146,8 +162,12 @@ void fail_scene(pbf_server* sv, SceneRec& sc, const std::string& why, int code) 
     sc.reqs.clear();
 }
 
+void credit_step(pbf_server* sv, SceneRec& sc, ReqRec& r, double t);
+
 // Marks completed steps of a finished launch; called with the lock held.
-void complete_launch(pbf_server* sv, const Launch& L, double t) {
+// Steps of coupled scenes are queued on `post` instead (their coupling and
+// rigid step run next, outside the lock).
+void complete_launch(pbf_server* sv, const Launch& L, double t, std::vector<PostItem>* post) {
     const uint32_t* fl = sv->flags + (size_t)L.slot * sv->cfg.max_batch_scenes;
     for (size_t k = 0; k < L.items.size(); ++k) {
         auto sit = sv->scenes.find(L.items[k].first);
@@ -161,18 +181,29 @@ void complete_launch(pbf_server* sv, const Launch& L, double t) {
         if (rit == sv->reqs.end()) continue;
         ReqRec& r = rit->second;
         if (r.state != PBF_REQ_PENDING) continue;
-        ++r.done;
-        ++sv->steps_done;
-        sv->particle_steps += sc.n;
-        sv->step_ms.push_back(t - r.t_prev);
-        r.t_prev = t;
-        sv->t_last = t;
-        if (r.done == r.nsteps) {
-            r.state = PBF_REQ_DONE;
-            ++sv->done_reqs;
-            sv->req_ms.push_back(t - r.t_submit);
-            if (!sc.reqs.empty() && sc.reqs.front() == r.id) sc.reqs.pop_front();
+        if (sc.coupled && post) {
+            // The step ends with its coupling and rigid step (run_posts).
+            sc.post = true;
+            post->push_back({sc.id, r.id, r.dt});
+            continue;
         }
+        credit_step(sv, sc, r, t);
+    }
+}
+
+// Counts one completed step of request r of scene sc at time t.
+void credit_step(pbf_server* sv, SceneRec& sc, ReqRec& r, double t) {
+    ++r.done;
+    ++sv->steps_done;
+    sv->particle_steps += sc.n;
+    sv->step_ms.push_back(t - r.t_prev);
+    r.t_prev = t;
+    sv->t_last = t;
+    if (r.done == r.nsteps) {
+        r.state = PBF_REQ_DONE;
+        ++sv->done_reqs;
+        sv->req_ms.push_back(t - r.t_submit);
+        if (!sc.reqs.empty() && sc.reqs.front() == r.id) sc.reqs.pop_front();
     }
 }
 
@@ -188,6 +219,7 @@ bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
     for (auto& kv : sv->scenes) {
         SceneRec& sc = kv.second;
         if (sc.state != PBF_SCENE_RESIDENT || !sc.s || sc.busy) continue;
+        if (sc.coupled && (sc.inflight > 0 || sc.post)) continue;  // one step at a time
         for (long long rid : sc.reqs) {
             ReqRec& r = sv->reqs[rid];
             if (r.state == PBF_REQ_PENDING && r.issued < r.nsteps) {
@@ -259,6 +291,53 @@ void issue_main(pbf_server* sv) {
     }
 }
 
+// Coupling and rigid step of coupled scenes whose PBF step just completed
+// (FluidWorld::step after the fluid step); called without the lock.  Only
+// the retire thread touches a scene's bodies while its `post` flag is set.
+void run_posts(pbf_server* sv, const std::vector<PostItem>& items) {
+    for (const PostItem& it : items) {
+        SceneRec* sc = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            auto sit = sv->scenes.find(it.scene);
+            if (sit != sv->scenes.end()) sc = &sit->second;
+        }
+        if (!sc) continue;
+        const int nb = (int)sc->bodies.size();
+        std::vector<float> f((size_t)3 * nb, 0.0f), tq((size_t)3 * nb, 0.0f);
+        int rc = pbf_scene_couple(sc->s, it.dt, nb ? f.data() : nullptr, nb ? tq.data() : nullptr);
+        std::string why;
+        if (rc) why = std::string("coupling failed: ") + pbf_last_error();
+        if (!rc && nb > 0) {
+            std::vector<float> pos((size_t)3 * nb), quat((size_t)4 * nb);
+            std::vector<int> dyn((size_t)nb);
+            for (int k = 0; k < nb; ++k) {
+                pbf_rigid_body& b = sc->bodies[(size_t)k];
+                if (b.inv_mass > 0.0f) {
+                    pbf_rigid::integrate_velocity(b.lin_vel, b.ang_vel, sc->gravity, &f[3 * k],
+                                                  b.inv_mass, b.inv_inertia, &tq[3 * k], it.dt);
+                    pbf_rigid::integrate_position(b.pos, b.quat, b.lin_vel, b.ang_vel, it.dt);
+                }
+                for (int d = 0; d < 3; ++d) pos[3 * k + d] = b.pos[d];
+                for (int d = 0; d < 4; ++d) quat[4 * k + d] = b.quat[d];
+                dyn[(size_t)k] = b.inv_mass > 0.0f ? 1 : 0;
+            }
+            rc = pbf_scene_set_bodies(sc->s, nb, pos.data(), quat.data(), dyn.data());
+            if (rc) why = std::string("setting the bodies failed: ") + pbf_last_error();
+        }
+        const double t = now_ms();
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sc->post = false;
+        if (rc) {
+            fail_scene(sv, *sc, why, rc);
+            continue;
+        }
+        auto rit = sv->reqs.find(it.req);
+        if (rit != sv->reqs.end() && rit->second.state == PBF_REQ_PENDING)
+            credit_step(sv, *sc, rit->second, t);
+    }
+}
+
 // Waits for the oldest launch and retires its steps.
 void retire_main(pbf_server* sv) {
     cudaSetDevice(sv->device);
@@ -286,7 +365,13 @@ void retire_main(pbf_server* sv) {
                 fail_scene(sv, sit->second, why, PBF_ERR_CUDA);
             }
         } else {
-            complete_launch(sv, L, t);
+            std::vector<PostItem> post;
+            complete_launch(sv, L, t, &post);
+            if (!post.empty()) {
+                lk.unlock();
+                run_posts(sv, post);
+                lk.lock();
+            }
         }
         sv->cv_work.notify_one();
         sv->cv_done.notify_all();
@@ -303,6 +388,28 @@ int materialize(pbf_server* sv, SceneRec& rec) {
     if (rc) {
         pbf_scene_destroy(s);
         return rc;
+    }
+    if (rec.coupled) {
+        const int nb = (int)rec.body.size(), nbodies = (int)rec.bodies.size();
+        rc = pbf_scene_set_boundary(s, nb, rec.local.data(), rec.body.data(), rec.psi.data());
+        if (!rc && nbodies > 0) {
+            std::vector<float> pos((size_t)3 * nbodies), quat((size_t)4 * nbodies);
+            std::vector<int> dyn((size_t)nbodies);
+            for (int k = 0; k < nbodies; ++k) {
+                const pbf_rigid_body& b = rec.bodies[(size_t)k];
+                for (int d = 0; d < 3; ++d) pos[3 * k + d] = b.pos[d];
+                for (int d = 0; d < 4; ++d) quat[4 * k + d] = b.quat[d];
+                dyn[(size_t)k] = b.inv_mass > 0.0f ? 1 : 0;
+            }
+            rc = pbf_scene_set_bodies(s, nbodies, pos.data(), quat.data(), dyn.data());
+        }
+        if (rc) {
+            pbf_scene_destroy(s);
+            return rc;
+        }
+        rec.local.clear();
+        rec.psi.clear();
+        rec.body.clear();
     }
     // The scene keeps its own stream: launches order themselves against it
     // with events, and client threads (reads, closes) never put work on the
@@ -433,16 +540,41 @@ int pbf_server_destroy(pbf_server* sv) {
     return PBF_OK;
 }
 
-int pbf_server_open_scene(pbf_server* sv, const pbf_settings* st, int n, const float* x3,
-                          const float* v3, float mass, const float* g3, long long* id_out,
-                          int* state_out) {
+}  // extern "C"
+
+namespace {
+
+struct CoupledArgs {
+    int nb = 0;
+    const float* local3 = nullptr;
+    const int* body = nullptr;
+    const float* psi = nullptr;
+    int nbodies = 0;
+    const pbf_rigid_body* bodies = nullptr;
+};
+
+int open_impl(pbf_server* sv, const pbf_settings* st, int n, const float* x3, const float* v3,
+              float mass, const float* g3, const CoupledArgs* cp, long long* id_out,
+              int* state_out) {
     int rc = check_server(sv);
     if (rc) return rc;
     if (!st || !id_out || (n > 0 && !x3)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
     if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n must be >= 0");
     rc = check_settings(st);
     if (rc) return rc;
-    const size_t charge = charge_of(n, grid_slots_for(*st, x3, n));
+    const uint32_t slots = grid_slots_for(*st, x3, n);
+    size_t charge = charge_of(n, slots);
+    if (cp) {
+        if (cp->nb < 0 || cp->nbodies < 0 || (cp->nb > 0 && (!cp->local3 || !cp->body || !cp->psi)) ||
+            (cp->nbodies > 0 && !cp->bodies))
+            return fail(PBF_ERR_INVALID_ARG, "bad boundary or bodies");
+        for (int i = 0; i < cp->nb; ++i)
+            if (cp->body[i] >= cp->nbodies)
+                return fail(PBF_ERR_INVALID_ARG, "a boundary particle names a missing body");
+        // The coupling runs on the scene's own step scratch and offsets.
+        charge += work_bytes(n > 0 ? n : 1) + sort_scratch_bytes(n > 0 ? n : 1) +
+                  (size_t)slots * kGridBytesPerSlot + (size_t)cp->nb * kBoundaryBytes;
+    }
     std::unique_lock<std::mutex> lk(sv->mu);
     if (charge + sv->scratch > sv->cfg.hbm_budget_bytes) {
         ++sv->rejected;
@@ -462,6 +594,13 @@ int pbf_server_open_scene(pbf_server* sv, const pbf_settings* st, int n, const f
         for (int d = 0; d < 3; ++d) rec.gravity[d] = g3[d];
     rec.x.assign(x3, x3 + (size_t)3 * n);
     if (v3) rec.v.assign(v3, v3 + (size_t)3 * n);
+    if (cp) {
+        rec.coupled = true;
+        rec.local.assign(cp->local3, cp->local3 + (size_t)3 * cp->nb);
+        rec.body.assign(cp->body, cp->body + cp->nb);
+        rec.psi.assign(cp->psi, cp->psi + cp->nb);
+        rec.bodies.assign(cp->bodies, cp->bodies + cp->nbodies);
+    }
     sv->admit_queue.push_back(id);
     admit_waiting(sv, lk);
     auto it = sv->scenes.find(id);
@@ -469,6 +608,31 @@ int pbf_server_open_scene(pbf_server* sv, const pbf_settings* st, int n, const f
     *id_out = id;
     if (state_out) *state_out = state;
     return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbf_server_open_scene(pbf_server* sv, const pbf_settings* st, int n, const float* x3,
+                          const float* v3, float mass, const float* g3, long long* id_out,
+                          int* state_out) {
+    return open_impl(sv, st, n, x3, v3, mass, g3, nullptr, id_out, state_out);
+}
+
+int pbf_server_open_coupled_scene(pbf_server* sv, const pbf_settings* st, int n, const float* x3,
+                                  const float* v3, float mass, const float* g3, int nb,
+                                  const float* local3, const int* body, const float* psi,
+                                  int nbodies, const pbf_rigid_body* bodies, long long* id_out,
+                                  int* state_out) {
+    CoupledArgs cp;
+    cp.nb = nb;
+    cp.local3 = local3;
+    cp.body = body;
+    cp.psi = psi;
+    cp.nbodies = nbodies;
+    cp.bodies = bodies;
+    return open_impl(sv, st, n, x3, v3, mass, g3, &cp, id_out, state_out);
 }
 
 int pbf_server_close_scene(pbf_server* sv, long long id) {
@@ -489,7 +653,7 @@ int pbf_server_close_scene(pbf_server* sv, long long id) {
             auto r = sv->reqs.find(rid);
             if (r != sv->reqs.end() && r->second.state == PBF_REQ_PENDING) pending = true;
         }
-        return !pending && sc.inflight == 0;
+        return !pending && sc.inflight == 0 && !sc.post;
     });
     it = sv->scenes.find(id);
     if (it == sv->scenes.end()) return PBF_OK;
@@ -579,7 +743,7 @@ int pbf_server_read(pbf_server* sv, long long id, int field, float* out) {
             if (sc.busy) return false;
             for (long long r : sc.reqs)
                 if (sv->reqs[r].state == PBF_REQ_PENDING) return false;
-            return sc.inflight == 0;
+            return sc.inflight == 0 && !sc.post;
         };
         sv->cv_done.wait(lk, idle);
         auto it = sv->scenes.find(id);
@@ -613,6 +777,27 @@ int pbf_server_read(pbf_server* sv, long long id, int field, float* out) {
     }
     sv->cv_done.notify_all();
     return rc;
+}
+
+int pbf_server_read_bodies(pbf_server* sv, long long id, pbf_rigid_body* out) {
+    int rc = check_server(sv);
+    if (rc) return rc;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    sv->cv_done.wait(lk, [&] {
+        auto it = sv->scenes.find(id);
+        if (it == sv->scenes.end()) return true;
+        const SceneRec& sc = it->second;
+        if (sc.busy || sc.post || sc.inflight > 0) return false;
+        for (long long r : sc.reqs)
+            if (sv->reqs[r].state == PBF_REQ_PENDING) return false;
+        return true;
+    });
+    auto it = sv->scenes.find(id);
+    if (it == sv->scenes.end()) return fail(PBF_ERR_INVALID_ARG, "no such scene");
+    const auto& b = it->second.bodies;
+    if (!b.empty() && !out) return fail(PBF_ERR_INVALID_ARG, "output is NULL");
+    std::copy(b.begin(), b.end(), out);
+    return PBF_OK;
 }
 
 int pbf_server_scene_state(pbf_server* sv, long long id, int* state_out) {

@@ -225,3 +225,84 @@ def test_reads_and_closes_while_other_scenes_run():
         got, steps = results[k]
         assert same(got, alone(w, [w.dt] * steps)), k
     srv.close()
+
+
+def test_coupled_served_scene_equals_fluid_world():
+    """A served scene with Akinci rigid bodies follows FluidWorld.step bit for
+    bit: fluid state (with boundary density) and the bodies' poses and
+    velocities after several steps, the PBF step batched with another scene."""
+    import novaphy_gb300 as nv
+
+    mb = nv.ModelBuilder()
+    mb.add_ground_plane(y=0.0)
+    si = mb.add_body(nv.RigidBody.from_sphere(0.5, 0.12),
+                     nv.Transform.from_translation(np.array([0.1, 0.25, 0.1], np.float32)))
+    mb.add_shape(nv.CollisionShape.make_sphere(0.12, si))
+    bi = mb.add_body(nv.RigidBody.from_box(0.8, np.array([0.05, 0.05, 0.05], np.float32)),
+                     nv.Transform(np.array([0.22, 0.3, 0.15], np.float32),
+                                  [0.0, 0.25881904, 0.0, 0.96592583]))
+    mb.add_shape(nv.CollisionShape.make_box(np.array([0.05, 0.05, 0.05], np.float32), bi))
+    model = mb.build()
+    pbf = nv.PBFSettings()
+    pbf.kernel_radius = 0.2
+    pbf.solver_iterations = 2
+    blk = nv.FluidBlockDef()
+    blk.lower = np.array([0, 0.05, 0], np.float32)
+    blk.upper = np.array([0.3, 0.4, 0.3], np.float32)
+    blk.particle_spacing = 0.05
+    fw = nv.FluidWorld(model, [blk], nv.SolverSettings(), pbf, boundary_extent=0.5)
+    x0 = fw.fluid_state.positions_array.copy()
+    v0 = fw.fluid_state.velocities_array.copy()
+    bps = fw.boundary_particles
+    local = np.stack([b.local_position for b in bps]).astype(np.float32)
+    body = np.array([b.body_index for b in bps], np.int32)
+    psi = np.array([b.volume for b in bps], np.float32)
+    bodies = []
+    for k, rb in enumerate(model.bodies):
+        tr = model.initial_transforms[k]
+        q = np.asarray(tr.rotation, np.float32)  # x, y, z, w
+        b = capi.RigidBody()
+        b.pos[:] = [float(c) for c in tr.position]
+        b.quat[:] = [float(q[3]), float(q[0]), float(q[1]), float(q[2])]
+        b.inv_mass = rb.inv_mass()
+        b.inv_inertia[:] = rb.inv_inertia()
+        bodies.append(b)
+    st = capi.Settings()
+    for name, _ in capi.Settings._fields_:
+        val = getattr(fw.pbf_settings, name)
+        if name in ("domain_lower", "domain_upper"):
+            getattr(st, name)[:] = [float(c) for c in val]
+        else:
+            setattr(st, name, val)
+    mass = fw.pbf_settings.particle_mass(0.05)
+    g = [0.0, -9.81, 0.0]
+    dt = float(np.float32(1 / 60))
+    nsteps = 4
+
+    other = small_scenes(k=1, seed=23)[0]
+    srv = capi.Server()
+    oid, _ = srv.open_scene(settings_of(other), other.x, other.v, other.mass, other.gravity)
+    sid, state = srv.open_coupled_scene(st, x0, v0, mass, g, local, body, psi, bodies)
+    assert state == capi.SCENE_RESIDENT
+    qo = srv.submit(oid, other.dt, nsteps)
+    qs = srv.submit(sid, dt, nsteps)
+    assert srv.wait(qs) == capi.REQ_DONE and srv.wait(qo) == capi.REQ_DONE
+    for _ in range(nsteps):
+        fw.step(dt)
+    fs = fw.fluid_state
+    for got, want in ((srv.read(sid, capi.FIELD_POSITIONS, len(x0)), fs.positions_array),
+                      (srv.read(sid, capi.FIELD_VELOCITIES, len(x0)), fs.velocities_array),
+                      (srv.read(sid, capi.FIELD_DENSITIES, len(x0)), fs.densities_array)):
+        assert np.array_equal(got.view(np.uint32), np.asarray(want, np.float32).view(np.uint32))
+    out = srv.read_bodies(sid, len(bodies))
+    for k, b in enumerate(out):
+        tr = fw.state.transforms[k]
+        q = np.asarray(tr.rotation, np.float32)
+        assert np.array_equal(np.array(b.pos, np.float32), np.asarray(tr.position, np.float32)), k
+        assert np.array_equal(np.array(b.quat, np.float32), q[[3, 0, 1, 2]]), k
+        assert np.array_equal(np.array(b.lin_vel, np.float32),
+                              np.asarray(fw.state.linear_velocities[k], np.float32)), k
+        assert np.array_equal(np.array(b.ang_vel, np.float32),
+                              np.asarray(fw.state.angular_velocities[k], np.float32)), k
+    assert out[0].pos[1] != 0.25  # the sphere moved
+    srv.close()
