@@ -49,7 +49,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from novaphy_gb300 import workloads  # noqa: E402
+from novaphy_gb300 import shard, workloads  # noqa: E402
 
 METRIC = "particle-steps/sec"
 UNIT = "particle-steps/s"
@@ -243,7 +243,7 @@ def cpu_scene_pool(sample):
                       f"throughput x {cores} cores"}
 
 
-def run_batched(args, device):
+def run_batched(args, device, ws=1, rank=0, dist=None):
     """Independent dam-break scenes of uneven size (workloads.batched_scenes:
     1,024 scenes, 2,000-64,000 particles log-uniform, 2-6 iterations) stepped
     (a) as one batch per step (pbf_batch_step: one sort and one launch per
@@ -256,7 +256,13 @@ def run_batched(args, device):
     from novaphy_gb300 import capi
 
     wl = workloads.batched_scenes(nscenes=args.batched_scenes)
+    if ws > 1:  # this rank's share of the scenes, dealt by particle count
+        wl = [wl[i] for i in shard.rank_scenes([w.n for w in wl], ws, rank)]
     total = int(sum(w.n for w in wl))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
     scenes = []
     for w in wl:
         sc = capi.Scene(capi.default_settings(**w.settings), w.x, w.v, mass=w.mass, device=device)
@@ -281,10 +287,12 @@ def run_batched(args, device):
     tuning = b.tuning()
     reseed()
     lat = []
+    barrier()
     t0 = time.perf_counter()
     for _ in range(k):
         lat.append(b.step_timed(scenes, dts))
     t_batch = time.perf_counter() - t0
+    job_units, job_batch = shard.job_throughput(total * k, t_batch, dist)
     reseed()
     dev_ms = b.replay_timed(scenes, seeds, dts, k)
     # The same with the Jacobi loop as one persistent cooperative launch.
@@ -335,7 +343,8 @@ def run_batched(args, device):
                     f"({min(w.n for w in wl)}-{max(w.n for w in wl)} per scene), r = 0.02, "
                     f"h = 4r, 2-6 iterations, dt = 1/120",
         "particles": total, "scenes": len(wl), "steps": k,
-        "value": total * k / t_batch, "unit": UNIT,
+        "value": job_units / job_batch, "unit": UNIT,
+        "ranks": ws, "rank0_particles": total,
         "plain_value": total * k / t_plain if t_plain else None,
         "speedup_vs_plain": t_plain / t_batch if t_plain else None,
         "plain_sync_value": total * ks / t_plain_sync if t_plain_sync else None,
@@ -355,11 +364,66 @@ def run_batched(args, device):
         sc.close()
     if not args.no_cpu_baseline and not args.no_batched_plain:
         progress("batched: cpu baseline")
-        out["cpu_baseline"] = cpu_scene_pool(wl[:: max(1, len(wl) // (2 * (os.cpu_count() or 1)))])
+        if rank == 0:
+            out["cpu_baseline"] = cpu_scene_pool(
+                wl[:: max(1, len(wl) // (2 * (os.cpu_count() or 1)))])
     return out
 
 
-def run_served(args, device):
+def sphere_boundary(w, device=0):
+    """Akinci boundary of a workload's rigid spheres (workloads.served_scenes):
+    body-frame samples at spacing r from the host sampler, psi from their
+    initial world positions on the device, and the bodies as RigidBody."""
+    import novaphy_gb300 as nv
+    from novaphy_gb300 import capi
+
+    sph = w.meta.get("spheres", [])
+    if not sph:
+        return None
+    r = w.meta["r"]
+    mb = nv.ModelBuilder()
+    bodies = []
+    for (c, rad, dens) in sph:
+        m = float(np.float32(dens) * np.float32(4.0 / 3.0 * np.pi) * np.float32(rad) ** 3)
+        rb = nv.RigidBody.from_sphere(m, rad)
+        bi = mb.add_body(rb, nv.Transform.from_translation(np.array(c, np.float32)))
+        mb.add_shape(nv.CollisionShape.make_sphere(rad, bi))
+        b = capi.RigidBody()
+        b.pos[:] = [float(v) for v in np.array(c, np.float32)]
+        b.quat[:] = [1.0, 0.0, 0.0, 0.0]
+        b.inv_mass = rb.inv_mass()
+        b.inv_inertia[:] = rb.inv_inertia()
+        bodies.append(b)
+    bps = nv.sample_model_boundaries(mb.build(), r, 1.0)
+    local = np.stack([b.local_position for b in bps]).astype(np.float32)
+    body = np.array([b.body_index for b in bps], np.int32)
+    centers = np.array([c for (c, _, _) in sph], np.float32)
+    world = (local + centers[body]).astype(np.float32)
+    psi = capi.boundary_volumes(world, w.settings["kernel_radius"], device)
+    return local, body, psi, bodies
+
+
+def rigid_step_np(state, f, t, g, dt):
+    """Host rigid step of free bodies in numpy (float32), for the plain arm:
+    the same semi-implicit Euler as the library's (timing only)."""
+    dt = np.float32(dt)
+    for k, b in enumerate(state):
+        if b["inv_mass"] == 0:
+            continue
+        b["v"] += (g + f[k] * b["inv_mass"]) * dt
+        b["w"] = (b["w"] + (b["ii"] @ t[k]) * dt) * np.float32(0.999)
+        b["p"] += b["v"] * dt
+        qw, qx, qy, qz = b["q"]
+        w = b["w"]
+        dq = np.float32(0.5) * np.array([-w[0] * qx - w[1] * qy - w[2] * qz,
+                                         w[0] * qw + w[2] * qy - w[1] * qz,
+                                         w[1] * qw - w[2] * qx + w[0] * qz,
+                                         w[2] * qw + w[1] * qx - w[0] * qy], np.float32)
+        q = b["q"] + dq * dt
+        b["q"] = (q / np.sqrt((q * q).sum())).astype(np.float32)
+
+
+def run_served(args, device, ws=1, rank=0, dist=None):
     """Serving run over workloads.served_scenes (256 clients, 1k-200k particles
     log-uniform, dam breaks and pools, dt = 1/240).  Each client draws request
     arrivals from its own Poisson process with mean 512 ms (so 2 ms for all
@@ -377,6 +441,8 @@ def run_served(args, device):
     from novaphy_gb300 import capi
 
     wl = workloads.served_scenes()
+    if ws > 1:  # this rank's clients, dealt by particle count; one server per GPU
+        wl = [wl[i] for i in shard.rank_scenes([w.n for w in wl], ws, rank)]
     dt = np.float32(wl[0].dt)
     T = float(args.serve_seconds)
     rng = np.random.default_rng(44)
@@ -390,6 +456,7 @@ def run_served(args, device):
             p.append((t, int(rng.choice([1, 4, 16]))))
         plans.append(p)
     demand = sum(wl[k].n * m for k in range(len(wl)) for _, m in plans[k])
+    coupled = [sphere_boundary(w, device) for w in wl]
 
     deadline_after = T + 90.0  # stop waiting for stragglers 90 s after the last arrival
 
@@ -411,8 +478,15 @@ def run_served(args, device):
             w = wl[k]
             st = capi.default_settings(**w.settings)
             r = np.random.default_rng(1000 + k)
+            cp = coupled[k]
+
+            def open_():
+                if cp is None:
+                    return srv.open_scene(st, w.x, w.v, w.mass, w.gravity)[0]
+                return srv.open_coupled_scene(st, w.x, w.v, w.mass, w.gravity, *cp)[0]
+
             try:
-                sid, _ = srv.open_scene(st, w.x, w.v, w.mass, w.gravity)
+                sid = open_()
                 left = int(r.geometric(1.0 / session_mean)) if session_mean else -1
                 mine = []
                 for (ta, m) in plans[k]:
@@ -423,7 +497,7 @@ def run_served(args, device):
                         wait_all(mine)
                         mine = []
                         srv.close_scene(sid)
-                        sid, _ = srv.open_scene(st, w.x, w.v, w.mass, w.gravity)
+                        sid = open_()
                         left = int(r.geometric(1.0 / session_mean))
                     mine.append(srv.submit(sid, float(dt), m))
                     left -= 1
@@ -441,7 +515,8 @@ def run_served(args, device):
         el = time.perf_counter() - t0
         stats = srv.stats()
         srv.close()
-        return {"value": stats["particle_steps"] / el, "unit": UNIT, "wall_s": el,
+        job_units, job_el = shard.job_throughput(stats["particle_steps"], el, dist)
+        return {"value": job_units / job_el, "unit": UNIT, "wall_s": el,
                 "particle_steps": stats["particle_steps"],
                 "step_ms_p50": stats["step_ms_p50"], "step_ms_p99": stats["step_ms_p99"],
                 "request_ms_p50": stats["request_ms_p50"],
@@ -461,14 +536,36 @@ def run_served(args, device):
                 "budget_bytes": int(cfg.hbm_budget_bytes)}
 
     def plain_run():
-        scenes = []
-        for w in wl:
+        scenes, rigid = [], []
+        for k, w in enumerate(wl):
             sc = capi.Scene(capi.default_settings(**w.settings), w.x, w.v, mass=w.mass,
                             device=device)
             sc.set_gravity(w.gravity)
             sc.step(float(dt), 1)  # warm-up: scratch and the step graph
             sc.reset(w.x, w.v)
+            cp = coupled[k]
+            st_b = None
+            if cp is not None:
+                local, body, psi, bodies = cp
+                sc.set_boundary(local, body, psi)
+                st_b = [{"p": np.array(b.pos, np.float32), "q": np.array(b.quat, np.float32),
+                         "v": np.zeros(3, np.float32), "w": np.zeros(3, np.float32),
+                         "inv_mass": np.float32(b.inv_mass),
+                         "ii": np.array(b.inv_inertia, np.float32).reshape(3, 3)} for b in bodies]
             scenes.append(sc)
+            rigid.append(st_b)
+
+        def plain_step(k):
+            sc, st_b = scenes[k], rigid[k]
+            if st_b is None:
+                sc.step(float(dt), 1)
+                return
+            nb = len(st_b)
+            sc.set_bodies(np.stack([b["p"] for b in st_b]), np.stack([b["q"] for b in st_b]),
+                          np.array([1 if b["inv_mass"] > 0 else 0 for b in st_b], np.int32))
+            f, t = sc.step_coupled(float(dt), np.zeros((nb, 3), np.float32),
+                                   np.zeros((nb, 3), np.float32))
+            rigid_step_np(st_b, f, t, np.asarray(wl[k].gravity, np.float32), dt)
         lat_step, lat_req = [], []
         done = [0]
         lock = threading.Lock()
@@ -486,7 +583,7 @@ def run_served(args, device):
                 prev = max(t0 + ta, time.perf_counter())
                 steps = []
                 for _ in range(m):
-                    sc.step(float(dt), 1)
+                    plain_step(k)
                     now = time.perf_counter()
                     steps.append((now - prev) * 1e3)
                     prev = now
@@ -503,7 +600,8 @@ def run_served(args, device):
         el = time.perf_counter() - t0
         for sc in scenes:
             sc.close()
-        return {"value": done[0] / el, "unit": UNIT, "wall_s": el, "particle_steps": done[0],
+        job_units, job_el = shard.job_throughput(done[0], el, dist)
+        return {"value": job_units / job_el, "unit": UNIT, "wall_s": el, "particle_steps": done[0],
                 "step_ms_p50": percentile(lat_step, 50), "step_ms_p99": percentile(lat_step, 99),
                 "request_ms_p50": percentile(lat_req, 50),
                 "request_ms_p99": percentile(lat_req, 99)}
@@ -524,13 +622,15 @@ def run_served(args, device):
     progress("served: plain")
     plain = plain_run()
     cpu = None
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and rank == 0:
         progress("served: cpu baseline")
         cpu = cpu_scene_pool(wl[:: max(1, len(wl) // (2 * (os.cpu_count() or 1)))])
     return {
         "workload": f"served_scenes: {len(wl)} clients, {sum(w.n for w in wl)} particles "
                     f"({min(w.n for w in wl)}-{max(w.n for w in wl)} per scene), dam breaks "
-                    f"and pools without rigid bodies, r = 0.02, h = 4r, 4 iterations, dt = 1/240, "
+                    f"and pools with {sum(len(w.meta['spheres']) for w in wl)} Akinci spheres in "
+                    f"{sum(1 for c in coupled if c is not None)} of them, r = 0.02, h = 4r, "
+                    f"4 iterations, dt = 1/240, "
                     f"s_corr k = 0.001 (PBFSettings default)",
         "arrivals": f"per-client Poisson, mean 512 ms (2 ms aggregate) over {T:.0f} s; "
                     f"k in {{1, 4, 16}}; {sum(len(p) for p in plans)} requests, "
@@ -778,7 +878,7 @@ def run_ours(args, ws, rank, local):
     batched = None
     if not args.no_batched:
         progress("batched scenes")
-        batched = run_batched(args, device)
+        batched = run_batched(args, device, ws, rank, dist)
     coupled = None
     if not args.no_coupled:
         progress("coupled scene")
@@ -786,7 +886,7 @@ def run_ours(args, ws, rank, local):
     served = None
     if not args.no_served:
         progress("served scenes")
-        served = run_served(args, device)
+        served = run_served(args, device, ws, rank, dist)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

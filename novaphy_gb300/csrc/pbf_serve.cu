@@ -16,6 +16,7 @@
 // grid (the share of the batch's offset table a launch holding it can use).
 // The batch scratch for max_batch_particles is reserved at creation.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -291,18 +292,18 @@ void issue_main(pbf_server* sv) {
     }
 }
 
-// Coupling and rigid step of coupled scenes whose PBF step just completed
+// Coupling and rigid step of one coupled scene whose PBF step just completed
 // (FluidWorld::step after the fluid step); called without the lock.  Only
-// the retire thread touches a scene's bodies while its `post` flag is set.
-void run_posts(pbf_server* sv, const std::vector<PostItem>& items) {
-    for (const PostItem& it : items) {
+// this call touches the scene's bodies while its `post` flag is set.
+void run_one_post(pbf_server* sv, const PostItem& it) {
+    {
         SceneRec* sc = nullptr;
         {
             std::lock_guard<std::mutex> lk(sv->mu);
             auto sit = sv->scenes.find(it.scene);
             if (sit != sv->scenes.end()) sc = &sit->second;
         }
-        if (!sc) continue;
+        if (!sc) return;
         const int nb = (int)sc->bodies.size();
         std::vector<float> f((size_t)3 * nb, 0.0f), tq((size_t)3 * nb, 0.0f);
         int rc = pbf_scene_couple(sc->s, it.dt, nb ? f.data() : nullptr, nb ? tq.data() : nullptr);
@@ -330,12 +331,33 @@ void run_posts(pbf_server* sv, const std::vector<PostItem>& items) {
         sc->post = false;
         if (rc) {
             fail_scene(sv, *sc, why, rc);
-            continue;
+            return;
         }
         auto rit = sv->reqs.find(it.req);
         if (rit != sv->reqs.end() && rit->second.state == PBF_REQ_PENDING)
             credit_step(sv, *sc, rit->second, t);
     }
+}
+
+// The post-passes of a retired launch, spread over up to kPostThreads host
+// threads so that the scenes' coupling kernels overlap on their own streams.
+constexpr size_t kPostThreads = 8;
+
+void run_posts(pbf_server* sv, const std::vector<PostItem>& items) {
+    const size_t nt = std::min(items.size(), kPostThreads);
+    if (nt <= 1) {
+        for (const PostItem& it : items) run_one_post(sv, it);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    pool.reserve(nt);
+    for (size_t k = 0; k < nt; ++k)
+        pool.emplace_back([&] {
+            cudaSetDevice(sv->device);
+            for (size_t i; (i = next.fetch_add(1)) < items.size();) run_one_post(sv, items[i]);
+        });
+    for (auto& t : pool) t.join();
 }
 
 // Waits for the oldest launch and retires its steps.

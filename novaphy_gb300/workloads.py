@@ -120,7 +120,9 @@ def served_scenes(nclients=256, seed=4, n_lo=1000, n_hi=200_000, r=0.02, dt=1.0 
     """One scene per client of a serving run, from ``default_rng(seed)``: a
     target count N = round(exp(U(ln n_lo, ln n_hi))); half dam breaks (a 1:1:2
     block in the corner of a box 3x its footprint and 1.5x its height), half
-    pools (a 2:2:1 block covering the floor of a box 2x its height).  h = 4r,
+    pools (a 2:2:1 block covering the floor of a box 2x its height), with 0-4
+    rigid spheres (radius 5r, density U(300, 1500)) above the fluid in
+    ``meta["spheres"]`` as (center, radius, density).  h = 4r,
     4 iterations, XSPH 0.01, vorticity 1e-4, and the s_corr defaults of
     PBFSettings (k = 0.001, dq = 0.3 h, n = 4): served scenes run hundreds of
     consecutive steps, and with k = 0.1 the fluid collapses into a few
@@ -147,5 +149,16 @@ def served_scenes(nclients=256, seed=4, n_lo=1000, n_hi=200_000, r=0.02, dt=1.0 
                       seed=int(rng.integers(0, 2**31)), vorticity=vorticity, steps=16,
                       name=f"client_{k}_{kind}")
         w.settings.update(corr_k=0.001, corr_delta_q=0.3)
+        # 0-4 Akinci spheres (radius 5r, density U(300, 1500)) above the fluid,
+        # spread over the box footprint: (center, radius, density) each.
+        spheres = []
+        rad = 5.0 * r
+        top = float(ext[2] + r / 2)
+        for j in range(int(rng.integers(0, 5))):
+            cx = float(rng.uniform(rad, box[0] - rad)) if box[0] > 2 * rad else box[0] / 2
+            cy = float(rng.uniform(rad, box[1] - rad)) if box[1] > 2 * rad else box[1] / 2
+            cz = min(top + 2.0 * rad * (1 + j % 2), box[2] - rad)
+            spheres.append(((cx, cy, max(cz, rad)), rad, float(rng.uniform(300.0, 1500.0))))
+        w.meta["spheres"] = spheres
         out.append(w)
     return out
