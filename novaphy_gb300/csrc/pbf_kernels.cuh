@@ -36,6 +36,35 @@ constexpr uint32_t kImpureBit = 0x80000000u;
 // e0 + (e1 + e2): the 3-term reduction order of Vector3f::squaredNorm.
 __device__ __forceinline__ float sqn(float x, float y, float z) { return x * x + (y * y + z * z); }
 
+// r = x_i - x_j of a candidate and sqn(r), with (r.x, r.y) as one paired
+// operation: fma(x_j, -1, x_i) rounds once, exactly as x_i - x_j, so the
+// result is the reference's subtraction bit for bit.  The exact build also
+// squares (r.x, r.y) as a pair; the _rn forms are never contracted, so the
+// sum keeps sqn's separately rounded terms.  With with_w, rw = x_i.w + x_j.w
+// (the lambda sum) comes from the same paired operation as r.z.
+template <bool with_w = false>
+__device__ __forceinline__ float rel_sq(const float4& xi, const float4& xj, float& rx, float& ry,
+                                        float& rz, float* rw = nullptr) {
+    const float2 dxy = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.0f, -1.0f),
+                                  make_float2(xi.x, xi.y));
+    rx = dxy.x;
+    ry = dxy.y;
+    if constexpr (with_w) {
+        const float2 dzw = __ffma2_rn(make_float2(xj.z, xj.w), make_float2(-1.0f, 1.0f),
+                                      make_float2(xi.z, xi.w));
+        rz = dzw.x;
+        *rw = dzw.y;
+    } else {
+        rz = xi.z - xj.z;
+    }
+#if PBF_FAST
+    return sqn(rx, ry, rz);
+#else
+    const float2 sq = __fmul2_rn(dxy, dxy);
+    return sq.x + (sq.y + rz * rz);
+#endif
+}
+
 __device__ __forceinline__ float poly6(float r_sq, const StepConsts& C) {
     if (r_sq >= C.h2) return 0.0f;
     const float diff = C.h2 - r_sq;
@@ -398,10 +427,8 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, const float4* xin,
     float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
         const float4 xj = ld_step<kPersist>(xin + q);
-        const float rx = xi.x - xj.x;
-        const float ry = xi.y - xj.y;
-        const float rz = xi.z - xj.z;
-        const float r_sq = sqn(rx, ry, rz);
+        float rx, ry, rz;
+        const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
             density += C.mass * poly6(r_sq, C);
             const float c = spiky_coeff(r_sq, C);
@@ -462,12 +489,9 @@ __device__ __forceinline__ void delta_at(uint32_t p, const float4* xin, float4* 
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
         const float4 xj = ld_step<kPersist>(xin + q);
-        const float rx = xi.x - xj.x;
-        const float ry = xi.y - xj.y;
-        const float rz = xi.z - xj.z;
-        const float r_sq = sqn(rx, ry, rz);
+        float rx, ry, rz, lambda_sum;
+        const float r_sq = rel_sq<true>(xi, xj, rx, ry, rz, &lambda_sum);
         if (r_sq < C.cut) {
-            const float lambda_sum = xi.w + xj.w;
             float s_corr = 0.0f;
             if (lambda_sum < -1e-10f && C.scorr_on) {
                 float ratio = poly6(r_sq, C) / C.w_dq;
@@ -622,10 +646,8 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
         float cx = 0.0f, cy = 0.0f, cz = 0.0f;
         for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
             const float4 xj = __ldg(xin + q);
-            const float rx = xi.x - xj.x;
-            const float ry = xi.y - xj.y;
-            const float rz = xi.z - xj.z;
-            const float r_sq = sqn(rx, ry, rz);
+            float rx, ry, rz;
+            const float r_sq = rel_sq(xi, xj, rx, ry, rz);
             if (r_sq < C.h2) {
                 const float4 vj = __ldg(sv + q);
                 const float w = poly6(r_sq, C);
@@ -658,10 +680,8 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
     float cx = 0.0f, cy = 0.0f, cz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
         const float4 xj = __ldg(xin + q);
-        const float rx = xi.x - xj.x;
-        const float ry = xi.y - xj.y;
-        const float rz = xi.z - xj.z;
-        const float r_sq = sqn(rx, ry, rz);
+        float rx, ry, rz;
+        const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
             const float4 vj = __ldg(sv + q);
             const float ux = vj.x - vi.x;
@@ -706,10 +726,8 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     for_each_candidate(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
         const float4 xj = __ldg(xin + q);
-        const float rx = xi.x - xj.x;
-        const float ry = xi.y - xj.y;
-        const float rz = xi.z - xj.z;
-        const float r_sq = sqn(rx, ry, rz);
+        float rx, ry, rz;
+        const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
             const float c = spiky_coeff(r_sq, C);
             const float a = __ldg(sv + q).w * (__ldg(som + q).w - wi.w);
