@@ -356,7 +356,8 @@ typedef struct pbf_server_stats {
     long long queue_depth;    /* requests submitted and not finished */
     /* Step latency: from the later of a request's submission and its
      * previous step's completion to this step's completion.  Request
-     * latency: submission to last step's completion.  Host clock, ms. */
+     * latency: submission to last step's completion.  Host clock, ms;
+     * percentiles of a fixed-memory log histogram, within 0.25 % of exact. */
     double step_ms_p50, step_ms_p99;
     double request_ms_p50, request_ms_p99;
     double particle_steps_per_s; /* first submission to last completion */
@@ -391,7 +392,9 @@ int pbf_server_submit(pbf_server* server, long long scene_id, float dt, int nste
                       long long* request_id);
 /* Waits up to timeout_s seconds (< 0: no limit) for a request; *state_out is
  * its pbf_request_state.  PBF_ERR_TIMEOUT if still pending; a failed request
- * returns its failure status, with the reason in pbf_last_error(). */
+ * returns its failure status, with the reason in pbf_last_error().  The
+ * server keeps the records of the latest 65536 finished requests; waiting on
+ * an older finished request returns PBF_ERR_INVALID_ARG. */
 int pbf_server_wait(pbf_server* server, long long request_id, double timeout_s, int* state_out);
 /* A rigid body of a served coupled scene: the state the host rigid step of
  * World integrates (free bodies, no contacts; src/dynamics/integrator.cpp).

@@ -73,7 +73,12 @@ struct TuneState {
     int next = 0;              // next choice to try
     int pending = -1;          // choice whose timing is in flight
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    double ms[kNumChoices] = {};
+    // A trial whose step failed before its timing was recorded keeps +inf
+    // and is never chosen.
+    double ms[kNumChoices];
+    TuneState() {
+        for (double& m : ms) m = 1e30;
+    }
 };
 
 }  // namespace
@@ -119,8 +124,10 @@ struct pbf_batch {
     int persist_blocks[2] = {-1, -1};  // co-resident grid per build (fast, exact)
     unsigned int* barrier = nullptr;   // grid barrier words
 
-    cudaGraphExec_t graph = nullptr;
-    GraphKey key{};
+    // One cached step graph per arithmetic build (index: exact), so a call
+    // that steps scenes of both builds does not recapture every group.
+    cudaGraphExec_t graph[2] = {};
+    GraphKey key[2];
     long long captures = 0, updates = 0, instantiations = 0;
 
     // Autotuner (off by default): per class of batch shape.
@@ -134,11 +141,11 @@ struct pbf_batch {
 namespace {
 
 void drop_graph(pbf_batch* b) {
-    if (b->graph) {
-        cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
+    for (int k = 0; k < 2; ++k) {
+        if (b->graph[k]) cudaGraphExecDestroy(b->graph[k]);
+        b->graph[k] = nullptr;
+        b->key[k] = GraphKey{};
     }
-    b->key = GraphKey{};
 }
 
 size_t extra_bytes(int c) {
@@ -316,20 +323,25 @@ Choice pick_choice(pbf_batch* b, const std::string& cls, int* trial) {
         else
             t.ms[t.pending] = 1e30;
         t.pending = -1;
-        if (t.next >= kNumChoices) {
-            int best = 0;
-            for (int k = 1; k < kNumChoices; ++k)
-                if (t.ms[k] < t.ms[best]) best = k;
-            t.done = true;
+    }
+    if (!t.done && t.next >= kNumChoices) {
+        // Every choice was tried (a trial whose step failed kept +inf).
+        int best = 0;
+        for (int k = 1; k < kNumChoices; ++k)
+            if (t.ms[k] < t.ms[best]) best = k;
+        t.done = true;
+        if (t.ms[best] < 1e30) {
             t.best = kChoices[best];
             t.best_ms = t.ms[best];
             save_tuning(b, cls, t);
         }
     }
     if (t.done) return t.best;
-    if (!t.e0) {
-        cudaEventCreate(&t.e0);
-        cudaEventCreate(&t.e1);
+    if (!t.e0 && (cudaEventCreate(&t.e0) != cudaSuccess || cudaEventCreate(&t.e1) != cudaSuccess)) {
+        // No timing events: keep the default choice and stop tuning this class.
+        cudaGetLastError();
+        t.done = true;
+        return t.best;
     }
     *trial = t.next++;
     return kChoices[*trial];
@@ -459,7 +471,8 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
     key.any_vort = any_vort;
     key.any_plain = any_plain;
     key.xsph_on = xsph_on;
-    if (!b->graph || !(key == b->key)) {
+    cudaGraphExec_t& graph = b->graph[exact];
+    if (!graph || !(key == b->key[exact])) {
         ++b->captures;
         cudaGraph_t g = nullptr;
         PBF_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -471,31 +484,31 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
         }
         if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
         bool updated = false;
-        if (b->graph) {
+        if (graph) {
             // Same launch topology with new sizes: update the parameters in place.
             cudaGraphExecUpdateResultInfo info{};
-            updated = cudaGraphExecUpdate(b->graph, g, &info) == cudaSuccess;
+            updated = cudaGraphExecUpdate(graph, g, &info) == cudaSuccess;
             if (updated) ++b->updates;
             if (!updated) {
                 cudaGetLastError();
-                cudaGraphExecDestroy(b->graph);
-                b->graph = nullptr;
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
             }
         }
         if (!updated) {
             ++b->instantiations;
-            ce = cudaGraphInstantiate(&b->graph, g, 0);
+            ce = cudaGraphInstantiate(&graph, g, 0);
             if (ce != cudaSuccess) {
                 cudaGraphDestroy(g);
-                b->graph = nullptr;
+                graph = nullptr;
                 return cuda_fail(ce, "cudaGraphInstantiate");
             }
         }
         cudaGraphDestroy(g);
-        b->key = key;
+        b->key[exact] = key;
     }
     if (ts) PBF_CUDA(cudaEventRecord(ts->e0, b->stream));
-    PBF_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    PBF_CUDA(cudaGraphLaunch(graph, b->stream));
     if (ts) {
         PBF_CUDA(cudaEventRecord(ts->e1, b->stream));
         ts->pending = trial;

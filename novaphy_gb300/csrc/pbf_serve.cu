@@ -29,6 +29,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "latency_hist.hpp"
 #include "pbf_internal.cuh"
 #include "rigid_step.hpp"
 
@@ -38,6 +39,9 @@ using namespace pbf::capi;
 namespace {
 
 constexpr size_t kGridBytesPerSlot = 5;  // one offset word + one alias byte
+// Records of finished requests kept for pbf_server_wait; older ones are
+// dropped, so a long-running server holds bounded host memory.
+constexpr size_t kFinishedKept = (size_t)1 << 16;
 // Device bytes per boundary particle of a coupled scene: local, world and force
 // float4s, body index, query cell and classification row, boundary index.
 constexpr size_t kBoundaryBytes = 256;
@@ -93,14 +97,6 @@ struct Launch {
     long long particles = 0;
 };
 
-double pct(std::vector<double> v, double q) {
-    if (v.empty()) return 0.0;
-    std::sort(v.begin(), v.end());
-    const double pos = q / 100.0 * (double)(v.size() - 1);
-    const size_t lo = (size_t)std::floor(pos), hi = std::min(lo + 1, v.size() - 1);
-    return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
-}
-
 }  // namespace
 
 struct pbf_server {
@@ -117,6 +113,7 @@ struct pbf_server {
     std::map<long long, SceneRec> scenes;
     std::deque<long long> admit_queue;
     std::unordered_map<long long, ReqRec> reqs;
+    std::deque<long long> finished;  // ids of finished requests, oldest first
     long long next_scene = 1, next_req = 1;
     size_t charged = 0;
 
@@ -131,7 +128,7 @@ struct pbf_server {
               launch_particles = 0;
     double t_first = -1.0, t_last = 0.0;
     double issue_ms = 0.0;  // host time spent issuing launches
-    std::vector<double> step_ms, req_ms;
+    pbf_stats::LatencyHist step_ms, req_ms;
 };
 
 namespace {
@@ -141,12 +138,34 @@ size_t charge_of(int n, uint32_t slots) {
     return (size_t)n * kStateBytesPerParticle + (size_t)slots * kGridBytesPerSlot;
 }
 
+// Records that request `id` reached a final state, dropping the oldest
+// finished records beyond kFinishedKept.
+void note_finished(pbf_server* sv, long long id) {
+    sv->finished.push_back(id);
+    while (sv->finished.size() > kFinishedKept) {
+        sv->reqs.erase(sv->finished.front());
+        sv->finished.pop_front();
+    }
+}
+
 void fail_request(pbf_server* sv, ReqRec& r, const std::string& why, int code) {
     if (r.state != PBF_REQ_PENDING) return;
     r.state = PBF_REQ_FAILED;
     r.why = why;
     r.code = code;
     ++sv->failed_reqs;
+    note_finished(sv, r.id);
+}
+
+// The request record of id, or nullptr when it does not exist (any more).
+ReqRec* find_req(pbf_server* sv, long long id) {
+    auto it = sv->reqs.find(id);
+    return it == sv->reqs.end() ? nullptr : &it->second;
+}
+
+bool req_pending(pbf_server* sv, long long id) {
+    const ReqRec* r = find_req(sv, id);
+    return r && r->state == PBF_REQ_PENDING;
 }
 
 // code: PBF_ERR_NONFINITE for a non-finite state, else the failing call's.
@@ -156,11 +175,11 @@ void fail_scene(pbf_server* sv, SceneRec& sc, const std::string& why, int code) 
     sc.why = why;
     sc.code = code;
     ++sv->failed_scenes;
-    for (long long rid : sc.reqs) {
-        auto it = sv->reqs.find(rid);
-        if (it != sv->reqs.end()) fail_request(sv, it->second, "its scene failed: " + why, code);
-    }
+    // Collect first: failing a request may drop older finished records.
+    const std::vector<long long> ids(sc.reqs.begin(), sc.reqs.end());
     sc.reqs.clear();
+    for (long long rid : ids)
+        if (ReqRec* r = find_req(sv, rid)) fail_request(sv, *r, "its scene failed: " + why, code);
 }
 
 void credit_step(pbf_server* sv, SceneRec& sc, ReqRec& r, double t);
@@ -197,14 +216,15 @@ void credit_step(pbf_server* sv, SceneRec& sc, ReqRec& r, double t) {
     ++r.done;
     ++sv->steps_done;
     sv->particle_steps += sc.n;
-    sv->step_ms.push_back(t - r.t_prev);
+    sv->step_ms.add(t - r.t_prev);
     r.t_prev = t;
     sv->t_last = t;
     if (r.done == r.nsteps) {
         r.state = PBF_REQ_DONE;
         ++sv->done_reqs;
-        sv->req_ms.push_back(t - r.t_submit);
+        sv->req_ms.add(t - r.t_submit);
         if (!sc.reqs.empty() && sc.reqs.front() == r.id) sc.reqs.pop_front();
+        note_finished(sv, r.id);  // last: may drop the record r refers to
     }
 }
 
@@ -222,9 +242,9 @@ bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
         if (sc.state != PBF_SCENE_RESIDENT || !sc.s || sc.busy) continue;
         if (sc.coupled && (sc.inflight > 0 || sc.post)) continue;  // one step at a time
         for (long long rid : sc.reqs) {
-            ReqRec& r = sv->reqs[rid];
-            if (r.state == PBF_REQ_PENDING && r.issued < r.nsteps) {
-                cand.push_back({r.t_submit, &sc, &r});
+            ReqRec* r = find_req(sv, rid);
+            if (r && r->state == PBF_REQ_PENDING && r->issued < r->nsteps) {
+                cand.push_back({r->t_submit, &sc, r});
                 break;
             }
         }
@@ -545,7 +565,11 @@ int pbf_server_destroy(pbf_server* sv) {
     if (sv->retirer.joinable()) sv->retirer.join();
     {
         std::lock_guard<std::mutex> lk(sv->mu);
-        for (auto& kv : sv->reqs) fail_request(sv, kv.second, "the server stopped", PBF_ERR_INVALID_ARG);
+        std::vector<long long> pending;
+        for (auto& kv : sv->reqs)
+            if (kv.second.state == PBF_REQ_PENDING) pending.push_back(kv.first);
+        for (long long rid : pending)
+            if (ReqRec* r = find_req(sv, rid)) fail_request(sv, *r, "the server stopped", PBF_ERR_INVALID_ARG);
     }
     sv->cv_done.notify_all();
     {
@@ -670,21 +694,16 @@ int pbf_server_close_scene(pbf_server* sv, long long id) {
         const SceneRec& sc = i2->second;
         if (sc.busy) return false;
         if (sc.state == PBF_SCENE_WAITING) return true;
-        bool pending = false;
-        for (long long rid : sc.reqs) {
-            auto r = sv->reqs.find(rid);
-            if (r != sv->reqs.end() && r->second.state == PBF_REQ_PENDING) pending = true;
-        }
-        return !pending && sc.inflight == 0 && !sc.post;
+        for (long long rid : sc.reqs)
+            if (req_pending(sv, rid)) return false;
+        return sc.inflight == 0 && !sc.post;
     });
     it = sv->scenes.find(id);
     if (it == sv->scenes.end()) return PBF_OK;
     SceneRec rec = std::move(it->second);
     sv->scenes.erase(it);
-    for (long long rid : rec.reqs) {
-        auto r = sv->reqs.find(rid);
-        if (r != sv->reqs.end()) fail_request(sv, r->second, "its scene was closed", PBF_ERR_INVALID_ARG);
-    }
+    for (long long rid : rec.reqs)
+        if (ReqRec* r = find_req(sv, rid)) fail_request(sv, *r, "its scene was closed", PBF_ERR_INVALID_ARG);
     if (rec.state == PBF_SCENE_WAITING) {
         sv->admit_queue.erase(std::remove(sv->admit_queue.begin(), sv->admit_queue.end(), id),
                               sv->admit_queue.end());
@@ -720,16 +739,17 @@ int pbf_server_submit(pbf_server* sv, long long scene, float dt, int nsteps, lon
     r.t_submit = r.t_prev = t;
     ++sv->submitted;
     if (sv->t_first < 0.0) sv->t_first = t;
+    *req_out = id;
     if (nsteps == 0 || sc.n == 0) {  // nothing to run (pbf_solver.cpp:21)
         r.state = PBF_REQ_DONE;
         ++sv->done_reqs;
-        sv->req_ms.push_back(0.0);
+        sv->req_ms.add(0.0);
+        note_finished(sv, id);
         sv->cv_done.notify_all();
     } else {
         sc.reqs.push_back(id);
         sv->cv_work.notify_one();
     }
-    *req_out = id;
     return PBF_OK;
 }
 
@@ -737,24 +757,26 @@ int pbf_server_wait(pbf_server* sv, long long rid, double timeout_s, int* state_
     int rc = check_server(sv);
     if (rc) return rc;
     std::unique_lock<std::mutex> lk(sv->mu);
-    auto it = sv->reqs.find(rid);
-    if (it == sv->reqs.end()) return fail(PBF_ERR_INVALID_ARG, "no such request");
-    auto done = [&] { return sv->reqs[rid].state != PBF_REQ_PENDING; };
+    const char* gone = "no such request (records of all but the latest 65536 finished requests are dropped)";
+    if (!find_req(sv, rid)) return fail(PBF_ERR_INVALID_ARG, gone);
+    auto done = [&] { return !req_pending(sv, rid); };
     if (timeout_s < 0.0) {
         sv->cv_done.wait(lk, done);
     } else if (!sv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
         if (state_out) *state_out = PBF_REQ_PENDING;
         return fail(PBF_ERR_TIMEOUT, "the request is still pending");
     }
-    const ReqRec& r = sv->reqs[rid];
-    if (state_out) *state_out = r.state;
-    if (r.state == PBF_REQ_FAILED) return fail(r.code, "the request failed: " + r.why);
+    const ReqRec* r = find_req(sv, rid);
+    if (!r) return fail(PBF_ERR_INVALID_ARG, gone);
+    if (state_out) *state_out = r->state;
+    if (r->state == PBF_REQ_FAILED) return fail(r->code, "the request failed: " + r->why);
     return PBF_OK;
 }
 
 int pbf_server_read(pbf_server* sv, long long id, int field, float* out) {
     int rc = check_server(sv);
     if (rc) return rc;
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "output is NULL");
     pbf_scene* s = nullptr;
     {
         std::unique_lock<std::mutex> lk(sv->mu);
@@ -764,7 +786,7 @@ int pbf_server_read(pbf_server* sv, long long id, int field, float* out) {
             const SceneRec& sc = i2->second;
             if (sc.busy) return false;
             for (long long r : sc.reqs)
-                if (sv->reqs[r].state == PBF_REQ_PENDING) return false;
+                if (req_pending(sv, r)) return false;
             return sc.inflight == 0 && !sc.post;
         };
         sv->cv_done.wait(lk, idle);
@@ -811,7 +833,7 @@ int pbf_server_read_bodies(pbf_server* sv, long long id, pbf_rigid_body* out) {
         const SceneRec& sc = it->second;
         if (sc.busy || sc.post || sc.inflight > 0) return false;
         for (long long r : sc.reqs)
-            if (sv->reqs[r].state == PBF_REQ_PENDING) return false;
+            if (req_pending(sv, r)) return false;
         return true;
     });
     auto it = sv->scenes.find(id);
@@ -852,10 +874,10 @@ int pbf_server_get_stats(pbf_server* sv, pbf_server_stats* out) {
     s.particle_steps = sv->particle_steps;
     s.launches = sv->launches;
     s.queue_depth = sv->submitted - sv->done_reqs - sv->failed_reqs;
-    s.step_ms_p50 = pct(sv->step_ms, 50.0);
-    s.step_ms_p99 = pct(sv->step_ms, 99.0);
-    s.request_ms_p50 = pct(sv->req_ms, 50.0);
-    s.request_ms_p99 = pct(sv->req_ms, 99.0);
+    s.step_ms_p50 = sv->step_ms.percentile(50.0);
+    s.step_ms_p99 = sv->step_ms.percentile(99.0);
+    s.request_ms_p50 = sv->req_ms.percentile(50.0);
+    s.request_ms_p99 = sv->req_ms.percentile(99.0);
     const double span = sv->t_last - sv->t_first;
     s.particle_steps_per_s = (sv->t_first >= 0.0 && span > 0.0)
                                  ? (double)sv->particle_steps / (span / 1e3)
@@ -890,6 +912,7 @@ int pbf_server_reset_stats(pbf_server* sv) {
         if (it->second.state != PBF_REQ_PENDING) it = sv->reqs.erase(it);
         else ++it;
     }
+    sv->finished.clear();
     return PBF_OK;
 }
 

@@ -306,3 +306,22 @@ def test_coupled_served_scene_equals_fluid_world():
                               np.asarray(fw.state.angular_velocities[k], np.float32)), k
     assert out[0].pos[1] != 0.25  # the sphere moved
     srv.close()
+
+
+def test_finished_request_records_are_bounded():
+    # Zero-step requests finish at submission: no device work, only records.
+    w = small_scenes(k=1)[0]
+    srv = capi.Server()
+    sid, _ = srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)
+    kept = 1 << 16
+    ids = [srv.submit(sid, w.dt, 0) for _ in range(kept + 10)]
+    assert srv.wait(ids[-1]) == capi.REQ_DONE
+    assert srv.wait(ids[10]) == capi.REQ_DONE  # the oldest record still kept
+    with pytest.raises(capi.PbfError):
+        srv.wait(ids[0])  # dropped
+    q = srv.submit(sid, w.dt, 2)  # real steps still run and report
+    assert srv.wait(q) == capi.REQ_DONE
+    st = srv.stats()
+    assert st["requests_done"] == kept + 11 and st["steps_done"] == 2
+    srv.close_scene(sid)
+    srv.close()
