@@ -430,7 +430,9 @@ def run_served(args, device, ws=1, rank=0, dist=None):
     clients together) and asks for k in {1, 4, 16} steps.
 
     served: requests go to the serving loop (pbf_server_*, continuous
-    batching).  Run at the full HBM budget and at a reduced budget sized to
+    batching).  Run at the full HBM budget; again with arrivals thinned to
+    about half of the throughput the first run measured (latency without an
+    overload's backlog); and at a reduced budget sized to
     half of the scenes' charged bytes, where client sessions of 8 requests
     on average close their scene and open a fresh one so that waiting scenes
     get admitted.  plain: each client steps its own scene with the drop-in
@@ -445,22 +447,30 @@ def run_served(args, device, ws=1, rank=0, dist=None):
         wl = [wl[i] for i in shard.rank_scenes([w.n for w in wl], ws, rank)]
     dt = np.float32(wl[0].dt)
     T = float(args.serve_seconds)
-    rng = np.random.default_rng(44)
-    plans = []
-    for k in range(len(wl)):
-        t, p = 0.0, []
-        while True:
-            t += float(rng.exponential(0.512))
-            if t >= T:
-                break
-            p.append((t, int(rng.choice([1, 4, 16]))))
-        plans.append(p)
-    demand = sum(wl[k].n * m for k in range(len(wl)) for _, m in plans[k])
+
+    def make_plans(mean_s, seed):
+        rng = np.random.default_rng(seed)
+        out = []
+        for k in range(len(wl)):
+            t, p = 0.0, []
+            while True:
+                t += float(rng.exponential(mean_s))
+                if t >= T:
+                    break
+                p.append((t, int(rng.choice([1, 4, 16]))))
+            out.append(p)
+        return out
+
+    def demand_of(pl):
+        return sum(wl[k].n * m for k in range(len(wl)) for _, m in pl[k])
+
+    plans = make_plans(0.512, 44)
+    demand = demand_of(plans)
     coupled = [sphere_boundary(w, device) for w in wl]
 
     deadline_after = T + 90.0  # stop waiting for stragglers 90 s after the last arrival
 
-    def served_run(budget=None, session_mean=None, max_batch=16 << 20):
+    def served_run(budget=None, session_mean=None, max_batch=16 << 20, plans=plans):
         cfg = capi.server_config(max_batch_particles=max_batch)
         if budget is not None:
             cfg.hbm_budget_bytes = int(budget)
@@ -608,8 +618,18 @@ def run_served(args, device, ws=1, rank=0, dist=None):
 
     progress("served: full budget")
     full = served_run(max_batch=args.served_max_batch)
+    # The same clients at about half of this rank's measured throughput, so
+    # that latencies show service time rather than the backlog of an overload.
+    own_rate = full["particle_steps"] / max(full["wall_s"], 1e-9)
+    mean_half = 0.512 * (demand / T) / max(0.5 * own_rate, 1.0)
+    plans_half = make_plans(mean_half, 45)
+    progress("served: half load")
+    half = served_run(max_batch=args.served_max_batch, plans=plans_half)
+    half["arrivals"] = (f"per-client Poisson, mean {mean_half * 1e3:.0f} ms, "
+                        f"{sum(len(p) for p in plans_half)} requests")
+    half["offered_fraction_of_capacity"] = demand_of(plans_half) / T / max(own_rate, 1.0)
     if args.served_full_only:
-        return {"value": full["value"], "unit": UNIT, "full_budget": full,
+        return {"value": full["value"], "unit": UNIT, "full_budget": full, "half_load": half,
                 "max_batch_particles": args.served_max_batch}
     total_charge = sum(w.n for w in wl) * capi.state_bytes_per_particle()
     small_batch = 1 << 20
@@ -640,7 +660,7 @@ def run_served(args, device, ws=1, rank=0, dist=None):
         "step_ms_p50": full["step_ms_p50"], "step_ms_p99": full["step_ms_p99"],
         "request_ms_p50": full["request_ms_p50"], "request_ms_p99": full["request_ms_p99"],
         "speedup_vs_plain": full["value"] / plain["value"],
-        "full_budget": full, "reduced_budget": reduced, "plain": plain,
+        "full_budget": full, "half_load": half, "reduced_budget": reduced, "plain": plain,
         "cpu_baseline": cpu,
     }
 
