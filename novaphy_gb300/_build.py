@@ -51,7 +51,8 @@ def nvcc() -> str:
 
 
 def _deps(src: str) -> list[str]:
-    out = [src]
+    # This file holds the compiler flags: editing it rebuilds everything.
+    out = [src, os.path.abspath(__file__)]
     for d in (CSRC, INCLUDE, HOST):
         if os.path.isdir(d):
             out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".cuh", ".h", ".hpp"))]
