@@ -55,7 +55,8 @@ typedef struct pbf_settings {
     /* --- extensions (not in the reference) --- */
     int exact_arithmetic; /* 1 (default): reference operation order with no
                              fused multiply-add and IEEE div/sqrt (bit-exact
-                             with the reference); 0: FMA + rsqrt fast path */
+                             with the reference); 0: fast path (FMA, rsqrt,
+                             approximate division) */
     int hash_compat;      /* 1 (default): reproduce the reference's XOR-hash
                              bucket merging (neighbor_search.cpp:89-97),
                              including double-visited buckets; 0: plain

@@ -36,7 +36,7 @@ NVCC_COMMON = [
 # Per-file arithmetic flags: the exact build must not contract a*b+c.
 CU_FLAGS = {
     "pbf_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
-    "pbf_fast.cu": ["-fmad=true", "-ftz=false"],
+    "pbf_fast.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=false"],
     "pbf_boundary.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
 }
 CU_SOURCES = ["radix_sort.cu", "pbf_exact.cu", "pbf_fast.cu", "pbf_boundary.cu", "pbf_capi.cu",

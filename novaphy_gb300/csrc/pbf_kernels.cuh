@@ -2,8 +2,8 @@
 //   pbf_exact.cu: PBF_FAST=0, built with -fmad=false and IEEE div/sqrt, so
 //                 every expression below rounds exactly like the reference's
 //                 float code (pbf_solver.cpp, sph_kernel.h) term by term;
-//   pbf_fast.cu:  PBF_FAST=1, built with FMA contraction and rsqrt in the
-//                 spiky gradient.
+//   pbf_fast.cu:  PBF_FAST=1, built with FMA contraction, approximate
+//                 division and square root, and rsqrt in the spiky gradient.
 // Summation order is the reference's in both builds: for particle i the
 // candidates are visited bucket by bucket over the 27 neighbour cells in
 // (dz, dy, dx) order and, inside a bucket, by ascending particle index
