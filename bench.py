@@ -540,6 +540,7 @@ def run_served(args, device, ws=1, rank=0, dist=None):
                 "issue_ms_mean": stats["issue_ms_mean"],
                 "graph_captures": stats["graph_captures"], "graph_updates": stats["graph_updates"],
                 "graph_instantiations": stats["graph_instantiations"],
+                "launches_direct": stats["launches_direct"],
                 "mean_launch_particles": stats["mean_launch_particles"],
                 "scenes_rejected": stats["scenes_rejected"],
                 "hbm_bytes_scratch": stats["hbm_bytes_scratch"],

@@ -371,6 +371,8 @@ typedef struct pbf_server_stats {
     long long graph_captures;        /* step graphs captured (new launch shapes) */
     long long graph_updates;         /* ... applied to the instantiated graph in place */
     long long graph_instantiations;  /* ... instantiated anew */
+    long long launches_direct;       /* step launches issued without a graph (a
+                                        shape is captured when seen twice in a row) */
 } pbf_server_stats;
 
 /* Defaults: 120 GB budget, 16M particles and 1024 scenes per launch, 2
@@ -415,9 +417,10 @@ typedef struct pbf_rigid_body {
  * pbf_boundary_volumes) owned by nbodies rigid bodies.  Each served step of
  * it is FluidWorld::step (src/fluid/fluid_world.cpp:46-99): the PBF step,
  * batched with the other scenes; the coupling (pbf_scene_couple); then the
- * host rigid step of the bodies under gravity and the coupling forces, before
- * the scene's next step.  The scene is charged its own step scratch too,
- * which the coupling uses. */
+ * rigid step of the bodies under gravity and the coupling forces (World's
+ * semi-implicit Euler of free bodies, run on the device with the same float
+ * operations), before the scene's next step.  The scene is charged its own
+ * step scratch too, which the coupling uses. */
 int pbf_server_open_coupled_scene(pbf_server* server, const pbf_settings* settings, int n,
                                   const float* x3, const float* v3, float mass,
                                   const float* gravity3, int nb, const float* local3,

@@ -128,6 +128,11 @@ struct pbf_batch {
     // that steps scenes of both builds does not recapture every group.
     cudaGraphExec_t graph[2] = {};
     GraphKey key[2];
+    // A shape is captured the second time in a row it is seen; a shape seen
+    // once (a serving loop's launches change shape nearly every time) is
+    // launched directly, which costs far less host time than a capture.
+    GraphKey seen[2];
+    long long direct = 0;
     long long captures = 0, updates = 0, instantiations = 0;
 
     // Autotuner (off by default): per class of batch shape.
@@ -472,7 +477,20 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
     key.any_plain = any_plain;
     key.xsph_on = xsph_on;
     cudaGraphExec_t& graph = b->graph[exact];
-    if (!graph || !(key == b->key[exact])) {
+    const bool cached = graph && key == b->key[exact];
+    if (!cached && !(key == b->seen[exact])) {
+        b->seen[exact] = key;
+        ++b->direct;
+        if (ts) PBF_CUDA(cudaEventRecord(ts->e0, b->stream));
+        cudaError_t e = enqueue(b->stream, nullptr);
+        if (e != cudaSuccess) return cuda_fail(e, "batch step");
+        if (ts) {
+            PBF_CUDA(cudaEventRecord(ts->e1, b->stream));
+            ts->pending = trial;
+        }
+        return PBF_OK;
+    }
+    if (!cached) {
         ++b->captures;
         cudaGraph_t g = nullptr;
         PBF_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -640,7 +658,8 @@ int batch_launch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const floa
 }
 
 void batch_counters(const pbf_batch* b, long long* captures, long long* updates,
-                    long long* instantiations) {
+                    long long* instantiations, long long* direct) {
+    *direct = b->direct;
     *captures = b->captures;
     *updates = b->updates;
     *instantiations = b->instantiations;

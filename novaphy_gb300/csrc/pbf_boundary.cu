@@ -5,6 +5,7 @@
 #define PBF_NS bnd
 #include "pbf_boundary.cuh"
 #include "pbf_kernels.cuh"
+#include "rigid_step.hpp"
 
 namespace pbf {
 namespace bnd {
@@ -169,6 +170,32 @@ __global__ void k_body_reduce(const float4* __restrict__ Fb, const float4* __res
     torque3[3 * k + 2] = t2;
 }
 
+// One thread per body (rigid_step.hpp on the device).
+__global__ void k_rigid_step(pbf_rigid_body* __restrict__ bodies, int nbodies,
+                             const float* __restrict__ force3, const float* __restrict__ torque3,
+                             int nforce, float gx, float gy, float gz, float dt,
+                             float4* __restrict__ body_pos, float4* __restrict__ body_quat) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nbodies) return;
+    pbf_rigid_body r = bodies[k];
+    if (r.inv_mass > 0.0f) {
+        const float g[3] = {gx, gy, gz};
+        float f[3] = {0.0f, 0.0f, 0.0f}, t[3] = {0.0f, 0.0f, 0.0f};
+        if (k < nforce)
+            for (int d = 0; d < 3; ++d) {
+                f[d] = force3[3 * k + d];
+                t[d] = torque3[3 * k + d];
+            }
+        pbf_rigid::integrate_velocity(r.lin_vel, r.ang_vel, g, f, r.inv_mass, r.inv_inertia, t, dt);
+        pbf_rigid::integrate_position(r.pos, r.quat, r.lin_vel, r.ang_vel, dt);
+        bodies[k] = r;
+    }
+    if (k < nforce) {
+        body_pos[k] = make_float4(r.pos[0], r.pos[1], r.pos[2], 0.0f);
+        body_quat[k] = make_float4(r.quat[0], r.quat[1], r.quat[2], r.quat[3]);
+    }
+}
+
 __global__ void __launch_bounds__(kBlock)
 k_volumes(const float4* __restrict__ world, int nb, const QuerySet Q, const PointIndex I,
           float* __restrict__ psi, const StepConsts C) {
@@ -260,6 +287,16 @@ cudaError_t body_reduce(const float4* Fb, const float4* bworld, const int* list_
     if (nbodies <= 0) return cudaSuccess;
     k_body_reduce<<<grid_of(nbodies, 32), 32, 0, st>>>(Fb, bworld, list_off, list, body_pos,
                                                        nbodies, force3, torque3);
+    return cudaGetLastError();
+}
+
+cudaError_t rigid_step(pbf_rigid_body* bodies, int nbodies, const float* force3,
+                       const float* torque3, int nforce, float gx, float gy, float gz, float dt,
+                       float4* body_pos, float4* body_quat, cudaStream_t st) {
+    using namespace bnd;
+    if (nbodies <= 0) return cudaSuccess;
+    k_rigid_step<<<grid_of(nbodies, 32), 32, 0, st>>>(bodies, nbodies, force3, torque3, nforce, gx,
+                                                      gy, gz, dt, body_pos, body_quat);
     return cudaGetLastError();
 }
 

@@ -7,6 +7,7 @@
 
 #include <cstdint>
 
+#include "novaphy_pbf.h"
 #include "pbf_types.cuh"
 #include "radix_sort.cuh"
 
@@ -70,6 +71,15 @@ cudaError_t coupling_forces(const float4* bworld, const int* body, const int* bo
 cudaError_t body_reduce(const float4* Fb, const float4* bworld, const int* list_off,
                         const int* list, const float4* body_pos, int nbodies, float* force3,
                         float* torque3, cudaStream_t st);
+
+// Rigid step of the bodies with inv_mass > 0 under gravity g and the coupling
+// force/torque of the step (force3/torque3 hold the first nforce bodies; the
+// others receive none), then the new poses of the first nforce bodies into
+// body_pos/body_quat for the next step's boundary positions.  The same float
+// operations as the host rigid step (rigid_step.hpp).
+cudaError_t rigid_step(pbf_rigid_body* bodies, int nbodies, const float* force3,
+                       const float* torque3, int nforce, float gx, float gy, float gz, float dt,
+                       float4* body_pos, float4* body_quat, cudaStream_t st);
 
 // psi_b = 1 / sum_b' poly6 (0 when the sum <= 1e-10), boundary.cpp:152-176.
 cudaError_t boundary_volumes(const float4* world, int nb, const QuerySet& Q, const PointIndex& I,

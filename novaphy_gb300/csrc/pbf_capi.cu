@@ -599,7 +599,8 @@ int pbf_scene_destroy(pbf_scene* s) {
     {
         DeviceGuard dg(s->device);
         if (s->stream) cudaStreamSynchronize(s->stream);
-        for (void* m : {s->bnd.mem, s->bnd.body_mem, s->bnd.sort_mem, s->bnd.fq_mem})
+        for (void* m : {s->bnd.mem, s->bnd.body_mem, s->bnd.sort_mem, s->bnd.fq_mem,
+                        static_cast<void*>(s->bnd.rb)})
             if (m) cudaFree(m);
         if (s->bnd.idx.off) cudaFree(s->bnd.idx.off);
         free_particles(s);
@@ -1244,15 +1245,17 @@ int pbf_scene_set_bodies(pbf_scene* s, int nbodies, const float* pos3, const flo
 
 namespace {
 
-// Boundary world positions from the current body poses, boundary density
-// added to the final densities, coupling forces and torques accumulated onto
-// force3 / torque3 (fluid_world.cpp:57-81 after the PBF step).  C are the
-// constants of the step that produced the current state.
-int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* torque3) {
+// Enqueues on the scene's stream: boundary world positions from the current
+// body poses, boundary density added to the final densities, coupling forces
+// and torques accumulated onto the device accumulators b.force3 / b.torque3,
+// which start from force_in / torque_in (host arrays) or from zero
+// (fluid_world.cpp:57-81 after the PBF step).  C are the constants of the step
+// that produced the current state.  Needs b.nb > 0.
+int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
+                     const float* torque_in) {
     auto& b = s->bnd;
     const int nbodies = b.nbodies;
     cudaStream_t st = s->stream;
-    if (b.nb == 0) return sync_and_check(s);
     // 1. boundary world positions from the step-start transforms (unchanged
     //    by the PBF step, which never reads the boundary)
     cudaError_t e = boundary_xform(b.local, b.body, b.nb, b.body_pos, b.body_quat, nbodies,
@@ -1289,21 +1292,91 @@ int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* t
     if (e == cudaSuccess)
         e = coupling_forces(b.world, b.body, b.body_dyn, b.nb, nbodies, b.bq, fidx, b.Fb, C, st);
     if (nbodies > 0) {
+        const size_t bytes = (size_t)nbodies * 12;
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(b.force3, force3, (size_t)nbodies * 12, cudaMemcpyHostToDevice, st);
+            e = force_in ? cudaMemcpyAsync(b.force3, force_in, bytes, cudaMemcpyHostToDevice, st)
+                         : cudaMemsetAsync(b.force3, 0, bytes, st);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(b.torque3, torque3, (size_t)nbodies * 12, cudaMemcpyHostToDevice, st);
+            e = torque_in ? cudaMemcpyAsync(b.torque3, torque_in, bytes, cudaMemcpyHostToDevice, st)
+                          : cudaMemsetAsync(b.torque3, 0, bytes, st);
         if (e == cudaSuccess)
             e = body_reduce(b.Fb, b.world, b.list_off, b.list, b.body_pos, nbodies, b.force3,
                             b.torque3, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(force3, b.force3, (size_t)nbodies * 12, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(torque3, b.torque3, (size_t)nbodies * 12, cudaMemcpyDeviceToHost, st);
     }
     if (e != cudaSuccess) return cuda_fail(e, "coupling forces");
+    return PBF_OK;
+}
+
+// The coupling after a step, with the forces and torques added onto the host
+// arrays force3 / torque3; waits for it.
+int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* torque3) {
+    auto& b = s->bnd;
+    if (b.nb == 0) return sync_and_check(s);
+    int rc = enqueue_coupling(s, C, force3, torque3);
+    if (rc) return rc;
+    if (b.nbodies > 0) {
+        const size_t bytes = (size_t)b.nbodies * 12;
+        PBF_CUDA(cudaMemcpyAsync(force3, b.force3, bytes, cudaMemcpyDeviceToHost, s->stream));
+        PBF_CUDA(cudaMemcpyAsync(torque3, b.torque3, bytes, cudaMemcpyDeviceToHost, s->stream));
+    }
     return sync_and_check(s);
 }
+
+}  // namespace
+
+namespace pbf {
+namespace capi {
+
+int scene_set_rigid(pbf_scene* s, int nbodies, const pbf_rigid_body* bodies) {
+    if (!s || nbodies < 0 || (nbodies > 0 && !bodies))
+        return fail(PBF_ERR_INVALID_ARG, "bad body arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    if (b.rb) cudaFree(b.rb);
+    b.rb = nullptr;
+    b.nrb = 0;
+    if (nbodies == 0) return PBF_OK;
+    PBF_CUDA(cudaMalloc(&b.rb, (size_t)nbodies * sizeof(pbf_rigid_body)));
+    PBF_CUDA(cudaMemcpyAsync(b.rb, bodies, (size_t)nbodies * sizeof(pbf_rigid_body),
+                             cudaMemcpyHostToDevice, s->stream));
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    b.nrb = nbodies;
+    return PBF_OK;
+}
+
+int scene_read_rigid(pbf_scene* s, pbf_rigid_body* out) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    if (b.nrb > 0)
+        PBF_CUDA(cudaMemcpyAsync(out, b.rb, (size_t)b.nrb * sizeof(pbf_rigid_body),
+                                 cudaMemcpyDeviceToHost, s->stream));
+    return sync_and_check(s);
+}
+
+int scene_couple_rigid_async(pbf_scene* s, float dt, const float g[3]) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    if (b.nb > 0 && b.nbodies < b.needed_bodies) return fail(PBF_ERR_INVALID_ARG, "set the bodies first");
+    if (s->n > 0 && b.nb > 0) {  // fluid_world.cpp:57
+        StepConsts C;
+        int rc = make_consts(s, dt, C);
+        if (!rc) rc = enqueue_coupling(s, C, nullptr, nullptr);
+        if (rc) return rc;
+    }
+    const int nforce = (s->n > 0 && b.nb > 0) ? b.nbodies : 0;
+    const cudaError_t e = rigid_step(b.rb, b.nrb, b.force3, b.torque3, nforce, g[0], g[1], g[2], dt,
+                                     b.body_pos, b.body_quat, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "rigid step");
+    return PBF_OK;
+}
+
+}  // namespace capi
+}  // namespace pbf
+
+namespace {
 
 int check_coupling_args(pbf_scene* s, float* force3, float* torque3) {
     auto& b = s->bnd;

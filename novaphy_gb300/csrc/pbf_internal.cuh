@@ -145,6 +145,10 @@ struct pbf_scene {
         float* torque3 = nullptr;
         pbf::SortScratch sort{};
         uint32_t idx_slots = 0;
+        // Device copy of all rigid bodies when they step on the device
+        // (served coupled scenes), else null.
+        pbf_rigid_body* rb = nullptr;
+        int nrb = 0;
     } bnd;
 };
 
@@ -175,6 +179,14 @@ int restore_on(pbf_scene* s, const pbf_snapshot* snap, cudaStream_t st);
 size_t scene_device_bytes(const pbf_scene* s);
 // Cell slots of the grid a scene with these settings and positions steps on.
 uint32_t grid_slots_for(const pbf_settings& st, const float* x3, int n);
+// Device copy of the scene's rigid bodies, which then step on the device.
+int scene_set_rigid(pbf_scene* s, int nbodies, const pbf_rigid_body* bodies);
+// The device copy of the rigid bodies, after the scene's queued work.
+int scene_read_rigid(pbf_scene* s, pbf_rigid_body* out);
+// FluidWorld's post-step on the scene's stream, without waiting: the coupling
+// of the step that produced the current state (boundary density, forces and
+// torques from zero) and the rigid step of the device bodies under gravity g.
+int scene_couple_rigid_async(pbf_scene* s, float dt, const float g[3]);
 
 }  // namespace capi
 }  // namespace pbf
@@ -192,7 +204,7 @@ int batch_launch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const floa
                  uint32_t* flags_host, cudaEvent_t done_event);
 // Step graphs captured, updated in place and instantiated so far.
 void batch_counters(const pbf_batch* b, long long* captures, long long* updates,
-                    long long* instantiations);
+                    long long* instantiations, long long* direct);
 // Grows the batch's scratch for `particles` particles and `scenes` scenes.
 int batch_reserve(pbf_batch* b, int particles, int scenes);
 size_t batch_bytes(const pbf_batch* b);

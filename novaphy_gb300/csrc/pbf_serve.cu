@@ -12,6 +12,12 @@
 // A second thread waits on the oldest launch's event and retires its steps,
 // which frees its slot for the next launch.
 //
+// Coupled scenes (FluidWorld with rigid bodies) step like the others: right
+// after a launch is issued, the issue thread enqueues on each coupled scene's
+// stream the coupling of its step and the rigid step of its bodies, which live
+// on the device.  The next launch waits for the scene's stream, so the device
+// runs step, coupling, rigid step, next step in order with no host round trip.
+//
 // Admission.  A scene is charged state_bytes * n + grid_bytes * slots of its
 // grid (the share of the batch's offset table a launch holding it can use).
 // The batch scratch for max_batch_particles is reserved at creation.
@@ -72,13 +78,7 @@ struct SceneRec {
     bool coupled = false;
     std::vector<float> local, psi;  // until the device copy is made
     std::vector<int> body;
-    std::vector<pbf_rigid_body> bodies;
-    bool post = false;  // coupling and rigid step of its last step still to run
-};
-
-struct PostItem {
-    long long scene, req;
-    float dt;
+    std::vector<pbf_rigid_body> bodies;  // until the device copy is made
 };
 
 struct ReqRec {
@@ -184,10 +184,10 @@ void fail_scene(pbf_server* sv, SceneRec& sc, const std::string& why, int code) 
 
 void credit_step(pbf_server* sv, SceneRec& sc, ReqRec& r, double t);
 
-// Marks completed steps of a finished launch; called with the lock held.
-// Steps of coupled scenes are queued on `post` instead (their coupling and
-// rigid step run next, outside the lock).
-void complete_launch(pbf_server* sv, const Launch& L, double t, std::vector<PostItem>* post) {
+// Marks completed steps of a finished launch; called with the lock held.  A
+// coupled scene's step is credited when its PBF step completes; its coupling
+// and rigid step follow on the scene's stream, ahead of any later work there.
+void complete_launch(pbf_server* sv, const Launch& L, double t) {
     const uint32_t* fl = sv->flags + (size_t)L.slot * sv->cfg.max_batch_scenes;
     for (size_t k = 0; k < L.items.size(); ++k) {
         auto sit = sv->scenes.find(L.items[k].first);
@@ -201,12 +201,6 @@ void complete_launch(pbf_server* sv, const Launch& L, double t, std::vector<Post
         if (rit == sv->reqs.end()) continue;
         ReqRec& r = rit->second;
         if (r.state != PBF_REQ_PENDING) continue;
-        if (sc.coupled && post) {
-            // The step ends with its coupling and rigid step (run_posts).
-            sc.post = true;
-            post->push_back({sc.id, r.id, r.dt});
-            continue;
-        }
         credit_step(sv, sc, r, t);
     }
 }
@@ -229,8 +223,15 @@ void credit_step(pbf_server* sv, SceneRec& sc, ReqRec& r, double t) {
 }
 
 // Builds the next launch from issuable requests; called with the lock held.
+// A coupled scene of a launch: its index among the launch's items and its
+// gravity.
+struct CoupledItem {
+    int item;
+    float g[3];
+};
+
 bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
-                  std::vector<float>& dts) {
+                  std::vector<float>& dts, std::vector<CoupledItem>& coupled) {
     struct Cand {
         double t;
         SceneRec* sc;
@@ -240,7 +241,6 @@ bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
     for (auto& kv : sv->scenes) {
         SceneRec& sc = kv.second;
         if (sc.state != PBF_SCENE_RESIDENT || !sc.s || sc.busy) continue;
-        if (sc.coupled && (sc.inflight > 0 || sc.post)) continue;  // one step at a time
         for (long long rid : sc.reqs) {
             ReqRec* r = find_req(sv, rid);
             if (r && r->state == PBF_REQ_PENDING && r->issued < r->nsteps) {
@@ -255,9 +255,13 @@ bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
     L.particles = 0;
     ptrs.clear();
     dts.clear();
+    coupled.clear();
     for (const Cand& c : cand) {
         if ((int)L.items.size() >= sv->cfg.max_batch_scenes) break;
         if (!L.items.empty() && L.particles + c.sc->n > sv->cfg.max_batch_particles) continue;
+        if (c.sc->coupled)
+            coupled.push_back({(int)L.items.size(), {c.sc->gravity[0], c.sc->gravity[1],
+                                                     c.sc->gravity[2]}});
         L.items.push_back({c.sc->id, c.r->id});
         L.particles += c.sc->n;
         ptrs.push_back(c.sc->s);
@@ -268,16 +272,48 @@ bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
     return !L.items.empty();
 }
 
+// Host threads that enqueue the coupled scenes' post-steps of one launch
+// (each scene has its own stream and lock, so they proceed in parallel).
+constexpr size_t kPostThreads = 8;
+
+void enqueue_posts(pbf_server* sv, const std::vector<CoupledItem>& coupled,
+                   const std::vector<pbf_scene*>& ptrs, const std::vector<float>& dts,
+                   std::vector<std::pair<int, std::string>>& failed) {
+    std::mutex fmu;
+    auto one = [&](const CoupledItem& c) {
+        if (scene_couple_rigid_async(ptrs[(size_t)c.item], dts[(size_t)c.item], c.g)) {
+            std::lock_guard<std::mutex> lk(fmu);
+            failed.push_back({c.item, pbf_last_error()});
+        }
+    };
+    const size_t nt = std::min(kPostThreads, coupled.size() / 8);
+    if (nt <= 1) {
+        for (const CoupledItem& c : coupled) one(c);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    pool.reserve(nt);
+    for (size_t t = 0; t < nt; ++t)
+        pool.emplace_back([&] {
+            cudaSetDevice(sv->device);
+            for (size_t i; (i = next.fetch_add(1)) < coupled.size();) one(coupled[i]);
+        });
+    for (auto& t : pool) t.join();
+}
+
 // Issues launches while slots are free and requests are pending.
 void issue_main(pbf_server* sv) {
     cudaSetDevice(sv->device);
     std::vector<pbf_scene*> ptrs;
     std::vector<float> dts;
+    std::vector<CoupledItem> coupled;
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
         if (sv->stop) break;
         Launch L;
-        if ((int)sv->inflight.size() >= sv->cfg.max_inflight || !build_launch(sv, L, ptrs, dts)) {
+        if ((int)sv->inflight.size() >= sv->cfg.max_inflight ||
+            !build_launch(sv, L, ptrs, dts, coupled)) {
             sv->cv_work.wait(lk);
             continue;
         }
@@ -288,8 +324,17 @@ void issue_main(pbf_server* sv) {
         const double t_issue = now_ms();
         const int rc = batch_launch(sv->batch, (int)ptrs.size(), ptrs.data(), dts.data(), fl,
                                     sv->events[L.slot]);
+        // FluidWorld's post-step of the coupled scenes, enqueued before the
+        // next launch is issued (scenes in flight are not closed).
+        std::vector<std::pair<int, std::string>> post_failed;
+        if (!rc) enqueue_posts(sv, coupled, ptrs, dts, post_failed);
         const double issued = now_ms() - t_issue;
         lk.lock();
+        for (const auto& pf : post_failed) {
+            auto sit = sv->scenes.find(L.items[(size_t)pf.first].first);
+            if (sit != sv->scenes.end())
+                fail_scene(sv, sit->second, "the coupling failed: " + pf.second, PBF_ERR_CUDA);
+        }
         sv->issue_ms += issued;
         ++sv->launches;
         sv->launch_scenes += (long long)L.items.size();
@@ -312,74 +357,6 @@ void issue_main(pbf_server* sv) {
     }
 }
 
-// Coupling and rigid step of one coupled scene whose PBF step just completed
-// (FluidWorld::step after the fluid step); called without the lock.  Only
-// this call touches the scene's bodies while its `post` flag is set.
-void run_one_post(pbf_server* sv, const PostItem& it) {
-    {
-        SceneRec* sc = nullptr;
-        {
-            std::lock_guard<std::mutex> lk(sv->mu);
-            auto sit = sv->scenes.find(it.scene);
-            if (sit != sv->scenes.end()) sc = &sit->second;
-        }
-        if (!sc) return;
-        const int nb = (int)sc->bodies.size();
-        std::vector<float> f((size_t)3 * nb, 0.0f), tq((size_t)3 * nb, 0.0f);
-        int rc = pbf_scene_couple(sc->s, it.dt, nb ? f.data() : nullptr, nb ? tq.data() : nullptr);
-        std::string why;
-        if (rc) why = std::string("coupling failed: ") + pbf_last_error();
-        if (!rc && nb > 0) {
-            std::vector<float> pos((size_t)3 * nb), quat((size_t)4 * nb);
-            std::vector<int> dyn((size_t)nb);
-            for (int k = 0; k < nb; ++k) {
-                pbf_rigid_body& b = sc->bodies[(size_t)k];
-                if (b.inv_mass > 0.0f) {
-                    pbf_rigid::integrate_velocity(b.lin_vel, b.ang_vel, sc->gravity, &f[3 * k],
-                                                  b.inv_mass, b.inv_inertia, &tq[3 * k], it.dt);
-                    pbf_rigid::integrate_position(b.pos, b.quat, b.lin_vel, b.ang_vel, it.dt);
-                }
-                for (int d = 0; d < 3; ++d) pos[3 * k + d] = b.pos[d];
-                for (int d = 0; d < 4; ++d) quat[4 * k + d] = b.quat[d];
-                dyn[(size_t)k] = b.inv_mass > 0.0f ? 1 : 0;
-            }
-            rc = pbf_scene_set_bodies(sc->s, nb, pos.data(), quat.data(), dyn.data());
-            if (rc) why = std::string("setting the bodies failed: ") + pbf_last_error();
-        }
-        const double t = now_ms();
-        std::lock_guard<std::mutex> lk(sv->mu);
-        sc->post = false;
-        if (rc) {
-            fail_scene(sv, *sc, why, rc);
-            return;
-        }
-        auto rit = sv->reqs.find(it.req);
-        if (rit != sv->reqs.end() && rit->second.state == PBF_REQ_PENDING)
-            credit_step(sv, *sc, rit->second, t);
-    }
-}
-
-// The post-passes of a retired launch, spread over up to kPostThreads host
-// threads so that the scenes' coupling kernels overlap on their own streams.
-constexpr size_t kPostThreads = 8;
-
-void run_posts(pbf_server* sv, const std::vector<PostItem>& items) {
-    const size_t nt = std::min(items.size(), kPostThreads);
-    if (nt <= 1) {
-        for (const PostItem& it : items) run_one_post(sv, it);
-        return;
-    }
-    std::atomic<size_t> next{0};
-    std::vector<std::thread> pool;
-    pool.reserve(nt);
-    for (size_t k = 0; k < nt; ++k)
-        pool.emplace_back([&] {
-            cudaSetDevice(sv->device);
-            for (size_t i; (i = next.fetch_add(1)) < items.size();) run_one_post(sv, items[i]);
-        });
-    for (auto& t : pool) t.join();
-}
-
 // Waits for the oldest launch and retires its steps.
 void retire_main(pbf_server* sv) {
     cudaSetDevice(sv->device);
@@ -396,7 +373,6 @@ void retire_main(pbf_server* sv) {
         const double t = now_ms();
         lk.lock();
         Launch L = std::move(sv->inflight.front());
-        sv->inflight.pop_front();
         if (e != cudaSuccess) {
             const std::string why =
                 std::string("a batch launch did not complete: ") + cudaGetErrorString(e);
@@ -407,14 +383,9 @@ void retire_main(pbf_server* sv) {
                 fail_scene(sv, sit->second, why, PBF_ERR_CUDA);
             }
         } else {
-            std::vector<PostItem> post;
-            complete_launch(sv, L, t, &post);
-            if (!post.empty()) {
-                lk.unlock();
-                run_posts(sv, post);
-                lk.lock();
-            }
+            complete_launch(sv, L, t);
         }
+        sv->inflight.pop_front();
         sv->cv_work.notify_one();
         sv->cv_done.notify_all();
     }
@@ -445,6 +416,7 @@ int materialize(pbf_server* sv, SceneRec& rec) {
             }
             rc = pbf_scene_set_bodies(s, nbodies, pos.data(), quat.data(), dyn.data());
         }
+        if (!rc) rc = scene_set_rigid(s, nbodies, rec.bodies.data());
         if (rc) {
             pbf_scene_destroy(s);
             return rc;
@@ -696,7 +668,7 @@ int pbf_server_close_scene(pbf_server* sv, long long id) {
         if (sc.state == PBF_SCENE_WAITING) return true;
         for (long long rid : sc.reqs)
             if (req_pending(sv, rid)) return false;
-        return sc.inflight == 0 && !sc.post;
+        return sc.inflight == 0;
     });
     it = sv->scenes.find(id);
     if (it == sv->scenes.end()) return PBF_OK;
@@ -787,7 +759,7 @@ int pbf_server_read(pbf_server* sv, long long id, int field, float* out) {
             if (sc.busy) return false;
             for (long long r : sc.reqs)
                 if (req_pending(sv, r)) return false;
-            return sc.inflight == 0 && !sc.post;
+            return sc.inflight == 0;
         };
         sv->cv_done.wait(lk, idle);
         auto it = sv->scenes.find(id);
@@ -826,22 +798,40 @@ int pbf_server_read(pbf_server* sv, long long id, int field, float* out) {
 int pbf_server_read_bodies(pbf_server* sv, long long id, pbf_rigid_body* out) {
     int rc = check_server(sv);
     if (rc) return rc;
-    std::unique_lock<std::mutex> lk(sv->mu);
-    sv->cv_done.wait(lk, [&] {
+    pbf_scene* s = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(sv->mu);
+        sv->cv_done.wait(lk, [&] {
+            auto it = sv->scenes.find(id);
+            if (it == sv->scenes.end()) return true;
+            const SceneRec& sc = it->second;
+            if (sc.busy || sc.inflight > 0) return false;
+            for (long long r : sc.reqs)
+                if (req_pending(sv, r)) return false;
+            return true;
+        });
         auto it = sv->scenes.find(id);
-        if (it == sv->scenes.end()) return true;
-        const SceneRec& sc = it->second;
-        if (sc.busy || sc.post || sc.inflight > 0) return false;
-        for (long long r : sc.reqs)
-            if (req_pending(sv, r)) return false;
-        return true;
-    });
-    auto it = sv->scenes.find(id);
-    if (it == sv->scenes.end()) return fail(PBF_ERR_INVALID_ARG, "no such scene");
-    const auto& b = it->second.bodies;
-    if (!b.empty() && !out) return fail(PBF_ERR_INVALID_ARG, "output is NULL");
-    std::copy(b.begin(), b.end(), out);
-    return PBF_OK;
+        if (it == sv->scenes.end()) return fail(PBF_ERR_INVALID_ARG, "no such scene");
+        SceneRec& sc = it->second;
+        const auto& b = sc.bodies;
+        if (!b.empty() && !out) return fail(PBF_ERR_INVALID_ARG, "output is NULL");
+        if (!sc.s || b.empty()) {  // not on the device yet: the host copy
+            std::copy(b.begin(), b.end(), out);
+            return PBF_OK;
+        }
+        // The bodies step on the device, after the scene's last step; the busy
+        // flag keeps launches and close_scene away while they are copied.
+        s = sc.s;
+        sc.busy = true;
+    }
+    rc = scene_read_rigid(s, out);
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        auto it = sv->scenes.find(id);
+        if (it != sv->scenes.end()) it->second.busy = false;
+    }
+    sv->cv_done.notify_all();
+    return rc;
 }
 
 int pbf_server_scene_state(pbf_server* sv, long long id, int* state_out) {
@@ -889,7 +879,8 @@ int pbf_server_get_stats(pbf_server* sv, pbf_server_stats* out) {
     s.state_bytes_per_particle = kStateBytesPerParticle;
     s.grid_bytes_per_slot = kGridBytesPerSlot;
     s.issue_ms_mean = sv->launches ? sv->issue_ms / sv->launches : 0.0;
-    batch_counters(sv->batch, &s.graph_captures, &s.graph_updates, &s.graph_instantiations);
+    batch_counters(sv->batch, &s.graph_captures, &s.graph_updates, &s.graph_instantiations,
+                   &s.launches_direct);
     *out = s;
     return PBF_OK;
 }
