@@ -78,18 +78,32 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def profile_value(kernel: str, key: str = "traffic_bytes_per_launch"):
+    """A per-launch figure of `kernel` (DRAM bytes, warp instructions) from the
+    committed ncu summary of the 1M case, if any."""
     p = os.path.join(ROOT, "profiles", f"{kernel}_dam_break_1m.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip())
             except ValueError:
                 return None
     return None
+
+
+def issue_roof(inst_per_launch, launch_ms, sm_mhz, sms=152):
+    """Third roof, the one that binds: warp instructions issued per cycle per SM
+    (4 schedulers, one instruction each per cycle).  Instructions per launch
+    come from the ncu capture of the same kernel on the same workload; the
+    launch time and SM clock are this run's."""
+    if not inst_per_launch or not launch_ms or not sm_mhz:
+        return None
+    ipc = inst_per_launch / (launch_ms / 1e3 * sm_mhz * 1e6 * sms)
+    return {"achieved": ipc, "peak": 4.0, "unit": "warp inst/cycle/SM", "frac": ipc / 4.0,
+            "inst_per_launch": inst_per_launch,
+            "source": "smsp__inst_executed.sum of profiles/k_delta_dam_break_1m.md"}
 
 
 class ClockSampler:
@@ -814,12 +828,14 @@ def run_ours(args, ws, rank, local):
     achieved = alg / (launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     kern = KERNEL_OF_PHASE[dom]
-    traffic = profile_traffic(kern)
+    traffic = profile_value(kern)
     roofline = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "alg_bytes_per_launch": alg, "launch_ms": launch_ms,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "fp32": fp32_roof(value / ws, iters)}
+                "fp32": fp32_roof(value / ws, iters),
+                "issue": issue_roof(profile_value(kern, "warp_instructions_per_launch"), launch_ms,
+                                    clocks.get("sm_mhz") if clocks else None)}
 
     progress("single scene: fast build")
     # The FMA build on the same batch.
