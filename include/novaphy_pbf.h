@@ -183,6 +183,12 @@ int pbf_scene_step_coupled(pbf_scene* scene, float dt, float* force3, float* tor
  * pbf_scene_step_coupled(dt) bit for bit (the PBF step never reads the
  * boundary).  dt must be the step's time step. */
 int pbf_scene_couple(pbf_scene* scene, float dt, float* force3, float* torque3);
+/* pbf_scene_couple that also reports the device time (ms) of its three
+ * phases in phase_ms[0..2]: boundary world positions, boundary density,
+ * coupling forces and torques (fluid_world.cpp:52-85 phase names
+ * fluid.boundary.positions, fluid.boundary_density, fluid.coupling.total). */
+int pbf_scene_couple_profiled(pbf_scene* scene, float dt, float* force3, float* torque3,
+                              float* phase_ms);
 
 /* World positions of the boundary particles used by the last coupled step. */
 int pbf_scene_read_boundary(pbf_scene* scene, float* world3);

@@ -173,6 +173,13 @@ PYBIND11_MODULE(_core, m) {
     py::class_<PerformanceMonitor>(m, "PerformanceMonitor")
         .def(py::init<>())
         .def_readwrite("enabled", &PerformanceMonitor::enabled)
+        .def_readwrite("trace_enabled", &PerformanceMonitor::trace_enabled)
+        .def_readwrite("trace_frame_capacity", &PerformanceMonitor::trace_frame_capacity)
+        .def("write_trace_json",
+             [](const PerformanceMonitor& m, const py::object& path) {
+                 m.write_trace_json(py::str(path).cast<std::string>());
+             },
+             py::arg("path"))
         .def("phase_stats", &PerformanceMonitor::phase_stats)
         .def("last_frame_metrics", &PerformanceMonitor::last_frame_metrics)
         .def_property_readonly("frame_count", &PerformanceMonitor::frame_count)

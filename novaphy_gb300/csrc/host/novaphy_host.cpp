@@ -4,7 +4,9 @@
 #include "rigid_step.hpp"
 
 #include <algorithm>
+#include <cstdio>
 #include <cstdlib>
+#include <fstream>
 
 namespace novaphy_gb300 {
 
@@ -349,26 +351,115 @@ void SimState::set_angular_velocity(int i, const Vec3& w) {
 
 void PerformanceMonitor::begin_frame() {
     pending_.clear();
-    frame_start_ = std::chrono::steady_clock::now();
+    trace_cur_.clear();
+    frame_start_ = Clock::now();
 }
 
 void PerformanceMonitor::end_frame() {
     if (!enabled) return;
-    last_total_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
-                                                               frame_start_)
-                         .count();
+    const Clock::time_point t = Clock::now();
+    last_total_ms_ = std::chrono::duration<double, std::milli>(t - frame_start_).count();
     metrics_ = pending_;
     ++frames_;
+    if (tracing()) {
+        const double ts = now_us(t);
+        for (const MetricValue& m : metrics_) {
+            TraceEvent e;
+            e.name = m.name;
+            e.ph = 'C';
+            e.ts_us = ts;
+            e.value = m.value;
+            trace_cur_.push_back(e);
+        }
+        trace_frames_.push_back(std::move(trace_cur_));
+        trace_cur_.clear();
+        const size_t cap = (size_t)std::max(trace_frame_capacity, 1);
+        if (trace_frames_.size() > cap)
+            trace_frames_.erase(trace_frames_.begin(),
+                                trace_frames_.begin() + (long)(trace_frames_.size() - cap));
+    }
 }
 
-void PerformanceMonitor::record_phase(const std::string& name, double ms) {
-    if (!enabled) return;
+double PerformanceMonitor::now_us(Clock::time_point t) const {
+    return std::chrono::duration<double, std::micro>(t - epoch_).count();
+}
+
+void PerformanceMonitor::stat(const std::string& name, double ms) {
     PhaseStat& p = phases_[name];
     p.name = name;
     p.last_ms = ms;
     p.max_ms = std::max(p.max_ms, ms);
     p.avg_ms = (p.avg_ms * p.samples + ms) / (p.samples + 1);
     ++p.samples;
+}
+
+void PerformanceMonitor::record_phase(const std::string& name, double ms) {
+    record_phase(name, ms, Clock::now() - std::chrono::duration_cast<Clock::duration>(
+                                              std::chrono::duration<double, std::milli>(ms)));
+}
+
+void PerformanceMonitor::record_phase(const std::string& name, double ms, Clock::time_point start) {
+    if (!enabled) return;
+    stat(name, ms);
+    if (tracing()) {
+        TraceEvent e;
+        e.name = name;
+        e.ts_us = now_us(start);
+        e.dur_us = ms * 1e3;
+        trace_cur_.push_back(e);
+    }
+}
+
+void PerformanceMonitor::record_device_phase(const std::string& name, double ms, double start_us) {
+    if (!enabled) return;
+    stat(name, ms);
+    if (tracing()) {
+        TraceEvent e;
+        e.name = name;
+        e.ts_us = start_us;
+        e.dur_us = ms * 1e3;
+        e.tid = 1;
+        trace_cur_.push_back(e);
+    }
+}
+
+namespace {
+std::string json_escape(const std::string& s) {
+    std::string o;
+    for (char c : s) {
+        if (c == '"' || c == '\\') {
+            o += '\\';
+            o += c;
+        } else if ((unsigned char)c < 0x20) {
+            char buf[8];
+            std::snprintf(buf, sizeof(buf), "\\u%04x", (unsigned)(unsigned char)c);
+            o += buf;
+        } else {
+            o += c;
+        }
+    }
+    return o;
+}
+}  // namespace
+
+void PerformanceMonitor::write_trace_json(const std::string& path) const {
+    std::ofstream out(path);
+    if (!out) throw std::runtime_error("cannot write the trace file " + path);
+    out.precision(17);
+    out << "{\"traceEvents\": [";
+    bool first = true;
+    for (const auto& frame : trace_frames_)
+        for (const TraceEvent& e : frame) {
+            out << (first ? "\n" : ",\n");
+            first = false;
+            out << "{\"name\": \"" << json_escape(e.name) << "\", \"ph\": \"" << e.ph
+                << "\", \"ts\": " << e.ts_us << ", \"pid\": 0, \"tid\": " << e.tid;
+            if (e.ph == 'X') out << ", \"dur\": " << e.dur_us << ", \"cat\": \"novaphy\"";
+            else out << ", \"args\": {\"value\": " << e.value << "}";
+            out << "}";
+        }
+    out << (first ? "" : "\n") << "], \"displayTimeUnit\": \"ms\"}\n";
+    if (!out) throw std::runtime_error("writing the trace file " + path + " failed");
 }
 
 void PerformanceMonitor::record_metric(const std::string& name, double value) {
@@ -388,18 +479,22 @@ void PerformanceMonitor::reset() {
     pending_.clear();
     frames_ = 0;
     last_total_ms_ = 0.0;
+    trace_cur_.clear();
+    trace_frames_.clear();
 }
 
 namespace {
 struct Scope {
     PerformanceMonitor& m;
     std::string name;
-    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    PerformanceMonitor::Clock::time_point t0 = PerformanceMonitor::Clock::now();
     Scope(PerformanceMonitor& mon, const char* n) : m(mon), name(n) {}
     ~Scope() {
-        m.record_phase(name, std::chrono::duration<double, std::milli>(
-                                 std::chrono::steady_clock::now() - t0)
-                                 .count());
+        m.record_phase(name,
+                       std::chrono::duration<double, std::milli>(
+                           PerformanceMonitor::Clock::now() - t0)
+                           .count(),
+                       t0);
     }
 };
 }  // namespace
@@ -443,7 +538,6 @@ void World::step_rigid_pipeline(float dt) {
             w = Vec3(wa[0], wa[1], wa[2]);
         }
     }
-    { Scope s(monitor_, "world.broadphase.sap"); }  // contacts are not modelled on this path
     {
         Scope s(monitor_, "world.integrate_position");
         for (int i = 0; i < n; ++i) {
@@ -464,6 +558,11 @@ void World::step_rigid_pipeline(float dt) {
         for (auto& f : state_.forces) f = Vec3{};
         for (auto& t : state_.torques) t = Vec3{};
     }
+    int dynamic = 0;
+    for (const RigidBody& b : model_.bodies) dynamic += b.is_static() ? 0 : 1;
+    monitor_.record_metric("bodies", (double)n);
+    monitor_.record_metric("dynamic_bodies", (double)dynamic);
+    monitor_.record_metric("shapes", (double)model_.shapes.size());
 }
 
 // ---- PBFSolver ----
@@ -582,13 +681,39 @@ void FluidWorld::step(float dt) {
                 f[(size_t)k] = state_.forces[(size_t)k];
                 t[(size_t)k] = state_.torques[(size_t)k];
             }
-            {
+            if (!boundary_.empty() && needed > 0)
+                check_pbf(pbf_scene_set_bodies(scene_, needed, pos.data(), quat.data(),
+                                               dyn.data()));
+            float* fp = needed ? &f[0].x : nullptr;
+            float* tp = needed ? &t[0].x : nullptr;
+            if (!monitor_.enabled) {
                 Scope p(monitor_, "fluid.pbf.total");
-                if (!boundary_.empty() && needed > 0)
-                    check_pbf(pbf_scene_set_bodies(scene_, needed, pos.data(), quat.data(),
-                                                   dyn.data()));
-                check_pbf(pbf_scene_step_coupled(scene_, dt, needed ? &f[0].x : nullptr,
-                                                 needed ? &t[0].x : nullptr));
+                check_pbf(pbf_scene_step_coupled(scene_, dt, fp, tp));
+            } else {
+                // Profiled: the same step (a plain launch sequence instead of
+                // the graph) with the device time of every reference phase.
+                float ph[PBF_NUM_PHASES];
+                {
+                    Scope p(monitor_, "fluid.pbf.total");
+                    check_pbf(pbf_scene_step_profiled(scene_, dt, ph, nullptr));
+                    double at = monitor_.now_us(p.t0);
+                    for (int k = 0; k < PBF_NUM_PHASES; ++k) {
+                        monitor_.record_device_phase(pbf_phase_name(k), ph[k], at);
+                        at += ph[k] * 1e3;
+                    }
+                }
+                if (!boundary_.empty()) {
+                    float cp[3];
+                    const PerformanceMonitor::Clock::time_point c0 = PerformanceMonitor::Clock::now();
+                    check_pbf(pbf_scene_couple_profiled(scene_, dt, fp, tp, cp));
+                    const char* names[3] = {"fluid.boundary.positions", "fluid.boundary_density",
+                                            "fluid.coupling.total"};
+                    double at = monitor_.now_us(c0);
+                    for (int k = 0; k < 3; ++k) {
+                        monitor_.record_device_phase(names[k], cp[k], at);
+                        at += cp[k] * 1e3;
+                    }
+                }
             }
             for (int k = 0; k < needed && k < model_.num_bodies(); ++k) {
                 state_.forces[(size_t)k] = f[(size_t)k];

@@ -252,25 +252,50 @@ struct MetricValue {
     double value = 0.0;
 };
 
+// With trace_enabled, the phases of the last trace_frame_capacity frames are
+// kept as Chrome trace events (complete events "X" for phases, counter events
+// "C" for metrics) and written by write_trace_json.  Host-timed phases sit on
+// thread 0 at their host time; device-timed phases (the PBF step and coupling
+// phases, measured with CUDA events) on thread 1, laid end to end from the
+// start of the host phase that ran them.
 class PerformanceMonitor {
 public:
+    using Clock = std::chrono::steady_clock;
     bool enabled = false;
+    bool trace_enabled = false;
+    int trace_frame_capacity = 120;
     void begin_frame();
     void end_frame();
     void record_phase(const std::string& name, double ms);
+    void record_phase(const std::string& name, double ms, Clock::time_point start);
+    void record_device_phase(const std::string& name, double ms, double start_us);
     void record_metric(const std::string& name, double value);
     std::vector<PhaseStat> phase_stats() const;
     std::vector<MetricValue> last_frame_metrics() const { return metrics_; }
     int frame_count() const { return frames_; }
     double last_frame_total_ms() const { return last_total_ms_; }
+    // Microseconds since the monitor was created (trace time stamps).
+    double now_us(Clock::time_point t = Clock::now()) const;
+    void write_trace_json(const std::string& path) const;
     void reset();
 
 private:
+    struct TraceEvent {
+        std::string name;
+        char ph = 'X';
+        double ts_us = 0.0, dur_us = 0.0, value = 0.0;
+        int tid = 0;
+    };
+    bool tracing() const { return enabled && trace_enabled; }
+    void stat(const std::string& name, double ms);
     std::map<std::string, PhaseStat> phases_;
     std::vector<MetricValue> metrics_, pending_;
     int frames_ = 0;
     double last_total_ms_ = 0.0;
-    std::chrono::steady_clock::time_point frame_start_{};
+    Clock::time_point frame_start_{};
+    Clock::time_point epoch_ = Clock::now();
+    std::vector<TraceEvent> trace_cur_;
+    std::vector<std::vector<TraceEvent>> trace_frames_;  // oldest first
 };
 
 // Rigid world: gravity, accumulated forces, symplectic Euler integration

@@ -1252,14 +1252,18 @@ namespace {
 // (fluid_world.cpp:57-81 after the PBF step).  C are the constants of the step
 // that produced the current state.  Needs b.nb > 0.
 int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
-                     const float* torque_in) {
+                     const float* torque_in, cudaEvent_t* marks = nullptr) {
     auto& b = s->bnd;
     const int nbodies = b.nbodies;
     cudaStream_t st = s->stream;
+    // marks[0..3]: start, after the positions, after the density, end
+    auto mark = [&](int k) { return marks ? cudaEventRecord(marks[k], st) : cudaSuccess; };
+    PBF_CUDA(mark(0));
     // 1. boundary world positions from the step-start transforms (unchanged
     //    by the PBF step, which never reads the boundary)
     cudaError_t e = boundary_xform(b.local, b.body, b.nb, b.body_pos, b.body_quat, nbodies,
                                    b.world, st);
+    if (e == cudaSuccess) e = mark(1);
     if (e != cudaSuccess) return cuda_fail(e, "boundary_xform");
     // 2. boundary density on the final positions (fluid_world.cpp:101-123)
     int rc = ensure_boundary_grid(s, C.grid.nslots);
@@ -1270,6 +1274,7 @@ int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
     QuerySet fq{b.fq_cell, s->B.sown, s->B.btab};
     if (e == cudaSuccess) e = index_classify(fq, s->B.x, s->n, b.idx, C, st);
     if (e == cudaSuccess) e = boundary_density(s->B.x, s->n, fq, b.idx, s->B.rho, C, st);
+    if (e == cudaSuccess) e = mark(2);
     if (e != cudaSuccess) return cuda_fail(e, "boundary density");
     // 3. coupling forces from a fresh fluid grid on the final positions
     //    (fluid_world.cpp:125-174); the step's sorted buffers are free now.
@@ -1303,23 +1308,50 @@ int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
             e = body_reduce(b.Fb, b.world, b.list_off, b.list, b.body_pos, nbodies, b.force3,
                             b.torque3, st);
     }
+    if (e == cudaSuccess) e = mark(3);
     if (e != cudaSuccess) return cuda_fail(e, "coupling forces");
     return PBF_OK;
 }
 
 // The coupling after a step, with the forces and torques added onto the host
 // arrays force3 / torque3; waits for it.
-int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* torque3) {
+// With phase_ms (3 entries), also the device time of the boundary positions,
+// the boundary density and the coupling forces.
+int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* torque3,
+                      float* phase_ms = nullptr) {
     auto& b = s->bnd;
+    if (phase_ms)
+        for (int k = 0; k < 3; ++k) phase_ms[k] = 0.0f;
     if (b.nb == 0) return sync_and_check(s);
-    int rc = enqueue_coupling(s, C, force3, torque3);
-    if (rc) return rc;
-    if (b.nbodies > 0) {
-        const size_t bytes = (size_t)b.nbodies * 12;
-        PBF_CUDA(cudaMemcpyAsync(force3, b.force3, bytes, cudaMemcpyDeviceToHost, s->stream));
-        PBF_CUDA(cudaMemcpyAsync(torque3, b.torque3, bytes, cudaMemcpyDeviceToHost, s->stream));
+    cudaEvent_t ev[4] = {};
+    int created = 0;
+    if (phase_ms)
+        for (; created < 4; ++created)
+            if (cudaEventCreate(&ev[created]) != cudaSuccess) break;
+    auto destroy = [&] {
+        for (int k = 0; k < created; ++k) cudaEventDestroy(ev[k]);
+    };
+    if (phase_ms && created < 4) {
+        destroy();
+        return cuda_fail(cudaGetLastError(), "cudaEventCreate");
     }
-    return sync_and_check(s);
+    int rc = enqueue_coupling(s, C, force3, torque3, phase_ms ? ev : nullptr);
+    if (!rc && b.nbodies > 0) {
+        const size_t bytes = (size_t)b.nbodies * 12;
+        cudaError_t e = cudaMemcpyAsync(force3, b.force3, bytes, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(torque3, b.torque3, bytes, cudaMemcpyDeviceToHost, s->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "coupling forces copy");
+    }
+    if (!rc) rc = sync_and_check(s);
+    if (!rc && phase_ms)
+        for (int k = 0; k < 3; ++k)
+            if (cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]) != cudaSuccess) {
+                rc = cuda_fail(cudaGetLastError(), "cudaEventElapsedTime");
+                break;
+            }
+    destroy();
+    return rc;
 }
 
 }  // namespace
@@ -1407,16 +1439,23 @@ int pbf_scene_step_coupled(pbf_scene* s, float dt, float* force3, float* torque3
 }
 
 int pbf_scene_couple(pbf_scene* s, float dt, float* force3, float* torque3) {
+    return pbf_scene_couple_profiled(s, dt, force3, torque3, nullptr);
+}
+
+int pbf_scene_couple_profiled(pbf_scene* s, float dt, float* force3, float* torque3,
+                              float* phase_ms) {
     if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     DeviceGuard dg(s->device);
+    if (phase_ms)
+        for (int k = 0; k < 3; ++k) phase_ms[k] = 0.0f;
     int rc = check_coupling_args(s, force3, torque3);
     if (rc) return rc;
     if (s->n == 0) return PBF_OK;
     StepConsts C;
     rc = make_consts(s, dt, C);
     if (rc) return rc;
-    return couple_after_step(s, C, force3, torque3);
+    return couple_after_step(s, C, force3, torque3, phase_ms);
 }
 
 int pbf_scene_read_boundary(pbf_scene* s, float* world3) {

@@ -150,3 +150,55 @@ def test_stepping_needs_a_device_and_says_so():
     st.init([[0, 0, 0], [0.02, 0, 0]])
     with pytest.raises(RuntimeError, match="CUDA"):
         novaphy.PBFSolver(novaphy.PBFSettings()).step(st, 1 / 60, [0, -9.81, 0], 0.125)
+
+
+def _free_body_world():
+    mb = novaphy.ModelBuilder()
+    mb.add_ground_plane(y=0.0)
+    half = np.array([0.5, 0.5, 0.5], np.float32)
+    for y in (0.5, 1.5):
+        i = mb.add_body(novaphy.RigidBody.from_box(1.0, half),
+                        novaphy.Transform.from_translation(np.array([0.0, y, 0.0], np.float32)))
+        mb.add_shape(novaphy.CollisionShape.make_box(half, i))
+    return novaphy.World(mb.build(), novaphy.SolverSettings())
+
+
+def test_monitor_is_off_by_default_and_records_nothing():
+    w = _free_body_world()
+    mon = w.performance_monitor
+    assert mon.enabled is False and mon.trace_enabled is False
+    w.step(1 / 120)
+    assert mon.frame_count == 0 and mon.phase_stats() == [] and mon.last_frame_metrics() == []
+    assert mon.last_frame_total_ms == 0.0
+
+
+def test_monitor_trace_json_and_reset(tmp_path):
+    import json
+
+    w = _free_body_world()
+    mon = w.performance_monitor
+    mon.enabled = True
+    mon.trace_enabled = True
+    mon.trace_frame_capacity = 2
+    for _ in range(3):
+        w.step(1 / 120)
+    phases = {p.name: p for p in mon.phase_stats()}
+    assert {"world.total", "world.integrate_velocity", "world.integrate_position"} <= set(phases)
+    assert phases["world.total"].samples == 3 and phases["world.total"].last_ms > 0.0
+    metrics = {m.name: m.value for m in mon.last_frame_metrics()}
+    assert metrics == {"bodies": 2.0, "dynamic_bodies": 2.0, "shapes": 3.0}
+    path = tmp_path / "trace.json"
+    mon.write_trace_json(path)
+    ev = json.loads(path.read_text())["traceEvents"]
+    xs = [e for e in ev if e["ph"] == "X"]
+    cs = [e for e in ev if e["ph"] == "C"]
+    # two frames kept: one world.total each, three counters each
+    assert sum(e["name"] == "world.total" for e in xs) == 2 and len(cs) == 6
+    assert all(e["dur"] >= 0.0 and e["ts"] >= 0.0 for e in xs)
+    tot = [e for e in xs if e["name"] == "world.total"][-1]
+    inner = [e for e in xs if e["name"] == "world.integrate_velocity"][-1]
+    assert tot["ts"] <= inner["ts"] and inner["ts"] + inner["dur"] <= tot["ts"] + tot["dur"] + 1.0
+    mon.reset()
+    assert mon.phase_stats() == [] and mon.last_frame_metrics() == [] and mon.frame_count == 0
+    mon.write_trace_json(str(path))
+    assert json.loads(path.read_text())["traceEvents"] == []

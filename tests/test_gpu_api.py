@@ -1,6 +1,7 @@
 """The NovaPhy-compatible API on the GPU: PBFSolver and FluidWorld, written
 after the reference's tests/python/test_pbf.py, test_coupling.py and
 test_performance_monitor.py, plus bit-exact checks against the oracle."""
+import json
 import os
 
 import numpy as np
@@ -119,21 +120,51 @@ def test_coupled_simulation_runs_and_sphere_falls():
     assert nf.state.transforms[0].position[1] < 0.8
 
 
-def test_monitor_reports_fluid_phases_and_metrics():
+def test_monitor_reports_fluid_phases_and_metrics(tmp_path):
     w = sphere_scene()
     mon = w.performance_monitor
     mon.enabled = True
+    mon.trace_enabled = True
     w.step(1 / 60)
-    phases = {p.name for p in mon.phase_stats()}
-    assert {"fluid.total", "fluid.pbf.total", "fluid.rigid_step", "world.total",
-            "world.broadphase.sap"} <= phases
+    phases = {p.name: p for p in mon.phase_stats()}
+    want = {"fluid.total", "fluid.pbf.total", "fluid.rigid_step", "world.total",
+            "fluid.boundary.positions", "fluid.boundary_density", "fluid.coupling.total"}
+    want |= {"fluid.pbf." + k for k in ("predict", "grid_build", "neighbor_query",
+                                         "iteration.compute_density",
+                                         "iteration.compute_delta_position", "xsph_viscosity",
+                                         "commit_positions")}
+    assert want <= set(phases)
+    assert phases["fluid.pbf.iteration.compute_density"].last_ms > 0.0
+    assert phases["fluid.coupling.total"].last_ms > 0.0
     metrics = {m.name: m.value for m in mon.last_frame_metrics()}
     assert metrics["fluid_particles"] > 0 and metrics["boundary_particles"] >= 0
     assert metrics["pbf_solver_iterations"] == 2.0
     assert abs(metrics["kernel_radius"] - 0.2) < 1e-6
+    assert metrics["bodies"] == 1.0 and metrics["dynamic_bodies"] == 1.0
     assert mon.frame_count == 1
+    path = tmp_path / "fluid_trace.json"
+    mon.write_trace_json(path)
+    ev = json.loads(path.read_text())["traceEvents"]
+    assert {e["name"] for e in ev if e["ph"] == "X" and e["tid"] == 1} >= {
+        "fluid.pbf.iteration.compute_density", "fluid.coupling.total"}
+    assert any(e["ph"] == "C" and e["name"] == "fluid_particles" for e in ev)
     mon.reset()
     assert mon.frame_count == 0 and mon.phase_stats() == []
+
+
+def test_profiled_fluid_world_steps_like_the_plain_one():
+    # The monitor switches to the profiled launch sequence; the state must not move.
+    a, b = sphere_scene(), sphere_scene()
+    b.performance_monitor.enabled = True
+    for _ in range(3):
+        a.step(1 / 60)
+        b.step(1 / 60)
+    for name in ("positions_array", "velocities_array", "densities_array"):
+        assert np.array_equal(getattr(a.fluid_state, name), getattr(b.fluid_state, name)), name
+    assert np.array_equal(np.asarray(a.fluid_state.lambdas, np.float32),
+                          np.asarray(b.fluid_state.lambdas, np.float32))
+    pa, pb = a.state.transforms[0].position, b.state.transforms[0].position
+    assert np.array_equal(np.asarray(pa, np.float32), np.asarray(pb, np.float32))
 
 
 def test_fluid_world_step_matches_oracle(port):
