@@ -159,7 +159,7 @@ __device__ __forceinline__ void for_each_candidate(const int4 cell, const uint32
                 const int wx = wrap(cell.x - 1, G.ox, G.gx);
                 if (wx + 2 < G.gx) {
                     const uint32_t q1 = __ldg(off + row + wx + 3);
-#pragma unroll 4
+#pragma unroll 8
                     for (uint32_t q = __ldg(off + row + wx); q < q1; ++q) f(q);
                 } else {
                     for (int d = 0; d < 3; ++d) {
