@@ -127,6 +127,7 @@ void pool_free(void* p, cudaStream_t st) {
 namespace {
 
 void free_particles(pbf_scene* s) {
+    ++s->buf_gen;
     if (s->graph) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
@@ -166,6 +167,7 @@ int alloc_particles(pbf_scene* s, int cap) {
 // Step scratch for the scene's capacity (sorted copies, keys, buckets, sort).
 int ensure_work(pbf_scene* s) {
     if (s->wmem && s->work_cap >= s->cap) return PBF_OK;
+    ++s->buf_gen;
     if (s->graph) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
@@ -260,6 +262,7 @@ namespace {
 
 int ensure_offsets(pbf_scene* s, uint32_t nslots) {
     if (s->off && s->off_cap >= nslots + 1) return PBF_OK;
+    ++s->buf_gen;
     if (s->graph) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
@@ -603,6 +606,7 @@ int pbf_scene_destroy(pbf_scene* s) {
                         static_cast<void*>(s->bnd.rb)})
             if (m) cudaFree(m);
         if (s->bnd.idx.off) cudaFree(s->bnd.idx.off);
+        if (s->couple_graph) cudaGraphExecDestroy(s->couple_graph);
         free_particles(s);
         if (s->off) cudaFree(s->off);
         if (s->d_flag) cudaFree(s->d_flag);
@@ -1092,6 +1096,7 @@ namespace {
 
 // Carves per-boundary-particle arrays for nb particles.
 int alloc_boundary(pbf_scene* s, int nb) {
+    ++s->buf_gen;
     auto& b = s->bnd;
     for (void* m : {b.mem, b.sort_mem}) if (m) cudaFree(m);
     b.mem = b.sort_mem = nullptr;
@@ -1132,6 +1137,7 @@ int alloc_boundary(pbf_scene* s, int nb) {
 int ensure_boundary_grid(pbf_scene* s, uint32_t nslots) {
     auto& b = s->bnd;
     if (b.idx.off && b.idx_slots >= nslots) return PBF_OK;
+    ++s->buf_gen;
     if (b.idx.off) cudaFree(b.idx.off);
     b.idx.off = nullptr;
     const size_t ob = align_up((size_t)(nslots + 1) * 4, 256);
@@ -1144,6 +1150,7 @@ int ensure_boundary_grid(pbf_scene* s, uint32_t nslots) {
 int ensure_fluid_queries(pbf_scene* s) {
     auto& b = s->bnd;
     if (b.fq_mem && b.fq_cap >= s->n) return PBF_OK;
+    ++s->buf_gen;
     if (b.fq_mem) cudaFree(b.fq_mem);
     b.fq_mem = nullptr;
     const int c = s->n > 0 ? s->n : 1;
@@ -1169,6 +1176,7 @@ int pbf_scene_set_boundary(pbf_scene* s, int nb, const float* local3, const int*
     auto& b = s->bnd;
     b.nbodies = 0;
     b.needed_bodies = 0;
+    ++s->buf_gen;
     if (b.body_mem) cudaFree(b.body_mem);
     b.body_mem = nullptr;
     if (nb == 0) return PBF_OK;
@@ -1365,6 +1373,7 @@ int scene_set_rigid(pbf_scene* s, int nbodies, const pbf_rigid_body* bodies) {
     std::lock_guard<std::mutex> lk(s->mu);
     DeviceGuard dg(s->device);
     auto& b = s->bnd;
+    ++s->buf_gen;
     if (b.rb) cudaFree(b.rb);
     b.rb = nullptr;
     b.nrb = 0;
@@ -1392,16 +1401,67 @@ int scene_couple_rigid_async(pbf_scene* s, float dt, const float g[3]) {
     DeviceGuard dg(s->device);
     auto& b = s->bnd;
     if (b.nb > 0 && b.nbodies < b.needed_bodies) return fail(PBF_ERR_INVALID_ARG, "set the bodies first");
-    if (s->n > 0 && b.nb > 0) {  // fluid_world.cpp:57
-        StepConsts C;
-        int rc = make_consts(s, dt, C);
-        if (!rc) rc = enqueue_coupling(s, C, nullptr, nullptr);
+    const bool couple = s->n > 0 && b.nb > 0;  // fluid_world.cpp:57
+    pbf_scene::CoupleKey key;
+    key.valid = true;
+    if (couple) {
+        // Every allocation happens here, before any capture.
+        int rc = make_consts(s, dt, key.C);
+        if (!rc) rc = ensure_boundary_grid(s, key.C.grid.nslots);
+        if (!rc) rc = ensure_fluid_queries(s);
         if (rc) return rc;
     }
-    const int nforce = (s->n > 0 && b.nb > 0) ? b.nbodies : 0;
-    const cudaError_t e = rigid_step(b.rb, b.nrb, b.force3, b.torque3, nforce, g[0], g[1], g[2], dt,
-                                     b.body_pos, b.body_quat, s->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "rigid step");
+    key.dt = dt;
+    for (int d = 0; d < 3; ++d) key.g[d] = g[d];
+    key.n = s->n;
+    key.nb = b.nb;
+    key.nbodies = b.nbodies;
+    key.nrb = b.nrb;
+    key.gen = s->buf_gen;
+    auto same = [](const pbf_scene::CoupleKey& x, const pbf_scene::CoupleKey& y) {
+        return x.valid && y.valid && consts_equal(x.C, y.C) && x.dt == y.dt && x.g[0] == y.g[0] &&
+               x.g[1] == y.g[1] && x.g[2] == y.g[2] && x.n == y.n && x.nb == y.nb &&
+               x.nbodies == y.nbodies && x.nrb == y.nrb && x.gen == y.gen;
+    };
+    auto enqueue_all = [&]() -> int {
+        if (couple) {
+            const int rc = enqueue_coupling(s, key.C, nullptr, nullptr);
+            if (rc) return rc;
+        }
+        const int nforce = couple ? b.nbodies : 0;
+        const cudaError_t e = rigid_step(b.rb, b.nrb, b.force3, b.torque3, nforce, g[0], g[1], g[2],
+                                         dt, b.body_pos, b.body_quat, s->stream);
+        return e == cudaSuccess ? PBF_OK : cuda_fail(e, "rigid step");
+    };
+    if (!graphs_enabled()) return enqueue_all();
+    if (!(s->couple_graph && same(key, s->couple_key))) {
+        if (!same(key, s->couple_seen)) {
+            // A key seen once runs directly; the second time in a row it is captured.
+            s->couple_seen = key;
+            return enqueue_all();
+        }
+        if (s->couple_graph) {
+            cudaGraphExecDestroy(s->couple_graph);
+            s->couple_graph = nullptr;
+        }
+        cudaGraph_t gr = nullptr;
+        PBF_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        const int erc = enqueue_all();
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &gr);
+        if (erc) {
+            if (gr) cudaGraphDestroy(gr);
+            return erc;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&s->couple_graph, gr, 0);
+        cudaGraphDestroy(gr);
+        if (ce != cudaSuccess) {
+            s->couple_graph = nullptr;
+            return cuda_fail(ce, "cudaGraphInstantiate");
+        }
+        s->couple_key = key;
+    }
+    PBF_CUDA(cudaGraphLaunch(s->couple_graph, s->stream));
     return PBF_OK;
 }
 

@@ -121,6 +121,22 @@ struct pbf_scene {
     int graph_iters = -1;
     int graph_exact = -1;
 
+    // Bumped whenever a device buffer that a captured graph uses is
+    // reallocated, so such graphs are captured anew.
+    unsigned long long buf_gen = 0;
+    // Graph of the post-step of a served coupled scene (coupling and rigid
+    // step, scene_couple_rigid_async), captured the second time in a row the
+    // same key is seen.
+    struct CoupleKey {
+        bool valid = false;
+        pbf::StepConsts C{};
+        float dt = 0.0f, g[3] = {0.0f, 0.0f, 0.0f};
+        int n = 0, nb = 0, nbodies = 0, nrb = 0;
+        unsigned long long gen = 0;
+    };
+    cudaGraphExec_t couple_graph = nullptr;
+    CoupleKey couple_key, couple_seen;
+
     // Akinci boundary (FluidWorld coupling).
     struct Boundary {
         int nb = 0, nbodies = 0, needed_bodies = 0;
