@@ -379,6 +379,8 @@ typedef struct pbf_server_stats {
     long long graph_instantiations;  /* ... instantiated anew */
     long long launches_direct;       /* step launches issued without a graph (a
                                         shape is captured when seen twice in a row) */
+    double post_ms_mean;             /* part of issue_ms_mean spent enqueueing the
+                                        coupled scenes' coupling and rigid step */
 } pbf_server_stats;
 
 /* Defaults: 120 GB budget, 16M particles and 1024 scenes per launch, 2

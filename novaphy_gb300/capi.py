@@ -521,7 +521,7 @@ class ServerStats(C.Structure):
         ("state_bytes_per_particle", C.c_size_t), ("grid_bytes_per_slot", C.c_size_t),
         ("issue_ms_mean", C.c_double), ("graph_captures", C.c_longlong),
         ("graph_updates", C.c_longlong), ("graph_instantiations", C.c_longlong),
-        ("launches_direct", C.c_longlong),
+        ("launches_direct", C.c_longlong), ("post_ms_mean", C.c_double),
     ]
 
     def as_dict(self) -> dict:

@@ -128,6 +128,7 @@ struct pbf_server {
               launch_particles = 0;
     double t_first = -1.0, t_last = 0.0;
     double issue_ms = 0.0;  // host time spent issuing launches
+    double post_ms = 0.0;   // ... of which enqueueing coupled scenes' post-steps
     pbf_stats::LatencyHist step_ms, req_ms;
 };
 
@@ -327,8 +328,10 @@ void issue_main(pbf_server* sv) {
         // FluidWorld's post-step of the coupled scenes, enqueued before the
         // next launch is issued (scenes in flight are not closed).
         std::vector<std::pair<int, std::string>> post_failed;
+        const double t_post = now_ms();
         if (!rc) enqueue_posts(sv, coupled, ptrs, dts, post_failed);
-        const double issued = now_ms() - t_issue;
+        const double t_end = now_ms();
+        const double issued = t_end - t_issue;
         lk.lock();
         for (const auto& pf : post_failed) {
             auto sit = sv->scenes.find(L.items[(size_t)pf.first].first);
@@ -336,6 +339,7 @@ void issue_main(pbf_server* sv) {
                 fail_scene(sv, sit->second, "the coupling failed: " + pf.second, PBF_ERR_CUDA);
         }
         sv->issue_ms += issued;
+        sv->post_ms += t_end - t_post;
         ++sv->launches;
         sv->launch_scenes += (long long)L.items.size();
         sv->launch_particles += L.particles;
@@ -879,6 +883,7 @@ int pbf_server_get_stats(pbf_server* sv, pbf_server_stats* out) {
     s.state_bytes_per_particle = kStateBytesPerParticle;
     s.grid_bytes_per_slot = kGridBytesPerSlot;
     s.issue_ms_mean = sv->launches ? sv->issue_ms / sv->launches : 0.0;
+    s.post_ms_mean = sv->launches ? sv->post_ms / sv->launches : 0.0;
     batch_counters(sv->batch, &s.graph_captures, &s.graph_updates, &s.graph_instantiations,
                    &s.launches_direct);
     *out = s;
@@ -894,6 +899,7 @@ int pbf_server_reset_stats(pbf_server* sv) {
     sv->steps_done = sv->particle_steps = sv->launches = 0;
     sv->launch_scenes = sv->launch_particles = 0;
     sv->issue_ms = 0.0;
+    sv->post_ms = 0.0;
     sv->rejected = 0;
     sv->t_first = -1.0;
     sv->t_last = 0.0;
