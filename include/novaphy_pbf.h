@@ -344,6 +344,10 @@ typedef struct pbf_server_config {
     int max_batch_particles; /* particles per launch (the scratch is sized for it) */
     int max_batch_scenes;    /* scenes per launch */
     int max_inflight;        /* launches queued on the GPU ahead of completion, >= 1 */
+    int min_step_particles;  /* a launch runs further steps of its scenes with the
+                                deepest queues only when each further step holds
+                                at least this many particles (and a quarter of
+                                the launch's); default 1M */
 } pbf_server_config;
 
 enum pbf_scene_state {

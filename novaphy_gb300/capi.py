@@ -500,6 +500,7 @@ class ServerConfig(C.Structure):
         ("max_batch_particles", C.c_int),
         ("max_batch_scenes", C.c_int),
         ("max_inflight", C.c_int),
+        ("min_step_particles", C.c_int),
     ]
 
 

@@ -107,14 +107,18 @@ struct pbf_batch {
     int tab_cap = 0;  // scenes
     void* tmem = nullptr;  // per-scene tables: StepConsts | StateRef | firsts
     size_t tab_refs_at = 0, tab_firsts_at = 0, tab_bytes = 0;
-    // Pinned host copies of the tables, used in turn; each one's event marks
-    // the end of its upload, so it is rewritten only after the copy is done.
-    static constexpr int kTabRing = 4;
+    // Pinned host copies of the tables, used in turn and allocated on first
+    // use; each one's event marks the end of its upload, so it is rewritten
+    // only after the copy is done.  Sized for the step uploads that can be
+    // queued at once (a serving launch runs up to 16 steps, two launches in
+    // flight), so that issuing a step does not wait for the device.
+    static constexpr int kTabRing = 64;
     char* h_tab[kTabRing] = {};
     cudaEvent_t h_tab_ev[kTabRing] = {};
     bool h_tab_used[kTabRing] = {};
     int h_tab_next = 0;
 
+    cudaEvent_t fork = nullptr;  // splits scenes' post-steps off between steps
     uint32_t* d_bad = nullptr;  // per-scene non-finite flags of the last call
     int bad_cap = 0;
     int bad_count = 0;
@@ -227,10 +231,6 @@ int ensure_tables(pbf_batch* b, int nscenes) {
     b->tab_firsts_at = b->tab_refs_at + align_up((size_t)c * sizeof(StateRef), 256);
     b->tab_bytes = b->tab_firsts_at + align_up((size_t)(c + 1) * 4, 256);
     PBF_CUDA(cudaMalloc(&b->tmem, b->tab_bytes));
-    for (int k = 0; k < pbf_batch::kTabRing; ++k) {
-        PBF_CUDA(cudaMallocHost(&b->h_tab[k], b->tab_bytes));
-        PBF_CUDA(cudaEventCreateWithFlags(&b->h_tab_ev[k], cudaEventDisableTiming));
-    }
     b->tab_cap = c;
     return PBF_OK;
 }
@@ -389,6 +389,10 @@ int step_group(pbf_batch* b, const std::vector<pbf_scene*>& list, const std::vec
 
     const int ring = b->h_tab_next;
     b->h_tab_next = (ring + 1) % pbf_batch::kTabRing;
+    if (!b->h_tab[ring]) {
+        PBF_CUDA(cudaMallocHost(&b->h_tab[ring], b->tab_bytes));
+        PBF_CUDA(cudaEventCreateWithFlags(&b->h_tab_ev[ring], cudaEventDisableTiming));
+    }
     if (b->h_tab_used[ring]) PBF_CUDA(cudaEventSynchronize(b->h_tab_ev[ring]));
     char* h = b->h_tab[ring];
     auto* htab = reinterpret_cast<StepConsts*>(h);
@@ -573,7 +577,7 @@ int release_scenes(pbf_batch* b, int nscenes, pbf_scene* const* scenes) {
 }
 
 int run_batch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
-              const int* nsteps) {
+              const int* nsteps, const LaunchSpec* spec = nullptr) {
     int max_steps = 0;
     for (int k = 0; k < nscenes; ++k) {
         const int m = nsteps ? nsteps[k] : 1;
@@ -609,6 +613,31 @@ int run_batch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* 
             rc = step_group(b, list, dts, orig, exact, nullptr);
             if (rc) return rc;
         }
+        if (spec && spec->sub && step < spec->nsub)
+            PBF_CUDA(cudaEventRecord(spec->sub[step], b->stream));
+        if (spec && spec->post && step + 1 < max_steps) {
+            // Post-steps of the scenes that step again, forked off the batch
+            // stream onto their own streams and joined before the next step.
+            bool forked = false;
+            for (int k = 0; k < nscenes; ++k) {
+                pbf_scene* s = scenes[k];
+                const int m = nsteps ? nsteps[k] : 1;
+                if (!spec->needs_post || !spec->needs_post[k] || m <= step + 1 || s->n <= 0)
+                    continue;
+                if (!forked) {
+                    if (!b->fork)
+                        PBF_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+                    PBF_CUDA(cudaEventRecord(b->fork, b->stream));
+                    forked = true;
+                }
+                PBF_CUDA(cudaStreamWaitEvent(s->stream, b->fork, 0));
+                rc = spec->post(spec->post_ctx, s, k);
+                if (rc) return rc;
+                if (!s->ev) PBF_CUDA(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
+                PBF_CUDA(cudaEventRecord(s->ev, s->stream));
+                PBF_CUDA(cudaStreamWaitEvent(b->stream, s->ev, 0));
+            }
+        }
     }
     return PBF_OK;
 }
@@ -638,22 +667,24 @@ int check_args(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float*
 namespace pbf {
 namespace capi {
 
-int batch_launch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
-                 uint32_t* flags_host, cudaEvent_t done_event) {
+int batch_launch(pbf_batch* b, const LaunchSpec& S) {
     std::lock_guard<std::mutex> lk(b->mu);
     DeviceGuard dg(b->device);
     SceneLocks L;
-    int rc = lock_scenes(b, nscenes, scenes, L);
+    const int nscenes = S.nscenes;
+    int rc = lock_scenes(b, nscenes, S.scenes, L);
     if (rc) return rc;
-    rc = wait_for_scenes(b, nscenes, scenes);
-    if (!rc) rc = run_batch(b, nscenes, scenes, dt, nullptr);
-    if (!rc && flags_host && nscenes > 0)
-        rc = cudaMemcpyAsync(flags_host, b->d_bad, (size_t)nscenes * 4, cudaMemcpyDeviceToHost,
+    rc = wait_for_scenes(b, nscenes, S.scenes);
+    if (!rc && S.start && cudaEventRecord(S.start, b->stream) != cudaSuccess)
+        rc = fail(PBF_ERR_CUDA, "start event");
+    if (!rc) rc = run_batch(b, nscenes, S.scenes, S.dt, S.nsteps, &S);
+    if (!rc && S.flags_host && nscenes > 0)
+        rc = cudaMemcpyAsync(S.flags_host, b->d_bad, (size_t)nscenes * 4, cudaMemcpyDeviceToHost,
                              b->stream) == cudaSuccess
                  ? PBF_OK
                  : fail(PBF_ERR_CUDA, "flags copy");
-    const int rc2 = release_scenes(b, nscenes, scenes);
-    if (!rc && done_event) PBF_CUDA(cudaEventRecord(done_event, b->stream));
+    const int rc2 = release_scenes(b, nscenes, S.scenes);
+    if (!rc && S.done) PBF_CUDA(cudaEventRecord(S.done, b->stream));
     return rc ? rc : rc2;
 }
 
@@ -728,6 +759,7 @@ int pbf_batch_destroy(pbf_batch* b) {
                         static_cast<void*>(b->d_bad), static_cast<void*>(b->barrier)})
             if (m) cudaFree(m);
         if (b->done) cudaEventDestroy(b->done);
+        if (b->fork) cudaEventDestroy(b->fork);
         if (b->stream) cudaStreamDestroy(b->stream);
     }
     delete b;

@@ -1399,6 +1399,10 @@ int scene_read_rigid(pbf_scene* s, pbf_rigid_body* out) {
 int scene_couple_rigid_async(pbf_scene* s, float dt, const float g[3]) {
     std::lock_guard<std::mutex> lk(s->mu);
     DeviceGuard dg(s->device);
+    return scene_couple_rigid_locked(s, dt, g);
+}
+
+int scene_couple_rigid_locked(pbf_scene* s, float dt, const float g[3]) {
     auto& b = s->bnd;
     if (b.nb > 0 && b.nbodies < b.needed_bodies) return fail(PBF_ERR_INVALID_ARG, "set the bodies first");
     const bool couple = s->n > 0 && b.nb > 0;  // fluid_world.cpp:57

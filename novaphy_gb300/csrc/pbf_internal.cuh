@@ -203,6 +203,8 @@ int scene_read_rigid(pbf_scene* s, pbf_rigid_body* out);
 // of the step that produced the current state (boundary density, forces and
 // torques from zero) and the rigid step of the device bodies under gravity g.
 int scene_couple_rigid_async(pbf_scene* s, float dt, const float g[3]);
+// The same for a caller that holds the scene's lock and current device.
+int scene_couple_rigid_locked(pbf_scene* s, float dt, const float g[3]);
 
 }  // namespace capi
 }  // namespace pbf
@@ -212,12 +214,27 @@ struct pbf_batch;
 namespace pbf {
 namespace capi {
 
-// One step of each scene (distinct, unlocked by the caller) as one batch
-// launch, asynchronous on the batch's stream.  When flags_host is given
-// (pinned, nscenes words), it receives each scene's non-finite flag once the
-// launch completes; done_event (if given) is recorded after the launch.
-int batch_launch(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float* dt,
-                 uint32_t* flags_host, cudaEvent_t done_event);
+// A batch launch of the serving loop: nsteps[k] steps of each scene
+// (distinct, unlocked by the caller; one each when nsteps is null),
+// asynchronous on the batch's stream.
+struct LaunchSpec {
+    int nscenes = 0;
+    pbf_scene* const* scenes = nullptr;
+    const float* dt = nullptr;
+    const int* nsteps = nullptr;
+    uint32_t* flags_host = nullptr;  // pinned, nscenes words: non-finite flag per scene
+    cudaEvent_t start = nullptr;     // recorded before the first step
+    cudaEvent_t* sub = nullptr;      // sub[s] recorded after step index s (s < nsub)
+    int nsub = 0;
+    cudaEvent_t done = nullptr;      // recorded after the launch
+    // Between two steps of a scene k with needs_post[k] set, post(ctx, s, k)
+    // enqueues its post-step on the scene's stream (the batch holds the
+    // scene's lock); the batch waits for it before that scene steps again.
+    int (*post)(void* ctx, pbf_scene* s, int k) = nullptr;
+    void* post_ctx = nullptr;
+    const unsigned char* needs_post = nullptr;
+};
+int batch_launch(pbf_batch* b, const LaunchSpec& L);
 // Step graphs captured, updated in place and instantiated so far.
 void batch_counters(const pbf_batch* b, long long* captures, long long* updates,
                     long long* instantiations, long long* direct);

@@ -5,7 +5,10 @@
 // Scheduling.  Every resident scene has a FIFO of requests; its issuable
 // request is the first one with steps not yet issued.  A launch takes one
 // step of every scene with an issuable request, oldest request first, up to
-// the per-launch particle and scene caps.  Up to max_inflight launches are
+// the per-launch particle and scene caps.  A heavily loaded launch takes
+// further steps of the scenes with the deepest queues (up to kMaxSubSteps
+// each; see build_launch): the batch runs them as consecutive steps, so deep
+// queues drain at several steps per launch instead of one.  Up to max_inflight launches are
 // queued on the batch stream; while they run, the scheduler builds the next
 // one from whatever is pending then (continuous batching), and a scene can
 // be in several queued launches at once because the stream orders them.
@@ -30,6 +33,7 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <functional>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -91,10 +95,20 @@ struct ReqRec {
     int code = PBF_OK;
 };
 
+constexpr int kMaxSubSteps = 16;  // steps of one scene in one launch
+
+struct LaunchItem {
+    long long scene = 0;
+    int steps = 0;
+    std::vector<std::pair<long long, int>> reqs;  // (request, steps taken from it), in order
+};
+
 struct Launch {
     int slot = 0;
-    std::vector<std::pair<long long, long long>> items;  // (scene, request)
-    long long particles = 0;
+    std::vector<LaunchItem> items;
+    long long particles = 0;  // particles of the launch's scenes
+    long long work = 0;       // particle-steps
+    int max_steps = 0;
 };
 
 }  // namespace
@@ -118,7 +132,8 @@ struct pbf_server {
     size_t charged = 0;
 
     std::deque<Launch> inflight;
-    std::vector<cudaEvent_t> events;
+    std::vector<cudaEvent_t> events;              // per slot: end of the launch
+    std::vector<cudaEvent_t> ev_start, ev_sub;    // per slot: timing of its steps
     uint32_t* flags = nullptr;  // pinned, max_inflight x max_batch_scenes
     int next_slot = 0;
 
@@ -188,21 +203,25 @@ void credit_step(pbf_server* sv, SceneRec& sc, ReqRec& r, double t);
 // Marks completed steps of a finished launch; called with the lock held.  A
 // coupled scene's step is credited when its PBF step completes; its coupling
 // and rigid step follow on the scene's stream, ahead of any later work there.
-void complete_launch(pbf_server* sv, const Launch& L, double t) {
+// t_step[s] is the completion time of the launch's step index s.
+void complete_launch(pbf_server* sv, const Launch& L, const std::vector<double>& t_step) {
     const uint32_t* fl = sv->flags + (size_t)L.slot * sv->cfg.max_batch_scenes;
     for (size_t k = 0; k < L.items.size(); ++k) {
-        auto sit = sv->scenes.find(L.items[k].first);
+        const LaunchItem& it = L.items[k];
+        auto sit = sv->scenes.find(it.scene);
         if (sit == sv->scenes.end()) continue;
         SceneRec& sc = sit->second;
-        --sc.inflight;
+        sc.inflight -= it.steps;
         if (fl[k])
             fail_scene(sv, sc, "a step committed a non-finite position or velocity",
                        PBF_ERR_NONFINITE);
-        auto rit = sv->reqs.find(L.items[k].second);
-        if (rit == sv->reqs.end()) continue;
-        ReqRec& r = rit->second;
-        if (r.state != PBF_REQ_PENDING) continue;
-        credit_step(sv, sc, r, t);
+        size_t s = 0;
+        for (const auto& rq : it.reqs)
+            for (int j = 0; j < rq.second; ++j, ++s) {
+                ReqRec* r = find_req(sv, rq.first);
+                if (r && r->state == PBF_REQ_PENDING)
+                    credit_step(sv, sc, *r, t_step[std::min(s, t_step.size() - 1)]);
+            }
     }
 }
 
@@ -231,8 +250,27 @@ struct CoupledItem {
     float g[3];
 };
 
+// The first request of sc with steps not yet issued, or null.
+ReqRec* issuable(pbf_server* sv, SceneRec& sc) {
+    for (long long rid : sc.reqs) {
+        ReqRec* r = find_req(sv, rid);
+        if (r && r->state == PBF_REQ_PENDING && r->issued < r->nsteps) return r;
+    }
+    return nullptr;
+}
+
+long long unissued_steps(pbf_server* sv, const SceneRec& sc) {
+    long long n = 0;
+    for (long long rid : sc.reqs) {
+        const ReqRec* r = find_req(sv, rid);
+        if (r && r->state == PBF_REQ_PENDING) n += r->nsteps - r->issued;
+    }
+    return n;
+}
+
 bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
-                  std::vector<float>& dts, std::vector<CoupledItem>& coupled) {
+                  std::vector<float>& dts, std::vector<int>& nsteps,
+                  std::vector<unsigned char>& needs_post, std::vector<CoupledItem>& coupled) {
     struct Cand {
         double t;
         SceneRec* sc;
@@ -253,24 +291,92 @@ bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
     if (cand.empty()) return false;
     std::sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.t < b.t; });
     L.items.clear();
-    L.particles = 0;
+    L.particles = L.work = 0;
+    L.max_steps = 0;
     ptrs.clear();
     dts.clear();
+    nsteps.clear();
+    needs_post.clear();
     coupled.clear();
+    std::vector<SceneRec*> recs;
+    const long long cap = sv->cfg.max_batch_particles;
     for (const Cand& c : cand) {
         if ((int)L.items.size() >= sv->cfg.max_batch_scenes) break;
-        if (!L.items.empty() && L.particles + c.sc->n > sv->cfg.max_batch_particles) continue;
+        if (!L.items.empty() && L.particles + c.sc->n > cap) continue;
         if (c.sc->coupled)
             coupled.push_back({(int)L.items.size(), {c.sc->gravity[0], c.sc->gravity[1],
                                                      c.sc->gravity[2]}});
-        L.items.push_back({c.sc->id, c.r->id});
+        LaunchItem it;
+        it.scene = c.sc->id;
+        it.steps = 1;
+        it.reqs.push_back({c.r->id, 1});
+        L.items.push_back(std::move(it));
         L.particles += c.sc->n;
         ptrs.push_back(c.sc->s);
         dts.push_back(c.r->dt);
+        needs_post.push_back(c.sc->coupled ? 1 : 0);
+        recs.push_back(c.sc);
         ++c.r->issued;
         ++c.sc->inflight;
     }
+    L.work = L.particles;
+    // Further steps, level by level: step index s of the launch takes the
+    // scenes that took every step before it and still have an issuable step
+    // with the same dt, deepest queue first, while the launch's particle-steps
+    // stay under the cap and under twice its particles.  A step index is only
+    // added when it holds at least a quarter of the launch's particles and
+    // min_step_particles: a batch step has a fixed cost, and a launch under
+    // light load must stay short for the requests that arrive meanwhile.
+    const long long extra_cap = std::min<long long>(cap, 2 * L.particles);
+    const long long level_min =
+        std::max<long long>(std::max(sv->cfg.min_step_particles, 0), L.particles / 4);
+    for (int level = 1; level < kMaxSubSteps; ++level) {
+        std::vector<std::pair<long long, int>> c;  // (unissued steps, -item)
+        for (size_t k = 0; k < L.items.size(); ++k) {
+            if (L.items[k].steps != level) continue;
+            const ReqRec* r = issuable(sv, *recs[k]);
+            if (r && r->dt == dts[k]) c.push_back({unissued_steps(sv, *recs[k]), -(int)k});
+        }
+        std::sort(c.begin(), c.end(), std::greater<std::pair<long long, int>>());
+        std::vector<size_t> take;
+        long long level_particles = 0;
+        for (const auto& e : c) {
+            const size_t k = (size_t)(-e.second);
+            if (L.work + level_particles + recs[k]->n > extra_cap) continue;
+            take.push_back(k);
+            level_particles += recs[k]->n;
+        }
+        if (take.empty() || level_particles < level_min) break;
+        for (size_t k : take) {
+            ReqRec* r = issuable(sv, *recs[k]);
+            ++r->issued;
+            ++recs[k]->inflight;
+            LaunchItem& it = L.items[k];
+            ++it.steps;
+            if (it.reqs.back().first == r->id) ++it.reqs.back().second;
+            else it.reqs.push_back({r->id, 1});
+        }
+        L.work += level_particles;
+    }
+    for (const LaunchItem& it : L.items) {
+        nsteps.push_back(it.steps);
+        L.max_steps = std::max(L.max_steps, it.steps);
+    }
     return !L.items.empty();
+}
+
+// Between two steps of a coupled scene inside one launch: its coupling and
+// rigid step (the batch holds the scene's lock and device).
+struct PostCtx {
+    const std::vector<float>* dts;
+    const std::vector<CoupledItem>* coupled;
+    std::vector<int> slot_of;  // item -> index in coupled
+};
+
+int post_between_steps(void* ctx, pbf_scene* s, int k) {
+    const PostCtx* c = static_cast<const PostCtx*>(ctx);
+    const CoupledItem& ci = (*c->coupled)[(size_t)c->slot_of[(size_t)k]];
+    return scene_couple_rigid_locked(s, (*c->dts)[(size_t)k], ci.g);
 }
 
 // Host threads that enqueue the coupled scenes' post-steps of one launch
@@ -308,13 +414,15 @@ void issue_main(pbf_server* sv) {
     cudaSetDevice(sv->device);
     std::vector<pbf_scene*> ptrs;
     std::vector<float> dts;
+    std::vector<int> nsteps;
+    std::vector<unsigned char> needs_post;
     std::vector<CoupledItem> coupled;
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
         if (sv->stop) break;
         Launch L;
         if ((int)sv->inflight.size() >= sv->cfg.max_inflight ||
-            !build_launch(sv, L, ptrs, dts, coupled)) {
+            !build_launch(sv, L, ptrs, dts, nsteps, needs_post, coupled)) {
             sv->cv_work.wait(lk);
             continue;
         }
@@ -323,8 +431,25 @@ void issue_main(pbf_server* sv) {
         uint32_t* fl = sv->flags + (size_t)L.slot * sv->cfg.max_batch_scenes;
         lk.unlock();
         const double t_issue = now_ms();
-        const int rc = batch_launch(sv->batch, (int)ptrs.size(), ptrs.data(), dts.data(), fl,
-                                    sv->events[L.slot]);
+        PostCtx pctx;
+        pctx.dts = &dts;
+        pctx.coupled = &coupled;
+        pctx.slot_of.assign(ptrs.size(), -1);
+        for (size_t c = 0; c < coupled.size(); ++c) pctx.slot_of[(size_t)coupled[c].item] = (int)c;
+        LaunchSpec spec;
+        spec.nscenes = (int)ptrs.size();
+        spec.scenes = ptrs.data();
+        spec.dt = dts.data();
+        spec.nsteps = nsteps.data();
+        spec.flags_host = fl;
+        spec.start = sv->ev_start[(size_t)L.slot];
+        spec.sub = &sv->ev_sub[(size_t)L.slot * kMaxSubSteps];
+        spec.nsub = kMaxSubSteps;
+        spec.done = sv->events[(size_t)L.slot];
+        spec.post = post_between_steps;
+        spec.post_ctx = &pctx;
+        spec.needs_post = needs_post.data();
+        const int rc = batch_launch(sv->batch, spec);
         // FluidWorld's post-step of the coupled scenes, enqueued before the
         // next launch is issued (scenes in flight are not closed).
         std::vector<std::pair<int, std::string>> post_failed;
@@ -334,7 +459,7 @@ void issue_main(pbf_server* sv) {
         const double issued = t_end - t_issue;
         lk.lock();
         for (const auto& pf : post_failed) {
-            auto sit = sv->scenes.find(L.items[(size_t)pf.first].first);
+            auto sit = sv->scenes.find(L.items[(size_t)pf.first].scene);
             if (sit != sv->scenes.end())
                 fail_scene(sv, sit->second, "the coupling failed: " + pf.second, PBF_ERR_CUDA);
         }
@@ -347,9 +472,9 @@ void issue_main(pbf_server* sv) {
             // The launch did not run: its scenes cannot be trusted.
             const std::string why = std::string("a batch launch failed: ") + pbf_last_error();
             for (auto& it : L.items) {
-                auto sit = sv->scenes.find(it.first);
+                auto sit = sv->scenes.find(it.scene);
                 if (sit == sv->scenes.end()) continue;
-                --sit->second.inflight;
+                sit->second.inflight -= it.steps;
                 fail_scene(sv, sit->second, why, rc);
             }
             sv->next_slot = L.slot;  // the slot was not used
@@ -372,22 +497,39 @@ void retire_main(pbf_server* sv) {
             continue;
         }
         const int slot = sv->inflight.front().slot;
+        const int max_steps = sv->inflight.front().max_steps;
         lk.unlock();
         const cudaError_t e = cudaEventSynchronize(sv->events[slot]);
         const double t = now_ms();
+        // Completion time of each step index: the host time at which the end
+        // of the launch was seen, less the device time from that step's end
+        // to the launch's last step.
+        std::vector<double> t_step((size_t)std::max(max_steps, 1), t);
+        if (e == cudaSuccess && max_steps > 1) {
+            float ms[kMaxSubSteps];
+            bool ok = true;
+            for (int s = 0; s < max_steps && ok; ++s)
+                ok = cudaEventElapsedTime(&ms[s], sv->ev_start[(size_t)slot],
+                                          sv->ev_sub[(size_t)slot * kMaxSubSteps + s]) == cudaSuccess;
+            if (ok)
+                for (int s = 0; s < max_steps; ++s)
+                    t_step[(size_t)s] = t - (double)(ms[max_steps - 1] - ms[s]);
+            else
+                cudaGetLastError();
+        }
         lk.lock();
         Launch L = std::move(sv->inflight.front());
         if (e != cudaSuccess) {
             const std::string why =
                 std::string("a batch launch did not complete: ") + cudaGetErrorString(e);
             for (auto& it : L.items) {
-                auto sit = sv->scenes.find(it.first);
+                auto sit = sv->scenes.find(it.scene);
                 if (sit == sv->scenes.end()) continue;
-                --sit->second.inflight;
+                sit->second.inflight -= it.steps;
                 fail_scene(sv, sit->second, why, PBF_ERR_CUDA);
             }
         } else {
-            complete_launch(sv, L, t);
+            complete_launch(sv, L, t_step);
         }
         sv->inflight.pop_front();
         sv->cv_work.notify_one();
@@ -482,6 +624,7 @@ int pbf_server_default_config(pbf_server_config* out) {
     out->max_batch_particles = 16 << 20;
     out->max_batch_scenes = 1024;
     out->max_inflight = 2;
+    out->min_step_particles = 1 << 20;
     return PBF_OK;
 }
 
@@ -511,13 +654,20 @@ int pbf_server_create(int device, const pbf_server_config* cfg, pbf_server** out
         for (auto& e : sv->events)
             if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
                 rc = fail(PBF_ERR_CUDA, "cudaEventCreate");
+        sv->ev_start.assign((size_t)cfg->max_inflight, nullptr);
+        sv->ev_sub.assign((size_t)cfg->max_inflight * kMaxSubSteps, nullptr);
+        for (auto* v : {&sv->ev_start, &sv->ev_sub})
+            for (auto& e : *v)
+                if (!rc && cudaEventCreate(&e) != cudaSuccess)
+                    rc = fail(PBF_ERR_CUDA, "cudaEventCreate");
         if (!rc && cudaMallocHost(&sv->flags, (size_t)cfg->max_inflight * cfg->max_batch_scenes *
                                                   sizeof(uint32_t)) != cudaSuccess)
             rc = fail(PBF_ERR_OOM, "pinned flags");
     }
     if (rc) {
-        for (auto e : sv->events)
-            if (e) cudaEventDestroy(e);
+        for (auto* v : {&sv->events, &sv->ev_start, &sv->ev_sub})
+            for (auto e : *v)
+                if (e) cudaEventDestroy(e);
         if (sv->flags) cudaFreeHost(sv->flags);
         pbf_batch_destroy(b);
         return rc;
@@ -553,8 +703,9 @@ int pbf_server_destroy(pbf_server* sv) {
         for (auto& kv : sv->scenes)
             if (kv.second.s) pbf_scene_destroy(kv.second.s);
         sv->scenes.clear();
-        for (auto e : sv->events)
-            if (e) cudaEventDestroy(e);
+        for (auto* v : {&sv->events, &sv->ev_start, &sv->ev_sub})
+            for (auto e : *v)
+                if (e) cudaEventDestroy(e);
         if (sv->flags) cudaFreeHost(sv->flags);
         pbf_batch_destroy(sv->batch);
     }

@@ -47,9 +47,11 @@ def same(a, b):
     return all(np.array_equal(x.view(np.uint32), y.view(np.uint32)) for x, y in zip(a, b))
 
 
-def test_alone_equals_mix_under_concurrent_clients():
+@pytest.mark.parametrize("min_step", [1 << 20, 0])
+def test_alone_equals_mix_under_concurrent_clients(min_step):
+    # min_step=0 lets launches take several steps of the deeper queues.
     ws = small_scenes()
-    srv = capi.Server()
+    srv = capi.Server(capi.server_config(min_step_particles=min_step))
     ids = []
     for w in ws:
         sid, st = srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)
@@ -280,7 +282,9 @@ def test_coupled_served_scene_equals_fluid_world():
     nsteps = 4
 
     other = small_scenes(k=1, seed=23)[0]
-    srv = capi.Server()
+    # min_step_particles=0: the 4-step requests run as multi-step launches, so
+    # the coupling and rigid step also run between steps inside a launch.
+    srv = capi.Server(capi.server_config(min_step_particles=0))
     oid, _ = srv.open_scene(settings_of(other), other.x, other.v, other.mass, other.gravity)
     sid, state = srv.open_coupled_scene(st, x0, v0, mass, g, local, body, psi, bodies)
     assert state == capi.SCENE_RESIDENT
@@ -324,4 +328,19 @@ def test_finished_request_records_are_bounded():
     st = srv.stats()
     assert st["requests_done"] == kept + 11 and st["steps_done"] == 2
     srv.close_scene(sid)
+    srv.close()
+
+
+def test_deep_queue_runs_several_steps_per_launch():
+    # A 16-step request alone: the launch takes further steps of the same
+    # scene (up to the particle-step cap), with the same result as 16 steps.
+    w = small_scenes(k=1, seed=12)[0]
+    srv = capi.Server(capi.server_config(min_step_particles=0))
+    sid, _ = srv.open_scene(settings_of(w), w.x, w.v, w.mass, w.gravity)
+    q = srv.submit(sid, w.dt, 16)
+    assert srv.wait(q) == capi.REQ_DONE
+    st = srv.stats()
+    assert st["steps_done"] == 16 and st["launches"] < 16, st
+    assert 0.0 < st["step_ms_p50"] <= st["step_ms_p99"]
+    assert same(served(srv, sid, w.n), alone(w, [w.dt] * 16))
     srv.close()
