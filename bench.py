@@ -46,12 +46,6 @@ import time
 
 import numpy as np
 
-# The serving loop puts work on one stream per resident scene, each waiting on
-# the batch stream; with the default 8 hardware queues those cross-stream waits
-# stall the host's launches (measured: 47 ms of post-step enqueue per launch
-# with 8 queues, 6 ms with 32).  Read when the CUDA context is created.
-os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
-
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
