@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "latency_hist.hpp"
+#include "launch_plan.hpp"
 #include "pbf_internal.cuh"
 #include "rigid_step.hpp"
 
@@ -320,43 +321,35 @@ bool build_launch(pbf_server* sv, Launch& L, std::vector<pbf_scene*>& ptrs,
         ++c.sc->inflight;
     }
     L.work = L.particles;
-    // Further steps, level by level: step index s of the launch takes the
-    // scenes that took every step before it and still have an issuable step
-    // with the same dt, deepest queue first, while the launch's particle-steps
-    // stay under the cap and under twice its particles.  A step index is only
-    // added when it holds at least a quarter of the launch's particles and
-    // min_step_particles: a batch step has a fixed cost, and a launch under
-    // light load must stay short for the requests that arrive meanwhile.
-    const long long extra_cap = std::min<long long>(cap, 2 * L.particles);
-    const long long level_min =
-        std::max<long long>(std::max(sv->cfg.min_step_particles, 0), L.particles / 4);
-    for (int level = 1; level < kMaxSubSteps; ++level) {
-        std::vector<std::pair<long long, int>> c;  // (unissued steps, -item)
-        for (size_t k = 0; k < L.items.size(); ++k) {
-            if (L.items[k].steps != level) continue;
-            const ReqRec* r = issuable(sv, *recs[k]);
-            if (r && r->dt == dts[k]) c.push_back({unissued_steps(sv, *recs[k]), -(int)k});
+    // Further steps of the deepest queues (launch_plan.hpp); a scene's further
+    // steps keep its first step's dt.
+    std::vector<pbf_plan::PlanItem> plan(L.items.size());
+    for (size_t k = 0; k < L.items.size(); ++k) {
+        plan[k].n = recs[k]->n;
+        plan[k].depth = unissued_steps(sv, *recs[k]);
+        long long avail = 0;
+        for (long long rid : recs[k]->reqs) {
+            const ReqRec* r = find_req(sv, rid);
+            if (!r || r->state != PBF_REQ_PENDING || r->issued >= r->nsteps) continue;
+            if (r->dt != dts[k]) break;
+            avail += r->nsteps - r->issued;
+            if (avail >= kMaxSubSteps) break;
         }
-        std::sort(c.begin(), c.end(), std::greater<std::pair<long long, int>>());
-        std::vector<size_t> take;
-        long long level_particles = 0;
-        for (const auto& e : c) {
-            const size_t k = (size_t)(-e.second);
-            if (L.work + level_particles + recs[k]->n > extra_cap) continue;
-            take.push_back(k);
-            level_particles += recs[k]->n;
-        }
-        if (take.empty() || level_particles < level_min) break;
-        for (size_t k : take) {
+        plan[k].avail = (int)std::min<long long>(avail, kMaxSubSteps);
+    }
+    const std::vector<int> steps = pbf_plan::plan_steps(
+        plan, cap, std::max(sv->cfg.min_step_particles, 0), kMaxSubSteps);
+    for (size_t k = 0; k < L.items.size(); ++k) {
+        LaunchItem& it = L.items[k];
+        for (int j = 1; j < steps[k]; ++j) {
             ReqRec* r = issuable(sv, *recs[k]);
             ++r->issued;
             ++recs[k]->inflight;
-            LaunchItem& it = L.items[k];
             ++it.steps;
             if (it.reqs.back().first == r->id) ++it.reqs.back().second;
             else it.reqs.push_back({r->id, 1});
+            L.work += recs[k]->n;
         }
-        L.work += level_particles;
     }
     for (const LaunchItem& it : L.items) {
         nsteps.push_back(it.steps);
