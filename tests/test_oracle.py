@@ -224,3 +224,19 @@ def test_candidate_lists_longer_than_the_point_count(port):
     assert np.isfinite(f).all() and np.isfinite(t).all()
     off, idx = port.neighbor_sets(x, np.float32(0.1))
     assert off[-1] == len(idx) and len(idx) <= n * (n - 1)
+
+
+def test_port_matches_reference_build_on_served_scenes(port, ref):
+    # The serving workload's settings (PBFSettings' s_corr defaults, pools and
+    # dam breaks at r = 0.02, h = 4r, dt = 1/240): 10 steps of its two
+    # smallest scenes, restatement against the reference build, bit for bit.
+    # Vorticity off: the reference reads no vorticity setting (the restatement
+    # adds confinement only for epsilon > 0).
+    ws = sorted(workloads.served_scenes(nclients=16, seed=4), key=lambda w: w.n)[:2]
+    for w in ws:
+        s = Settings.make(**dict(w.settings, vorticity_epsilon=0.0))
+        z = np.zeros(w.n, np.float32)
+        a = port.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 10)
+        b = ref.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 10)
+        for u, t in zip(a, b):
+            assert np.array_equal(u, t), w.name
