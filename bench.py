@@ -774,6 +774,22 @@ def fp32_roof(particle_steps_per_s, iters, candidates=1728, neighbours=250):
             "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)"}
 
 
+def side_section(ws, fn):
+    """Runs one of the sections beside the headline (batched, coupled,
+    served).  On one rank, a failure is reported in that section's place
+    instead of losing the whole line; with several ranks it propagates, since
+    the other ranks would wait in a collective."""
+    if ws > 1:
+        return fn()
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001 - reported in the JSON line
+        import traceback
+
+        traceback.print_exc()
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def run_ours(args, ws, rank, local):
     from novaphy_gb300 import capi
 
@@ -916,15 +932,15 @@ def run_ours(args, ws, rank, local):
     batched = None
     if not args.no_batched:
         progress("batched scenes")
-        batched = run_batched(args, device, ws, rank, dist)
+        batched = side_section(ws, lambda: run_batched(args, device, ws, rank, dist))
     coupled = None
     if not args.no_coupled:
         progress("coupled scene")
-        coupled = run_coupled(args, device)
+        coupled = side_section(ws, lambda: run_coupled(args, device))
     served = None
     if not args.no_served:
         progress("served scenes")
-        served = run_served(args, device, ws, rank, dist)
+        served = side_section(ws, lambda: run_served(args, device, ws, rank, dist))
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
