@@ -4,8 +4,8 @@
   ``oracle/_build/liboracle_pbf.so`` with ``-O2 -ffp-contract=off`` (no fused
   multiply-add, so the operation order is the reference's on x86 and Arm).
 * ``build_ref()`` compiles the reference's own, unmodified fluid sources from
-  ``/root/reference`` (src/fluid/pbf_solver.cpp, neighbor_search.cpp,
-  particle_state.cpp and src/sim/performance_monitor.cpp) with the C-ABI
+  ``/root/reference`` (the fluid sources, src/sim/performance_monitor.cpp and
+  the rigid World that FluidWorld inherits; see REF_SOURCES) with the C-ABI
   harness ``oracle/ref_harness.cpp`` against the Eigen-API subset in
   ``oracle/eigen_shim`` into ``oracle/_ref/libref_pbf.so``.  The reference's
   own CMake build needs Eigen3 and tinyxml2, which are not installed; it is
@@ -24,7 +24,22 @@ REF_SOURCES = [
     "src/fluid/pbf_solver.cpp",
     "src/fluid/neighbor_search.cpp",
     "src/fluid/particle_state.cpp",
+    "src/fluid/boundary.cpp",
+    "src/fluid/fluid_world.cpp",
     "src/sim/performance_monitor.cpp",
+    # the rigid World that FluidWorld inherits (free bodies, contacts)
+    "src/sim/world.cpp",
+    "src/sim/state.cpp",
+    "src/core/body.cpp",
+    "src/core/shape.cpp",
+    "src/core/model_builder.cpp",
+    "src/core/joint.cpp",
+    "src/collision/broadphase.cpp",
+    "src/collision/narrowphase.cpp",
+    "src/dynamics/free_body_solver.cpp",
+    "src/dynamics/integrator.cpp",
+    "src/math/math_utils.cpp",
+    "src/math/spatial.cpp",
 ]
 PORT_LIB = os.path.join(HERE, "_build", "liboracle_pbf.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_pbf.so")
@@ -61,7 +76,7 @@ def build_ref(verbose: bool = False) -> str | None:
         return REF_LIB if os.path.exists(REF_LIB) else None
     srcs = [os.path.join(REFERENCE_ROOT, s) for s in REF_SOURCES]
     harness = os.path.join(HERE, "ref_harness.cpp")
-    shim = [os.path.join(HERE, "eigen_shim", "Eigen", f) for f in ("Core", "Geometry")]
+    shim = [os.path.join(HERE, "eigen_shim", "Eigen", f) for f in ("Core", "Geometry", "Dense")]
     if _newer(REF_LIB, srcs + [harness] + shim):
         return REF_LIB
     os.makedirs(os.path.dirname(REF_LIB), exist_ok=True)

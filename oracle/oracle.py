@@ -275,6 +275,80 @@ class Ref:
         L.ref_cubic_spline.restype = C.c_float
         L.ref_spiky_grad.argtypes = [_f32p, C.c_float, _f32p]
         L.ref_default_settings.argtypes = [C.POINTER(Settings)]
+        L.ref_boundary_volumes.argtypes = [C.c_int, _f32p, C.c_float, _f32p]
+        L.ref_boundary_volumes.restype = C.c_int
+        L.ref_boundary_world_positions.argtypes = [C.c_int, _f32p, _i32p, C.c_int, _f32p, _f32p,
+                                                   _f32p]
+        L.ref_fluid_world_run.argtypes = [C.POINTER(Settings), _f32p, _f32p, C.c_float, C.c_int,
+                                          _i32p, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_float,
+                                          C.c_float, C.c_float, C.c_int, C.c_int, _f32p, _f32p,
+                                          _f32p, _f32p, _f32p, _f32p, _f32p, _f32p]
+        L.ref_fluid_world_run.restype = C.c_int
+        L.ref_sample_box.argtypes = [_f32p, _f32p, _f32p, C.c_float, C.c_void_p, C.c_int]
+        L.ref_sample_sphere.argtypes = [C.c_float, _f32p, _f32p, C.c_float, C.c_void_p, C.c_int]
+        L.ref_sample_plane.argtypes = [_f32p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_int]
+
+    def boundary_volumes(self, world, h):
+        world = _f32(world, (-1, 3))
+        psi = np.zeros(len(world), np.float32)
+        if self.lib.ref_boundary_volumes(len(world), world, h, psi) != 0:
+            raise ValueError("compute_boundary_volumes threw")
+        return psi
+
+    def boundary_world_positions(self, local, body, body_pos, body_quat):
+        local = _f32(local, (-1, 3))
+        body = np.ascontiguousarray(body, dtype=np.int32)
+        bp = _f32(body_pos, (-1, 3))
+        bq = _f32(body_quat, (-1, 4))
+        out = np.zeros_like(local)
+        self.lib.ref_boundary_world_positions(len(local), local, body, len(bp), bp, bq, out)
+        return out
+
+    def fluid_world(self, settings: Settings, lower, upper, spacing, bodies, plane_y=None,
+                    boundary_extent=1.0, dt=1.0 / 60.0, nsteps=1, cap=1 << 20):
+        """The reference FluidWorld (fluid_world.cpp with its rigid World) after
+        nsteps steps.  bodies: list of (kind, size3, mass, pos3, quat4 (w, x, y,
+        z)) with kind "sphere" (size3[0] = radius) or "box" (half extents).
+        Returns (x, v, rho, lam, body_pos, body_quat, body_v, body_w)."""
+        nb = len(bodies)
+        kind = np.array([0 if b[0] == "sphere" else 1 for b in bodies] or [0], np.int32)
+        size = _f32([list(b[1]) for b in bodies] or [[0, 0, 0]], (-1, 3))
+        mass = _f32([b[2] for b in bodies] or [0])
+        pos = _f32([list(b[3]) for b in bodies] or [[0, 0, 0]], (-1, 3))
+        quat = _f32([list(b[4]) for b in bodies] or [[1, 0, 0, 0]], (-1, 4))
+        x = np.zeros((cap, 3), np.float32)
+        v = np.zeros((cap, 3), np.float32)
+        rho = np.zeros(cap, np.float32)
+        lam = np.zeros(cap, np.float32)
+        bp = np.zeros((max(nb, 1), 3), np.float32)
+        bq = np.zeros((max(nb, 1), 4), np.float32)
+        bv = np.zeros((max(nb, 1), 3), np.float32)
+        bw = np.zeros((max(nb, 1), 3), np.float32)
+        n = self.lib.ref_fluid_world_run(
+            C.byref(settings), _f32(lower, (3,)), _f32(upper, (3,)), spacing, nb, kind, size,
+            mass, pos, quat, 0 if plane_y is None else 1, 0.0 if plane_y is None else plane_y,
+            boundary_extent, dt, nsteps, cap, x, v, rho, lam, bp, bq, bv, bw)
+        if n < 0:
+            raise ValueError("the reference FluidWorld failed")
+        return x[:n], v[:n], rho[:n], lam[:n], bp[:nb], bq[:nb], bv[:nb], bw[:nb]
+
+    def _sampled(self, fn, *args):
+        m = fn(*args, None, 0)
+        out = np.zeros((max(m, 1), 3), np.float32)
+        fn(*args, out.ctypes.data, m)
+        return out[:m]
+
+    def sample_box(self, half, lt_pos=(0, 0, 0), lt_quat=(1, 0, 0, 0), spacing=0.1):
+        return self._sampled(self.lib.ref_sample_box, _f32(half, (3,)), _f32(lt_pos, (3,)),
+                             _f32(lt_quat, (4,)), spacing)
+
+    def sample_sphere(self, radius, lt_pos=(0, 0, 0), lt_quat=(1, 0, 0, 0), spacing=0.1):
+        return self._sampled(self.lib.ref_sample_sphere, radius, _f32(lt_pos, (3,)),
+                             _f32(lt_quat, (4,)), spacing)
+
+    def sample_plane(self, normal, offset, spacing, extent):
+        return self._sampled(self.lib.ref_sample_plane, _f32(normal, (3,)), offset, spacing,
+                             extent)
 
     def default_settings(self) -> Settings:
         s = Settings()

@@ -3,11 +3,18 @@
 // links it).  Built by oracle/build_oracle.py into oracle/_ref/ from the
 // reference's unmodified files
 //   src/fluid/pbf_solver.cpp, src/fluid/neighbor_search.cpp,
-//   src/fluid/particle_state.cpp, src/sim/performance_monitor.cpp
+//   src/fluid/particle_state.cpp, src/fluid/boundary.cpp,
+//   src/fluid/fluid_world.cpp, src/sim/performance_monitor.cpp, and the rigid
+//   pipeline FluidWorld inherits (src/sim/world.cpp, state.cpp, src/core/
+//   body.cpp, shape.cpp, model_builder.cpp, joint.cpp, src/collision/*.cpp,
+//   src/dynamics/free_body_solver.cpp, integrator.cpp, src/math/*.cpp)
 // against the Eigen-API subset in oracle/eigen_shim (Eigen3 is absent here).
 #include <cstring>
 #include <vector>
 
+#include "novaphy/core/model_builder.h"
+#include "novaphy/fluid/boundary.h"
+#include "novaphy/fluid/fluid_world.h"
 #include "novaphy/fluid/neighbor_search.h"
 #include "novaphy/fluid/particle_state.h"
 #include "novaphy/fluid/pbf_solver.h"
@@ -149,6 +156,150 @@ float ref_cubic_spline(float r, float h) { return SPHKernels::cubic_spline(r, h)
 void ref_spiky_grad(const float* r, float h, float* out) {
     Vec3f g = SPHKernels::spiky_grad(Vec3f(r[0], r[1], r[2]), h);
     for (int c = 0; c < 3; ++c) out[c] = g[c];
+}
+
+// Samplers (boundary.cpp:15-126) on a shape built from its fields; they write
+// up to cap body-frame positions and return the count.
+static int copy_samples(const std::vector<BoundaryParticle>& bp, float* out3, int cap) {
+    const int m = (int)bp.size();
+    if (out3)
+        for (int i = 0; i < m && i < cap; ++i)
+            for (int d = 0; d < 3; ++d) out3[3 * i + d] = bp[(size_t)i].local_position(d);
+    return m;
+}
+
+static Transform local_tf(const float* lt_pos, const float* lt_quat) {
+    Transform t;
+    t.position = Vec3f(lt_pos[0], lt_pos[1], lt_pos[2]);
+    t.rotation = Quatf(lt_quat[0], lt_quat[1], lt_quat[2], lt_quat[3]);
+    return t;
+}
+
+int ref_sample_box(const float* half, const float* lt_pos, const float* lt_quat, float spacing,
+                   float* out3, int cap) {
+    CollisionShape s;
+    s.type = ShapeType::Box;
+    s.box.half_extents = Vec3f(half[0], half[1], half[2]);
+    s.local_transform = local_tf(lt_pos, lt_quat);
+    s.body_index = 0;
+    return copy_samples(sample_box_boundary(s, spacing), out3, cap);
+}
+
+int ref_sample_sphere(float radius, const float* lt_pos, const float* lt_quat, float spacing,
+                      float* out3, int cap) {
+    CollisionShape s;
+    s.type = ShapeType::Sphere;
+    s.sphere.radius = radius;
+    s.local_transform = local_tf(lt_pos, lt_quat);
+    s.body_index = 0;
+    return copy_samples(sample_sphere_boundary(s, spacing), out3, cap);
+}
+
+int ref_sample_plane(const float* normal, float offset, float spacing, float extent, float* out3,
+                     int cap) {
+    CollisionShape s;
+    s.type = ShapeType::Plane;
+    s.plane.normal = Vec3f(normal[0], normal[1], normal[2]);
+    s.plane.offset = offset;
+    return copy_samples(sample_plane_boundary(s, spacing, extent), out3, cap);
+}
+
+// FluidWorld::step (fluid_world.cpp:46-99) over nsteps steps of a world with
+// one fluid block and nb bodies: kind[k] 0 = sphere (size[3k] = radius),
+// 1 = box (size[3k..3k+2] = half extents), mass[k], pose pos3/quat4 (w, x, y,
+// z), plus a ground plane at y = plane_y when with_plane.  Gravity is the
+// World default (0, -9.81, 0).  Writes the fluid state (n particles, as
+// ParticleState) and the bodies' poses and velocities; returns n, or -1.
+int ref_fluid_world_run(const ref_settings* st, const float* lower, const float* upper,
+                        float spacing, int nb, const int* kind, const float* size,
+                        const float* mass, const float* pos3, const float* quat4, int with_plane,
+                        float plane_y, float boundary_extent, float dt, int nsteps, int cap,
+                        float* x3, float* v3, float* rho, float* lam, float* body_pos3,
+                        float* body_quat4, float* body_v3, float* body_w3) {
+    try {
+        ModelBuilder mb;
+        if (with_plane) mb.add_ground_plane(plane_y);
+        for (int k = 0; k < nb; ++k) {
+            Transform t;
+            t.position = Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]);
+            t.rotation = Quatf(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2], quat4[4 * k + 3]);
+            if (kind[k] == 0) {
+                const int b = mb.add_body(RigidBody::from_sphere(mass[k], size[3 * k]), t);
+                mb.add_shape(CollisionShape::make_sphere(size[3 * k], b));
+            } else {
+                const Vec3f he(size[3 * k], size[3 * k + 1], size[3 * k + 2]);
+                const int b = mb.add_body(RigidBody::from_box(mass[k], he), t);
+                mb.add_shape(CollisionShape::make_box(he, b));
+            }
+        }
+        FluidBlockDef blk;
+        blk.lower = Vec3f(lower[0], lower[1], lower[2]);
+        blk.upper = Vec3f(upper[0], upper[1], upper[2]);
+        blk.particle_spacing = spacing;
+        FluidWorld fw(mb.build(), {blk}, SolverSettings{}, to_settings(st), boundary_extent);
+        for (int s = 0; s < nsteps; ++s) fw.step(dt);
+        const ParticleState& ps = fw.fluid_state();
+        const int n = ps.num_particles();
+        if (n > cap) return -1;
+        for (int i = 0; i < n; ++i) {
+            for (int d = 0; d < 3; ++d) {
+                x3[3 * i + d] = ps.positions[(size_t)i](d);
+                v3[3 * i + d] = ps.velocities[(size_t)i](d);
+            }
+            rho[i] = ps.densities[(size_t)i];
+            lam[i] = ps.lambdas[(size_t)i];
+        }
+        const SimState& ss = fw.state();
+        for (int k = 0; k < nb; ++k) {
+            const Transform& t = ss.transforms[(size_t)k];
+            for (int d = 0; d < 3; ++d) {
+                body_pos3[3 * k + d] = t.position(d);
+                body_v3[3 * k + d] = ss.linear_velocities[(size_t)k](d);
+                body_w3[3 * k + d] = ss.angular_velocities[(size_t)k](d);
+            }
+            body_quat4[4 * k] = t.rotation.w();
+            body_quat4[4 * k + 1] = t.rotation.x();
+            body_quat4[4 * k + 2] = t.rotation.y();
+            body_quat4[4 * k + 3] = t.rotation.z();
+        }
+        return n;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// Akinci volumes of boundary particles at world positions
+// (compute_boundary_volumes, boundary.cpp:152-176).  1 if it throws.
+int ref_boundary_volumes(int nb, const float* world3, float h, float* psi) {
+    std::vector<BoundaryParticle> bp((size_t)nb);
+    std::vector<Vec3f> w((size_t)nb);
+    for (int i = 0; i < nb; ++i) w[(size_t)i] = Vec3f(world3[3 * i], world3[3 * i + 1], world3[3 * i + 2]);
+    try {
+        compute_boundary_volumes(bp, w, h);
+    } catch (...) {
+        return 1;
+    }
+    for (int i = 0; i < nb; ++i) psi[i] = bp[(size_t)i].volume;
+    return 0;
+}
+
+// World positions of boundary particles under body poses (w, x, y, z
+// quaternions, taken as given) (boundary_world_positions, boundary.cpp:178-192).
+void ref_boundary_world_positions(int nb, const float* local3, const int* body, int nbodies,
+                                  const float* pos3, const float* quat4, float* out3) {
+    std::vector<BoundaryParticle> bp((size_t)nb);
+    for (int i = 0; i < nb; ++i) {
+        bp[(size_t)i].local_position = Vec3f(local3[3 * i], local3[3 * i + 1], local3[3 * i + 2]);
+        bp[(size_t)i].body_index = body[i];
+    }
+    std::vector<Transform> tr((size_t)nbodies);
+    for (int k = 0; k < nbodies; ++k) {
+        tr[(size_t)k].position = Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]);
+        tr[(size_t)k].rotation = Quatf(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2], quat4[4 * k + 3]);
+    }
+    const std::vector<Vec3f> w = boundary_world_positions(bp, tr);
+    for (int i = 0; i < nb; ++i)
+        for (int d = 0; d < 3; ++d) out3[3 * i + d] = w[(size_t)i](d);
 }
 
 }  // extern "C"
