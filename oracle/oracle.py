@@ -284,6 +284,10 @@ class Ref:
                                           C.c_float, C.c_float, C.c_int, C.c_int, _f32p, _f32p,
                                           _f32p, _f32p, _f32p, _f32p, _f32p, _f32p]
         L.ref_fluid_world_run.restype = C.c_int
+        L.ref_world_run.argtypes = [C.c_int, _i32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
+                                    C.c_void_p, C.c_void_p, C.c_float, C.c_int, _f32p, _f32p,
+                                    _f32p, _f32p]
+        L.ref_world_run.restype = C.c_int
         L.ref_sample_box.argtypes = [_f32p, _f32p, _f32p, C.c_float, C.c_void_p, C.c_int]
         L.ref_sample_sphere.argtypes = [C.c_float, _f32p, _f32p, C.c_float, C.c_void_p, C.c_int]
         L.ref_sample_plane.argtypes = [_f32p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_int]
@@ -331,6 +335,29 @@ class Ref:
         if n < 0:
             raise ValueError("the reference FluidWorld failed")
         return x[:n], v[:n], rho[:n], lam[:n], bp[:nb], bq[:nb], bv[:nb], bw[:nb]
+
+    def world(self, bodies, lin, ang, dt, nsteps, force=None, torque=None):
+        """The reference rigid World (no ground plane) after nsteps steps of
+        free bodies (as fluid_world's bodies) from velocities lin/ang, with
+        constant force/torque applied before each step.  Returns
+        (pos, quat (w, x, y, z), lin_vel, ang_vel)."""
+        nb = len(bodies)
+        kind = np.array([0 if b[0] == "sphere" else 1 for b in bodies], np.int32)
+        size = _f32([list(b[1]) for b in bodies], (-1, 3))
+        mass = _f32([b[2] for b in bodies])
+        pos = _f32([list(b[3]) for b in bodies], (-1, 3))
+        quat = _f32([list(b[4]) for b in bodies], (-1, 4))
+        f = None if force is None else _f32(force, (-1, 3))
+        t = None if torque is None else _f32(torque, (-1, 3))
+        out = [np.zeros((nb, 3), np.float32), np.zeros((nb, 4), np.float32),
+               np.zeros((nb, 3), np.float32), np.zeros((nb, 3), np.float32)]
+        rc = self.lib.ref_world_run(nb, kind, size, mass, pos, quat, _f32(lin, (-1, 3)),
+                                    _f32(ang, (-1, 3)),
+                                    None if f is None else f.ctypes.data,
+                                    None if t is None else t.ctypes.data, dt, nsteps, *out)
+        if rc:
+            raise ValueError("the reference World failed")
+        return tuple(out)
 
     def _sampled(self, fn, *args):
         m = fn(*args, None, 0)

@@ -268,6 +268,62 @@ int ref_fluid_world_run(const ref_settings* st, const float* lower, const float*
     }
 }
 
+// World::step (world.cpp) over nsteps steps of nb free bodies (kind, size,
+// mass and pose as ref_fluid_world_run) starting from linear and angular
+// velocities lin3/ang3, with optional constant forces/torques applied before
+// every step (force3/torque3, may be null).  No ground plane.  Writes poses and
+// velocities.  Returns 0, or -1.
+int ref_world_run(int nb, const int* kind, const float* size, const float* mass,
+                  const float* pos3, const float* quat4, const float* lin3, const float* ang3,
+                  const float* force3, const float* torque3, float dt, int nsteps,
+                  float* body_pos3, float* body_quat4, float* body_v3, float* body_w3) {
+    try {
+        ModelBuilder mb;
+        for (int k = 0; k < nb; ++k) {
+            Transform t;
+            t.position = Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]);
+            t.rotation = Quatf(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2], quat4[4 * k + 3]);
+            if (kind[k] == 0) {
+                const int b = mb.add_body(RigidBody::from_sphere(mass[k], size[3 * k]), t);
+                mb.add_shape(CollisionShape::make_sphere(size[3 * k], b));
+            } else {
+                const Vec3f he(size[3 * k], size[3 * k + 1], size[3 * k + 2]);
+                const int b = mb.add_body(RigidBody::from_box(mass[k], he), t);
+                mb.add_shape(CollisionShape::make_box(he, b));
+            }
+        }
+        World w(mb.build(), SolverSettings{});
+        for (int k = 0; k < nb; ++k) {
+            w.state().set_linear_velocity(k, Vec3f(lin3[3 * k], lin3[3 * k + 1], lin3[3 * k + 2]));
+            w.state().set_angular_velocity(k, Vec3f(ang3[3 * k], ang3[3 * k + 1], ang3[3 * k + 2]));
+        }
+        for (int s = 0; s < nsteps; ++s) {
+            for (int k = 0; k < nb; ++k) {
+                if (force3) w.apply_force(k, Vec3f(force3[3 * k], force3[3 * k + 1], force3[3 * k + 2]));
+                if (torque3)
+                    w.apply_torque(k, Vec3f(torque3[3 * k], torque3[3 * k + 1], torque3[3 * k + 2]));
+            }
+            w.step(dt);
+        }
+        const SimState& ss = w.state();
+        for (int k = 0; k < nb; ++k) {
+            const Transform& t = ss.transforms[(size_t)k];
+            for (int d = 0; d < 3; ++d) {
+                body_pos3[3 * k + d] = t.position(d);
+                body_v3[3 * k + d] = ss.linear_velocities[(size_t)k](d);
+                body_w3[3 * k + d] = ss.angular_velocities[(size_t)k](d);
+            }
+            body_quat4[4 * k] = t.rotation.w();
+            body_quat4[4 * k + 1] = t.rotation.x();
+            body_quat4[4 * k + 2] = t.rotation.y();
+            body_quat4[4 * k + 3] = t.rotation.z();
+        }
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
 // Akinci volumes of boundary particles at world positions
 // (compute_boundary_volumes, boundary.cpp:152-176).  1 if it throws.
 int ref_boundary_volumes(int nb, const float* world3, float h, float* psi) {

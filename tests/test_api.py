@@ -202,3 +202,44 @@ def test_monitor_trace_json_and_reset(tmp_path):
     assert mon.phase_stats() == [] and mon.last_frame_metrics() == [] and mon.frame_count == 0
     mon.write_trace_json(str(path))
     assert json.loads(path.read_text())["traceEvents"] == []
+
+
+def test_host_world_free_bodies_match_reference_build(ref):
+    """The host World's rigid step (free bodies: symplectic Euler with angular
+    damping, quaternion update) against the reference's World compiled from
+    its sources, bit for bit, with spinning bodies and constant wrenches."""
+    bodies = [("sphere", (0.12, 0.0, 0.0), 0.5, (0.0, 1.0, 0.0), (1.0, 0.0, 0.0, 0.0)),
+              ("box", (0.1, 0.05, 0.08), 0.8, (2.0, 3.0, -1.0), (0.5, 0.5, 0.5, 0.5))]
+    lin = np.array([[0.3, 1.0, -0.2], [-1.0, 0.5, 0.25]], np.float32)
+    ang = np.array([[0.0, 2.0, 1.0], [3.0, -1.0, 0.5]], np.float32)
+    force = np.array([[0.1, 2.0, 0.0], [0.0, 0.0, -1.5]], np.float32)
+    torque = np.array([[0.01, 0.0, -0.02], [0.0, 0.03, 0.01]], np.float32)
+    dt, steps = float(np.float32(1 / 120)), 50
+    rp, rq, rv, rw = ref.world(bodies, lin, ang, dt, steps, force, torque)
+
+    mb = novaphy.ModelBuilder()
+    for kind, size, mass, pos, q in bodies:
+        t = novaphy.Transform(np.array(pos, np.float32), [q[1], q[2], q[3], q[0]])
+        if kind == "sphere":
+            i = mb.add_body(novaphy.RigidBody.from_sphere(mass, size[0]), t)
+            mb.add_shape(novaphy.CollisionShape.make_sphere(size[0], i))
+        else:
+            he = np.array(size, np.float32)
+            i = mb.add_body(novaphy.RigidBody.from_box(mass, he), t)
+            mb.add_shape(novaphy.CollisionShape.make_box(he, i))
+    w = novaphy.World(mb.build(), novaphy.SolverSettings())
+    for k in range(2):
+        w.state.set_linear_velocity(k, lin[k])
+        w.state.set_angular_velocity(k, ang[k])
+    for _ in range(steps):
+        for k in range(2):
+            w.apply_force(k, force[k])
+            w.apply_torque(k, torque[k])
+        w.step(dt)
+    for k in range(2):
+        tr = w.state.transforms[k]
+        q = np.asarray(tr.rotation, np.float32)  # x, y, z, w
+        assert np.array_equal(np.asarray(tr.position, np.float32), rp[k]), k
+        assert np.array_equal(np.array([q[3], q[0], q[1], q[2]], np.float32), rq[k]), k
+        assert np.array_equal(np.asarray(w.state.linear_velocities[k], np.float32), rv[k]), k
+        assert np.array_equal(np.asarray(w.state.angular_velocities[k], np.float32), rw[k]), k
