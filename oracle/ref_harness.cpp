@@ -207,7 +207,7 @@ int ref_sample_plane(const float* normal, float offset, float spacing, float ext
 // FluidWorld::step (fluid_world.cpp:46-99) over nsteps steps of a world with
 // one fluid block and nb bodies: kind[k] 0 = sphere (size[3k] = radius),
 // 1 = box (size[3k..3k+2] = half extents), mass[k], pose pos3/quat4 (w, x, y,
-// z), plus a ground plane at y = plane_y when with_plane.  Gravity is the
+// z; normalised), plus a ground plane at y = plane_y when with_plane.  Gravity is the
 // World default (0, -9.81, 0).  Writes the fluid state (n particles, as
 // ParticleState) and the bodies' poses and velocities; returns n, or -1.
 int ref_fluid_world_run(const ref_settings* st, const float* lower, const float* upper,
@@ -220,9 +220,10 @@ int ref_fluid_world_run(const ref_settings* st, const float* lower, const float*
         ModelBuilder mb;
         if (with_plane) mb.add_ground_plane(plane_y);
         for (int k = 0; k < nb; ++k) {
-            Transform t;
-            t.position = Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]);
-            t.rotation = Quatf(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2], quat4[4 * k + 3]);
+            // Transform(p, q) normalises q, as the reference's Python API does.
+            const Transform t(Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]),
+                              Quatf(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2],
+                                    quat4[4 * k + 3]));
             if (kind[k] == 0) {
                 const int b = mb.add_body(RigidBody::from_sphere(mass[k], size[3 * k]), t);
                 mb.add_shape(CollisionShape::make_sphere(size[3 * k], b));
@@ -280,9 +281,10 @@ int ref_world_run(int nb, const int* kind, const float* size, const float* mass,
     try {
         ModelBuilder mb;
         for (int k = 0; k < nb; ++k) {
-            Transform t;
-            t.position = Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]);
-            t.rotation = Quatf(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2], quat4[4 * k + 3]);
+            // Transform(p, q) normalises q, as the reference's Python API does.
+            const Transform t(Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]),
+                              Quatf(quat4[4 * k], quat4[4 * k + 1], quat4[4 * k + 2],
+                                    quat4[4 * k + 3]));
             if (kind[k] == 0) {
                 const int b = mb.add_body(RigidBody::from_sphere(mass[k], size[3 * k]), t);
                 mb.add_shape(CollisionShape::make_sphere(size[3 * k], b));

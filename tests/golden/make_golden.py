@@ -7,6 +7,7 @@ oracle restatement (oracle/pbf_oracle.c) reproduces every fixture bit for
 bit, so the fixtures pin the restatement.
 
 Run from the repository root:  python tests/golden/make_golden.py
+(fluid_world.npz alone: python tests/golden/make_golden.py fluid_world)
 """
 from __future__ import annotations
 
@@ -126,5 +127,39 @@ def main():
     print("fixtures written", out)
 
 
+# The coupled scene of fluid_world.npz: a fluid block over a ground plane, a
+# sphere and a rotated box in opposite corners, apart from each other and from
+# the plane through these steps (at least 0.2 m between centres, against 0.15
+# for a contact), so that the reference's contact solver stays idle; h = 0.2,
+# 2 iterations, dt = 1/60, 5 steps.
+FLUID_WORLD = dict(
+    lower=[0.0, 0.05, 0.0], upper=[0.3, 0.4, 0.3], spacing=0.05, plane_y=0.0,
+    boundary_extent=0.5, steps=5,
+    bodies=[("sphere", (0.08, 0.0, 0.0), 0.5, (0.06, 0.25, 0.06), (1.0, 0.0, 0.0, 0.0)),
+            ("box", (0.04, 0.04, 0.04), 0.8, (0.26, 0.33, 0.26),
+             (0.96592583, 0.0, 0.25881904, 0.0))],
+)
+
+
+def fluid_world_fixture():
+    """FluidWorld.step of the reference (fluid_world.cpp with its rigid
+    World, built from its sources) on the coupled scene, 5 steps."""
+    R = Ref()
+    c = FLUID_WORLD
+    s = Settings.make(kernel_radius=0.2, solver_iterations=2)
+    dt = float(np.float32(1 / 60))
+    x, v, rho, lam, bp, bq, bv, bw = R.fluid_world(
+        s, c["lower"], c["upper"], c["spacing"], c["bodies"], plane_y=c["plane_y"],
+        boundary_extent=c["boundary_extent"], dt=dt, nsteps=c["steps"])
+    np.savez_compressed(os.path.join(HERE, "fluid_world.npz"), x=x, v=v, rho=rho, lam=lam,
+                        body_pos=bp, body_quat=bq, body_v=bv, body_w=bw)
+    print("fluid_world.npz written:", len(x), "particles")
+
+
 if __name__ == "__main__":
-    main()
+    # With names, only those fixtures: python tests/golden/make_golden.py fluid_world
+    if sys.argv[1:] == ["fluid_world"]:
+        fluid_world_fixture()
+    else:
+        main()
+        fluid_world_fixture()

@@ -202,3 +202,49 @@ def test_fluid_world_step_matches_oracle(port):
     g = np.array([0, -9.81, 0], np.float32)
     v_want = (g + f[0] * inv_m) * np.float32(dt)
     npt.assert_array_equal(np.asarray(w.state.linear_velocities[0], np.float32), v_want)
+
+
+def test_fluid_world_matches_reference_fixture():
+    """Five FluidWorld steps of a coupled scene (fluid block, ground plane, a
+    sphere and a rotated box that stay clear of each other and of the plane, so
+    the reference's contact solver has nothing to do) against the reference's own FluidWorld built
+    from its sources (tests/golden/fluid_world.npz, make_golden.py): fluid
+    state with boundary density and the bodies' poses and velocities, bit for
+    bit."""
+    g = np.load(os.path.join(GOLDEN, "fluid_world.npz"))
+    mb = novaphy.ModelBuilder()
+    mb.add_ground_plane(y=0.0)
+    i = mb.add_body(novaphy.RigidBody.from_sphere(0.5, 0.08),
+                    novaphy.Transform(np.array([0.06, 0.25, 0.06], np.float32), [0, 0, 0, 1]))
+    mb.add_shape(novaphy.CollisionShape.make_sphere(0.08, i))
+    he = np.array([0.04, 0.04, 0.04], np.float32)
+    i = mb.add_body(novaphy.RigidBody.from_box(0.8, he),
+                    novaphy.Transform(np.array([0.26, 0.33, 0.26], np.float32),
+                                      [0.0, 0.25881904, 0.0, 0.96592583]))
+    mb.add_shape(novaphy.CollisionShape.make_box(he, i))
+    pbf = novaphy.PBFSettings()
+    pbf.kernel_radius = 0.2
+    pbf.solver_iterations = 2
+    blk = novaphy.FluidBlockDef()
+    blk.lower = np.array([0.0, 0.05, 0.0], np.float32)
+    blk.upper = np.array([0.3, 0.4, 0.3], np.float32)
+    blk.particle_spacing = 0.05
+    fw = novaphy.FluidWorld(mb.build(), [blk], novaphy.SolverSettings(), pbf,
+                            boundary_extent=0.5)
+    dt = float(np.float32(1 / 60))
+    for _ in range(5):
+        fw.step(dt)
+    fs = fw.fluid_state
+    assert np.array_equal(fs.positions_array, g["x"])
+    assert np.array_equal(fs.velocities_array, g["v"])
+    assert np.array_equal(fs.densities_array, g["rho"])
+    assert np.array_equal(np.asarray(fs.lambdas, np.float32), g["lam"])
+    for k in range(2):
+        tr = fw.state.transforms[k]
+        q = np.asarray(tr.rotation, np.float32)  # x, y, z, w
+        assert np.array_equal(np.asarray(tr.position, np.float32), g["body_pos"][k]), k
+        assert np.array_equal(np.array([q[3], q[0], q[1], q[2]], np.float32), g["body_quat"][k]), k
+        assert np.array_equal(np.asarray(fw.state.linear_velocities[k], np.float32),
+                              g["body_v"][k]), k
+        assert np.array_equal(np.asarray(fw.state.angular_velocities[k], np.float32),
+                              g["body_w"][k]), k
