@@ -207,8 +207,13 @@ int check_settings(const pbf_settings* st) {
     return PBF_OK;
 }
 
-// Grid fitted to the domain (clamp on) or to the particles' bounding box,
-// with two cells of margin; each axis >= 4 and at most 2^24 slots in total.
+// Grid fitted to the domain (clamp on, two cells of margin) or to the
+// particles' bounding box (clamp off).  Without the clamp nothing keeps the
+// fluid inside its first box, so that grid gets max(8, extent) cells of
+// margin per side, up to 256: a resident scene whose fluid falls or spreads
+// keeps its particles in the grid for many steps instead of wrapping onto the
+// slower aliased-bucket walk (any fit gives the same results).  Each axis
+// >= 4 and at most 2^24 slots in total.
 GridDesc fit_grid(const pbf_scene* s) {
     const pbf_settings& st = s->settings;
     const float inv = 1.0f / st.kernel_radius;
@@ -225,16 +230,30 @@ GridDesc fit_grid(const pbf_scene* s) {
             hi[d] = 0.0f;
         }
     }
-    long long o[3], g[3];
+    const long long kMaxSlots = 1LL << 24;
+    long long a0[3], ext[3], mar[3];
     for (int d = 0; d < 3; ++d) {
         double a = std::floor((double)lo[d] * inv), b = std::floor((double)hi[d] * inv);
         if (!std::isfinite(a) || !std::isfinite(b) || b - a > 4096.0) b = a + 4096.0;
         if (!std::isfinite(a) || std::fabs(a) > 1e9) a = 0.0, b = 4096.0;
-        o[d] = (long long)a - 2;
-        g[d] = (long long)(b - a) + 5;
-        if (g[d] < 4) g[d] = 4;
+        a0[d] = (long long)a;
+        ext[d] = (long long)(b - a);
+        mar[d] = st.use_domain_bounds ? 2 : std::min<long long>(256, std::max<long long>(8, ext[d]));
     }
-    const long long kMaxSlots = 1LL << 24;
+    // The margin gives way first when the slots would exceed the cap.
+    auto slots = [&](long long cap_m) {
+        long long p = 1;
+        for (int d = 0; d < 3; ++d) p *= std::max(4LL, ext[d] + 2 * std::min(mar[d], cap_m) + 1);
+        return p;
+    };
+    long long cap_m = 256;
+    while (cap_m > 2 && slots(cap_m) > kMaxSlots) cap_m /= 2;
+    long long o[3], g[3];
+    for (int d = 0; d < 3; ++d) {
+        const long long m = std::max(2LL, std::min(mar[d], cap_m));
+        o[d] = a0[d] - m;
+        g[d] = std::max(4LL, ext[d] + 2 * m + 1);
+    }
     while (g[0] * g[1] * g[2] > kMaxSlots) {
         int m = 0;
         for (int d = 1; d < 3; ++d)
