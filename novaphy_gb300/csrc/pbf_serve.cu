@@ -7,19 +7,22 @@
 // step of every scene with an issuable request, oldest request first, up to
 // the per-launch particle and scene caps.  A heavily loaded launch takes
 // further steps of the scenes with the deepest queues (up to kMaxSubSteps
-// each; see build_launch): the batch runs them as consecutive steps, so deep
-// queues drain at several steps per launch instead of one.  Up to max_inflight launches are
-// queued on the batch stream; while they run, the scheduler builds the next
-// one from whatever is pending then (continuous batching), and a scene can
-// be in several queued launches at once because the stream orders them.
+// each; launch_plan.hpp): the batch runs them as consecutive steps, so deep
+// queues drain at several steps per launch instead of one.  Up to
+// max_inflight launches are queued on the batch stream; while they run, the
+// scheduler builds the next one from whatever is pending then (continuous
+// batching), and a scene can be in several queued launches at once because
+// the stream orders them.
 // A second thread waits on the oldest launch's event and retires its steps,
 // which frees its slot for the next launch.
 //
 // Coupled scenes (FluidWorld with rigid bodies) step like the others: right
 // after a launch is issued, the issue thread enqueues on each coupled scene's
-// stream the coupling of its step and the rigid step of its bodies, which live
-// on the device.  The next launch waits for the scene's stream, so the device
-// runs step, coupling, rigid step, next step in order with no host round trip.
+// stream the coupling of its last step and the rigid step of its bodies,
+// which live on the device (between two steps of one launch, the batch does
+// the same and waits for it).  The next launch waits for the scene's stream,
+// so the device runs step, coupling, rigid step, next step in order with no
+// host round trip.
 //
 // Admission.  A scene is charged state_bytes * n + grid_bytes * slots of its
 // grid (the share of the batch's offset table a launch holding it can use).
