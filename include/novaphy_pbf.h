@@ -411,9 +411,9 @@ int pbf_server_submit(pbf_server* server, long long scene_id, float dt, int nste
  * server keeps the records of the latest 65536 finished requests; waiting on
  * an older finished request returns PBF_ERR_INVALID_ARG. */
 int pbf_server_wait(pbf_server* server, long long request_id, double timeout_s, int* state_out);
-/* A rigid body of a served coupled scene: the state World's rigid step
- * integrates (free bodies, no contacts; src/dynamics/integrator.cpp), which
- * the server runs on the device.
+/* A rigid body of a served coupled scene: the state World's semi-implicit
+ * Euler integrates (src/dynamics/integrator.cpp), which the server runs on
+ * the device for free bodies (served scenes model no rigid contacts).
  * inv_mass 0 marks a static body; inv_inertia is RigidBody::inv_inertia,
  * row-major. */
 typedef struct pbf_rigid_body {

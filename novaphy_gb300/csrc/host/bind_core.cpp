@@ -110,7 +110,50 @@ PYBIND11_MODULE(_core, m) {
                     py::arg("body_idx"), py::arg("local") = Transform::identity(),
                     py::arg("friction") = 0.5f, py::arg("restitution") = 0.3f)
         .def_static("make_plane", &CollisionShape::make_plane, py::arg("normal"), py::arg("offset"),
-                    py::arg("friction") = 0.5f, py::arg("restitution") = 0.0f);
+                    py::arg("friction") = 0.5f, py::arg("restitution") = 0.0f)
+        .def("compute_aabb", &CollisionShape::compute_aabb, py::arg("body_transform"));
+
+    py::class_<AABB>(m, "AABB")
+        .def(py::init<>())
+        .def(py::init<const Vec3&, const Vec3&>(), py::arg("min"), py::arg("max"))
+        .def_readwrite("min", &AABB::min)
+        .def_readwrite("max", &AABB::max)
+        .def("overlaps", &AABB::overlaps, py::arg("other"))
+        .def("center", &AABB::center)
+        .def("half_extents", &AABB::half_extents)
+        .def("surface_area", &AABB::surface_area)
+        .def("is_valid", &AABB::is_valid)
+        .def_static("from_sphere", &AABB::from_sphere, py::arg("center"), py::arg("radius"));
+
+    py::class_<ContactPoint>(m, "ContactPoint")
+        .def(py::init<>())
+        .def_readwrite("position", &ContactPoint::position)
+        .def_readwrite("normal", &ContactPoint::normal)
+        .def_readwrite("penetration", &ContactPoint::penetration)
+        .def_readwrite("body_a", &ContactPoint::body_a)
+        .def_readwrite("body_b", &ContactPoint::body_b)
+        .def_readwrite("friction", &ContactPoint::friction)
+        .def_readwrite("restitution", &ContactPoint::restitution);
+
+    py::class_<BroadPhasePair>(m, "BroadPhasePair")
+        .def(py::init<>())
+        .def_readwrite("body_a", &BroadPhasePair::body_a)
+        .def_readwrite("body_b", &BroadPhasePair::body_b);
+
+    py::class_<SweepAndPrune>(m, "SweepAndPrune")
+        .def(py::init<>())
+        .def("update", &SweepAndPrune::update, py::arg("aabbs"), py::arg("static_mask"))
+        .def("get_pairs", &SweepAndPrune::get_pairs);
+
+    m.def(
+        "collide_shapes",
+        [](const CollisionShape& a, const Transform& ta, const CollisionShape& b,
+           const Transform& tb) {
+            std::vector<ContactPoint> c;
+            const bool hit = collide_shapes(a, ta, b, tb, c);
+            return py::make_tuple(hit, c);
+        },
+        py::arg("shape_a"), py::arg("transform_a"), py::arg("shape_b"), py::arg("transform_b"));
 
     py::class_<RigidBody>(m, "RigidBody")
         .def(py::init<>())
@@ -121,6 +164,17 @@ PYBIND11_MODULE(_core, m) {
             const auto a = b.inv_inertia();
             return std::vector<float>(a.begin(), a.end());
         })
+        .def_property(
+            "inertia",
+            [](const RigidBody& b) {
+                py::array_t<float> a({3, 3});
+                std::memcpy(a.mutable_data(), b.inertia.data(), 9 * sizeof(float));
+                return a;
+            },
+            [](RigidBody& b, py::array_t<float, py::array::c_style | py::array::forcecast> a) {
+                if (a.size() != 9) throw py::value_error("inertia must be 3x3");
+                std::memcpy(b.inertia.data(), a.data(), 9 * sizeof(float));
+            })
         .def("is_static", &RigidBody::is_static)
         .def_static("from_box", &RigidBody::from_box, py::arg("mass"), py::arg("half_extents"))
         .def_static("from_sphere", &RigidBody::from_sphere, py::arg("mass"), py::arg("radius"))
@@ -141,7 +195,9 @@ PYBIND11_MODULE(_core, m) {
         .def("add_shape", &ModelBuilder::add_shape, py::arg("shape"))
         .def("add_ground_plane", &ModelBuilder::add_ground_plane, py::arg("y") = 0.0f,
              py::arg("friction") = 0.5f, py::arg("restitution") = 0.0f)
-        .def("build", &ModelBuilder::build);
+        .def("build", &ModelBuilder::build)
+        .def_property_readonly("num_bodies", &ModelBuilder::num_bodies)
+        .def_property_readonly("num_shapes", &ModelBuilder::num_shapes);
 
     py::class_<SolverSettings>(m, "SolverSettings")
         .def(py::init<>())
@@ -149,7 +205,10 @@ PYBIND11_MODULE(_core, m) {
         .def_readwrite("baumgarte", &SolverSettings::baumgarte)
         .def_readwrite("slop", &SolverSettings::slop)
         .def_readwrite("warm_starting", &SolverSettings::warm_starting)
-        .def_readwrite("sleep_enabled", &SolverSettings::sleep_enabled);
+        .def_readwrite("sleep_enabled", &SolverSettings::sleep_enabled)
+        .def_readwrite("sleep_energy_threshold", &SolverSettings::sleep_energy_threshold)
+        .def_readwrite("sleep_time_required", &SolverSettings::sleep_time_required)
+        .def_readwrite("sleep_ema_alpha", &SolverSettings::sleep_ema_alpha);
 
     py::class_<SimState>(m, "SimState")
         .def(py::init<>())
@@ -159,7 +218,12 @@ PYBIND11_MODULE(_core, m) {
         .def("set_linear_velocity", &SimState::set_linear_velocity, py::arg("body_index"),
              py::arg("velocity"))
         .def("set_angular_velocity", &SimState::set_angular_velocity, py::arg("body_index"),
-             py::arg("velocity"));
+             py::arg("velocity"))
+        .def("apply_force", &SimState::apply_force, py::arg("body_index"), py::arg("force"))
+        .def("apply_torque", &SimState::apply_torque, py::arg("body_index"), py::arg("torque"))
+        .def_readonly("sleeping", &SimState::sleeping)
+        .def_readonly("island_id", &SimState::island_id)
+        .def("is_sleeping", &SimState::is_sleeping, py::arg("body_index"));
 
     py::class_<PhaseStat>(m, "PerformancePhaseStat")
         .def_readonly("name", &PhaseStat::name)
@@ -194,6 +258,7 @@ PYBIND11_MODULE(_core, m) {
         .def_property_readonly("gravity", &World::gravity)
         .def_property_readonly("state", &World::state, py::return_value_policy::reference_internal)
         .def_property_readonly("model", &World::model, py::return_value_policy::reference_internal)
+        .def_property_readonly("contacts", &World::contacts)
         .def_property_readonly("performance_monitor", &World::performance_monitor,
                                py::return_value_policy::reference_internal)
         .def("apply_force", &World::apply_force, py::arg("body_index"), py::arg("force"))

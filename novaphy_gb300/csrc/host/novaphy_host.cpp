@@ -333,22 +333,6 @@ std::vector<BoundaryParticle> sample_model_boundaries(const Model& model, float 
 
 // ---- world ----
 
-void SimState::init(const std::vector<Transform>& t) {
-    transforms = t;
-    linear_velocities.assign(t.size(), Vec3{});
-    angular_velocities.assign(t.size(), Vec3{});
-    forces.assign(t.size(), Vec3{});
-    torques.assign(t.size(), Vec3{});
-}
-
-void SimState::set_linear_velocity(int i, const Vec3& v) {
-    if (i >= 0 && i < (int)linear_velocities.size()) linear_velocities[(size_t)i] = v;
-}
-
-void SimState::set_angular_velocity(int i, const Vec3& w) {
-    if (i >= 0 && i < (int)angular_velocities.size()) angular_velocities[(size_t)i] = w;
-}
-
 void PerformanceMonitor::begin_frame() {
     pending_.clear();
     trace_cur_.clear();
@@ -499,16 +483,23 @@ struct Scope {
 };
 }  // namespace
 
-World::World(const Model& model, SolverSettings settings) : model_(model), settings_(settings) {
+World::World(const Model& model, SolverSettings settings) : model_(model), solver_(settings) {
+    for (const CollisionShape& sh : model_.shapes)
+        if (sh.body_index >= model_.num_bodies())
+            throw std::invalid_argument("shape refers to a body the model does not have");
     state_.init(model_.initial_transforms);
 }
 
+// With sleep on, a force or torque first wakes a sleeping body (at rest, its
+// island with it), world.cpp:184-218.
 void World::apply_force(int i, const Vec3& f) {
-    if (i >= 0 && i < (int)state_.forces.size()) state_.forces[(size_t)i] += f;
+    if (solver_.settings().sleep_enabled && state_.is_sleeping(i)) state_.wake_body(i);
+    state_.apply_force(i, f);
 }
 
 void World::apply_torque(int i, const Vec3& t) {
-    if (i >= 0 && i < (int)state_.torques.size()) state_.torques[(size_t)i] += t;
+    if (solver_.settings().sleep_enabled && state_.is_sleeping(i)) state_.wake_body(i);
+    state_.apply_torque(i, t);
 }
 
 void World::step(float dt) {
@@ -517,14 +508,30 @@ void World::step(float dt) {
     monitor_.end_frame();
 }
 
+float World::kinetic_energy(int i) const {
+    const RigidBody& b = model_.bodies[(size_t)i];
+    const Vec3& v = state_.linear_velocities[(size_t)i];
+    const Vec3& w = state_.angular_velocities[(size_t)i];
+    const auto& I = b.inertia;
+    const Vec3 iw(I[0] * w.x + (I[1] * w.y + I[2] * w.z), I[3] * w.x + (I[4] * w.y + I[5] * w.z),
+                  I[6] * w.x + (I[7] * w.y + I[8] * w.z));
+    return b.mass * v.squaredNorm() + w.dot(iw);
+}
+
+// The reference's step order (world.cpp:30-182); sleeping bodies neither
+// integrate nor move, and count as static in the broad phase.
 void World::step_rigid_pipeline(float dt) {
     Scope total(monitor_, "world.total");
     const int n = model_.num_bodies();
+    const SolverSettings& set = solver_.settings();
+    const bool sleep = set.sleep_enabled;
+    int dynamic = 0;
     {
         Scope s(monitor_, "world.integrate_velocity");
         for (int i = 0; i < n; ++i) {
             const RigidBody& b = model_.bodies[(size_t)i];
-            if (b.is_static()) continue;
+            if (b.is_static() || (sleep && state_.is_sleeping(i))) continue;
+            ++dynamic;
             Vec3& v = state_.linear_velocities[(size_t)i];
             Vec3& w = state_.angular_velocities[(size_t)i];
             const float g[3] = {gravity_.x, gravity_.y, gravity_.z};
@@ -536,12 +543,77 @@ void World::step_rigid_pipeline(float dt) {
             pbf_rigid::integrate_velocity(va, wa, g, fa, b.inv_mass(), ii.data(), ta, dt);
             v = Vec3(va[0], va[1], va[2]);
             w = Vec3(wa[0], wa[1], wa[2]);
+            if (sleep) state_.update_energy(i, kinetic_energy(i), set.sleep_ema_alpha);
         }
+    }
+    const int ns = model_.num_shapes();
+    std::vector<AABB> boxes((size_t)ns);
+    std::vector<bool> fixed((size_t)ns);
+    {
+        Scope s(monitor_, "world.broadphase.build_aabbs");
+        for (int k = 0; k < ns; ++k) {
+            const CollisionShape& sh = model_.shapes[(size_t)k];
+            if (sh.body_index >= 0) {
+                boxes[(size_t)k] = sh.compute_aabb(state_.transforms[(size_t)sh.body_index]);
+                fixed[(size_t)k] = model_.bodies[(size_t)sh.body_index].is_static() ||
+                                   (sleep && state_.is_sleeping(sh.body_index));
+            } else {
+                boxes[(size_t)k] = sh.compute_aabb(Transform::identity());
+                fixed[(size_t)k] = true;
+            }
+        }
+    }
+    {
+        Scope s(monitor_, "world.broadphase.sap");
+        broadphase_.update(boxes, fixed);
+    }
+    contacts_.clear();
+    {
+        Scope s(monitor_, "world.narrowphase.total");
+        std::vector<ContactPoint> found;
+        for (const BroadPhasePair& p : broadphase_.get_pairs()) {
+            const CollisionShape& sa = model_.shapes[(size_t)p.body_a];
+            const CollisionShape& sb = model_.shapes[(size_t)p.body_b];
+            const Transform ta =
+                sa.body_index >= 0 ? state_.transforms[(size_t)sa.body_index] : Transform::identity();
+            const Transform tb =
+                sb.body_index >= 0 ? state_.transforms[(size_t)sb.body_index] : Transform::identity();
+            found.clear();
+            if (!collide_shapes(sa, ta, sb, tb, found)) continue;
+            for (ContactPoint& c : found) {
+                c.friction = combine_friction(sa.friction, sb.friction);
+                c.restitution = combine_restitution(sa.restitution, sb.restitution);
+                contacts_.push_back(c);
+            }
+        }
+    }
+    if (sleep) {
+        Scope s(monitor_, "world.build_islands");
+        state_.build_islands(contacts_);
+    }
+    {
+        Scope s(monitor_, "world.solver.total");
+        solver_.solve(contacts_, model_.bodies, state_.transforms, state_.linear_velocities,
+                      state_.angular_velocities, state_.sleeping, dt, &monitor_);
+    }
+    if (sleep) {
+        {
+            // an awake body touching a sleeping one wakes the sleeper's island
+            Scope s(monitor_, "world.propagate_wakes");
+            for (const ContactPoint& c : contacts_) {
+                const bool a = c.body_a >= 0 && state_.is_sleeping(c.body_a);
+                const bool b = c.body_b >= 0 && state_.is_sleeping(c.body_b);
+                if (a && !b) state_.propagate_wake_through_island(c.body_a);
+                else if (!a && b) state_.propagate_wake_through_island(c.body_b);
+            }
+        }
+        Scope s(monitor_, "world.evaluate_sleep");
+        state_.evaluate_sleep(dt, set.sleep_energy_threshold, set.sleep_time_required);
     }
     {
         Scope s(monitor_, "world.integrate_position");
         for (int i = 0; i < n; ++i) {
-            if (model_.bodies[(size_t)i].is_static()) continue;
+            if (model_.bodies[(size_t)i].is_static() || (sleep && state_.is_sleeping(i))) continue;
             Transform& tr = state_.transforms[(size_t)i];
             const Vec3& v = state_.linear_velocities[(size_t)i];
             const Vec3& w = state_.angular_velocities[(size_t)i];
@@ -555,14 +627,14 @@ void World::step_rigid_pipeline(float dt) {
     }
     {
         Scope s(monitor_, "world.clear_forces");
-        for (auto& f : state_.forces) f = Vec3{};
-        for (auto& t : state_.torques) t = Vec3{};
+        state_.clear_forces();
     }
-    int dynamic = 0;
-    for (const RigidBody& b : model_.bodies) dynamic += b.is_static() ? 0 : 1;
     monitor_.record_metric("bodies", (double)n);
     monitor_.record_metric("dynamic_bodies", (double)dynamic);
-    monitor_.record_metric("shapes", (double)model_.shapes.size());
+    monitor_.record_metric("shapes", (double)ns);
+    monitor_.record_metric("candidate_pairs", (double)broadphase_.get_pairs().size());
+    monitor_.record_metric("contacts", (double)contacts_.size());
+    monitor_.record_metric("solver_iterations", (double)set.velocity_iterations);
 }
 
 // ---- PBFSolver ----
@@ -716,6 +788,16 @@ void FluidWorld::step(float dt) {
                 }
             }
             for (int k = 0; k < needed && k < model_.num_bodies(); ++k) {
+                // With sleep on, a sleeping body that took coupling force
+                // wakes (World::apply_force); the test is on the body's
+                // summed force and torque changing.
+                const Vec3& f0 = state_.forces[(size_t)k];
+                const Vec3& t0 = state_.torques[(size_t)k];
+                const bool touched = f0.x != f[(size_t)k].x || f0.y != f[(size_t)k].y ||
+                                     f0.z != f[(size_t)k].z || t0.x != t[(size_t)k].x ||
+                                     t0.y != t[(size_t)k].y || t0.z != t[(size_t)k].z;
+                if (touched && solver_.settings().sleep_enabled && state_.is_sleeping(k))
+                    state_.wake_body(k);
                 state_.forces[(size_t)k] = f[(size_t)k];
                 state_.torques[(size_t)k] = t[(size_t)k];
             }

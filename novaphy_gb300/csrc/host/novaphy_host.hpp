@@ -5,6 +5,7 @@
 // sampling) and the small rigid-body state stay on the host.
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -32,10 +33,18 @@ struct Vec3 {
     Vec3 operator+(const Vec3& o) const { return {x + o.x, y + o.y, z + o.z}; }
     Vec3 operator-(const Vec3& o) const { return {x - o.x, y - o.y, z - o.z}; }
     Vec3 operator*(float s) const { return {x * s, y * s, z * s}; }
+    Vec3 operator/(float s) const { return {x / s, y / s, z / s}; }
+    Vec3 operator-() const { return {-x, -y, -z}; }
     Vec3& operator+=(const Vec3& o) {
         x = x + o.x;
         y = y + o.y;
         z = z + o.z;
+        return *this;
+    }
+    Vec3& operator-=(const Vec3& o) {
+        x = x - o.x;
+        y = y - o.y;
+        z = z - o.z;
         return *this;
     }
     float dot(const Vec3& o) const { return x * o.x + (y * o.y + z * o.z); }
@@ -56,10 +65,27 @@ struct Vec3 {
 inline Vec3 operator*(float s, const Vec3& v) { return {s * v.x, s * v.y, s * v.z}; }
 static_assert(sizeof(Vec3) == 3 * sizeof(float), "Vec3 must be a packed float[3]");
 
+// Row-major 3x3 matrix; products sum their three terms as t0 + (t1 + t2).
+using Mat3 = std::array<float, 9>;
+
 // Unit quaternion (w, x, y, z).
 struct Quat {
     float w = 1.0f, x = 0.0f, y = 0.0f, z = 0.0f;
     Vec3 vec() const { return {x, y, z}; }
+    Quat conjugate() const { return {w, -x, -y, -z}; }
+    // Hamilton product, each component summed left to right.
+    Quat operator*(const Quat& o) const {
+        return {w * o.w - x * o.x - y * o.y - z * o.z, w * o.x + x * o.w + y * o.z - z * o.y,
+                w * o.y + y * o.w + z * o.x - x * o.z, w * o.z + z * o.w + x * o.y - y * o.x};
+    }
+    // R = I + 2 (w [v]x + [v]x^2), written out per entry.
+    Mat3 rotation_matrix() const {
+        const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
+        const float wx = w * x, wy = w * y, wz = w * z;
+        return {1.0f - 2.0f * (yy + zz), 2.0f * (xy - wz),        2.0f * (xz + wy),
+                2.0f * (xy + wz),        1.0f - 2.0f * (xx + zz), 2.0f * (yz - wx),
+                2.0f * (xz - wy),        2.0f * (yz + wx),        1.0f - 2.0f * (xx + yy)};
+    }
     // v' = v + w t + q.vec x t with t = 2 (q.vec x v)
     Vec3 rotate(const Vec3& v) const {
         Vec3 t = vec().cross(v);
@@ -84,7 +110,17 @@ struct Transform {
     Quat rotation;
     Transform() = default;
     Transform(const Vec3& p, const Quat& q) : position(p), rotation(q.normalized()) {}
+    // Composition and inverse renormalise the rotation, as the constructor does.
+    Transform operator*(const Transform& o) const {
+        return Transform(position + rotation.rotate(o.position), rotation * o.rotation);
+    }
+    Transform inverse() const {
+        const Quat r = rotation.conjugate();
+        return Transform(r.rotate(Vec3(-position.x, -position.y, -position.z)), r);
+    }
     Vec3 transform_point(const Vec3& p) const { return position + rotation.rotate(p); }
+    Vec3 transform_vector(const Vec3& v) const { return rotation.rotate(v); }
+    Mat3 rotation_matrix() const { return rotation.rotation_matrix(); }
     static Transform identity() { return Transform(); }
     static Transform from_translation(const Vec3& t) { return Transform(t, Quat{}); }
     static Transform from_axis_angle(const Vec3& axis, float angle) {
@@ -163,6 +199,30 @@ private:
 
 enum class ShapeType { Box, Sphere, Plane };
 
+// Axis-aligned box (include/novaphy/core/aabb.h); the default is empty
+// (min = +FLT_MAX, max = -FLT_MAX) so that expand() starts from nothing.
+struct AABB {
+    Vec3 min{3.402823466e+38f, 3.402823466e+38f, 3.402823466e+38f};
+    Vec3 max{-3.402823466e+38f, -3.402823466e+38f, -3.402823466e+38f};
+    AABB() = default;
+    AABB(const Vec3& lo, const Vec3& hi) : min(lo), max(hi) {}
+    bool overlaps(const AABB& o) const {
+        return (min.x <= o.max.x && max.x >= o.min.x) && (min.y <= o.max.y && max.y >= o.min.y) &&
+               (min.z <= o.max.z && max.z >= o.min.z);
+    }
+    void expand(const Vec3& p);
+    Vec3 center() const { return 0.5f * (min + max); }
+    Vec3 half_extents() const { return 0.5f * (max - min); }
+    float surface_area() const {
+        const Vec3 d = max - min;
+        return 2.0f * (d.x * d.y + d.y * d.z + d.z * d.x);
+    }
+    bool is_valid() const { return min.x <= max.x && min.y <= max.y && min.z <= max.z; }
+    static AABB from_sphere(const Vec3& c, float r) {
+        return AABB(c - Vec3(r, r, r), c + Vec3(r, r, r));
+    }
+};
+
 struct CollisionShape {
     ShapeType type = ShapeType::Box;
     int body_index = -1;
@@ -179,6 +239,10 @@ struct CollisionShape {
                                       float friction = 0.5f, float restitution = 0.3f);
     static CollisionShape make_plane(const Vec3& normal, float offset, float friction = 0.5f,
                                      float restitution = 0.0f);
+    // World box of the shape on a body at body_transform (shape.h:66-80):
+    // the 8 posed corners of a box, centre +- radius of a sphere, +-1e6 for
+    // a plane.
+    AABB compute_aabb(const Transform& body_transform) const;
 };
 
 struct RigidBody {
@@ -207,6 +271,8 @@ public:
     int add_shape(const CollisionShape& shape);
     int add_ground_plane(float y = 0.0f, float friction = 0.5f, float restitution = 0.0f);
     Model build() const { return model_; }
+    int num_bodies() const { return model_.num_bodies(); }
+    int num_shapes() const { return model_.num_shapes(); }
 
 private:
     Model model_;
@@ -225,20 +291,115 @@ std::vector<BoundaryParticle> sample_plane_boundary(const CollisionShape& s, flo
 std::vector<BoundaryParticle> sample_model_boundaries(const Model& model, float spacing,
                                                       float plane_extent = 1.0f);
 
+// Contact solver and sleep settings (include/novaphy/dynamics/free_body_solver.h:19-31).
 struct SolverSettings {
-    int velocity_iterations = 20;
-    float baumgarte = 0.2f;
+    int velocity_iterations = 30;
+    float baumgarte = 0.3f;
     float slop = 0.005f;
     bool warm_starting = true;
     bool sleep_enabled = false;
+    float sleep_energy_threshold = 0.01f;
+    float sleep_time_required = 0.5f;
+    float sleep_ema_alpha = 0.8f;
+};
+
+// ---- rigid contacts (host; the reference's World pipeline around the fluid) ----
+
+// One contact (include/novaphy/core/contact.h:14-35): normal from body_a
+// toward body_b, penetration > 0 when overlapping; body -1 is the world.
+struct ContactPoint {
+    Vec3 position, normal;
+    float penetration = 0.0f;
+    int body_a = -1, body_b = -1, shape_a = -1, shape_b = -1;
+    float friction = 0.5f, restitution = 0.0f;
+    float accumulated_normal_impulse = 0.0f;
+    float accumulated_tangent_impulse_1 = 0.0f, accumulated_tangent_impulse_2 = 0.0f;
+};
+inline float combine_friction(float a, float b) { return std::sqrt(a * b); }
+inline float combine_restitution(float a, float b) { return std::max(a, b); }
+
+// Contacts between two posed shapes, appended to `contacts`
+// (src/collision/narrowphase.cpp:390-437 and the pairs before it): sphere-
+// sphere, sphere-plane, box-sphere, box-plane (corners below the plane),
+// box-box (15-axis SAT, up to 4 incident corners, else the midpoint).
+// Returns whether the pair touches; plane-plane never does.
+bool collide_shapes(const CollisionShape& a, const Transform& ta, const CollisionShape& b,
+                    const Transform& tb, std::vector<ContactPoint>& contacts);
+
+struct BroadPhasePair {
+    int body_a = -1, body_b = -1;  // shape indices, body_a < body_b
+    bool operator==(const BroadPhasePair& o) const { return body_a == o.body_a && body_b == o.body_b; }
+};
+
+// Broad phase (include/novaphy/collision/broadphase.h): every pair of boxes
+// that overlap on all three axes (closed intervals), except pairs of two
+// static shapes, as (lower, higher) index sorted lexicographically.
+class SweepAndPrune {
+public:
+    void update(const std::vector<AABB>& aabbs, const std::vector<bool>& static_mask);
+    const std::vector<BroadPhasePair>& get_pairs() const { return pairs_; }
+
+private:
+    std::vector<int> order_;
+    std::vector<BroadPhasePair> pairs_;
 };
 
 struct SimState {
     std::vector<Transform> transforms;
     std::vector<Vec3> linear_velocities, angular_velocities, forces, torques;
+    // Sleep bookkeeping (include/novaphy/sim/state.h): a body sleeps with its
+    // whole contact island once every member's smoothed energy stayed below
+    // the threshold for the required time.
+    std::vector<int> sleeping;
+    std::vector<float> sleep_timer, smoothed_energy;
+    std::vector<int> island_id;
     void init(const std::vector<Transform>& t);
+    void clear_forces();
     void set_linear_velocity(int i, const Vec3& v);
     void set_angular_velocity(int i, const Vec3& w);
+    void apply_force(int i, const Vec3& f);
+    void apply_torque(int i, const Vec3& t);
+    void wake_body(int i);
+    bool is_sleeping(int i) const;
+    void update_energy(int i, float energy, float alpha);
+    float get_smoothed_energy(int i) const;
+    void build_islands(const std::vector<ContactPoint>& contacts);
+    void evaluate_sleep(float dt, float energy_threshold, float time_threshold);
+    void propagate_wake_through_island(int i);
+};
+
+// Sequential-impulse contact solver (src/dynamics/free_body_solver.cpp):
+// per contact a normal row (accumulated impulse clamped at 0, Baumgarte and
+// restitution bias) and two friction rows (clamped to the friction cone of
+// the normal impulse), warm started from the contacts' accumulated impulses,
+// velocity_iterations sweeps in contact order.
+class PerformanceMonitor;
+class ContactSolver {
+public:
+    explicit ContactSolver(SolverSettings s = {}) : settings_(s) {}
+    // With a monitor, its phases world.solver.{pre_step,warm_start,
+    // iteration.solve_velocity} are recorded.
+    void solve(std::vector<ContactPoint>& contacts, const std::vector<RigidBody>& bodies,
+               const std::vector<Transform>& transforms, std::vector<Vec3>& lin,
+               std::vector<Vec3>& ang, const std::vector<int>& sleeping, float dt,
+               PerformanceMonitor* monitor = nullptr);
+    SolverSettings& settings() { return settings_; }
+    const SolverSettings& settings() const { return settings_; }
+
+private:
+    struct Row {
+        Vec3 r_a, r_b, t1, t2;
+        float k_n = 0.0f, k_t1 = 0.0f, k_t2 = 0.0f;  // effective masses (inverted)
+        float bias = 0.0f;
+        Mat3 inv_i_a{}, inv_i_b{};  // world-frame inverse inertia
+    };
+    void prepare(std::vector<ContactPoint>& contacts, const std::vector<RigidBody>& bodies,
+                 const std::vector<Transform>& transforms, const std::vector<Vec3>& lin,
+                 const std::vector<Vec3>& ang, const std::vector<int>& sleeping, float dt);
+    void sweep(std::vector<ContactPoint>& contacts, const std::vector<RigidBody>& bodies,
+               std::vector<Vec3>& lin, std::vector<Vec3>& ang);
+    SolverSettings settings_;
+    std::vector<Row> rows_;
 };
 
 // Phase timers and per-frame metrics (include/novaphy/sim/performance_monitor.h).
@@ -298,8 +459,10 @@ private:
     std::vector<std::vector<TraceEvent>> trace_frames_;  // oldest first
 };
 
-// Rigid world: gravity, accumulated forces, symplectic Euler integration
-// (src/dynamics/integrator.cpp:20-60).  Contacts are not modelled here.
+// Rigid world (src/sim/world.cpp:30-182): symplectic Euler velocity update
+// (src/dynamics/integrator.cpp:20-60), shape boxes, broad phase, narrow
+// phase, contact islands and sleep (when enabled), the contact solver,
+// position update, forces cleared.
 class World {
 public:
     explicit World(const Model& model, SolverSettings settings = {});
@@ -309,15 +472,22 @@ public:
     const Vec3& gravity() const { return gravity_; }
     SimState& state() { return state_; }
     const Model& model() const { return model_; }
+    const std::vector<ContactPoint>& contacts() const { return contacts_; }
+    SolverSettings& solver_settings() { return solver_.settings(); }
     PerformanceMonitor& performance_monitor() { return monitor_; }
+    // Forces and torques last one step; with sleep on they wake the body.
     void apply_force(int body, const Vec3& f);
     void apply_torque(int body, const Vec3& t);
 
 protected:
     void step_rigid_pipeline(float dt);
+    // m |v|^2 + w . (I w): twice the kinetic energy, the sleep test's measure.
+    float kinetic_energy(int body) const;
     Model model_;
-    SolverSettings settings_;
+    ContactSolver solver_;
     SimState state_;
+    SweepAndPrune broadphase_;
+    std::vector<ContactPoint> contacts_;
     Vec3 gravity_{0.0f, -9.81f, 0.0f};  // include/novaphy/sim/world.h:157
     PerformanceMonitor monitor_;
 };

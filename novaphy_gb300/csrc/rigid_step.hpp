@@ -1,7 +1,8 @@
-// Rigid step of free bodies (no contacts), shared by the host World
-// (csrc/host/novaphy_host.cpp) and the serving loop's coupled scenes, whose
-// bodies step on the device (csrc/pbf_boundary.cu), so that every caller
-// integrates with the same float operations: semi-implicit Euler as in
+// Velocity and position integration of rigid bodies, shared by the host
+// World (csrc/host/novaphy_host.cpp, which runs its contact solve between
+// the two) and the serving loop's coupled scenes, whose bodies step on the
+// device as free bodies without contacts (csrc/pbf_boundary.cu), so that
+// every caller integrates with the same float operations: semi-implicit Euler as in
 // src/dynamics/integrator.cpp:20-60,
 //   v += (g + f / m) dt,  w += I^-1 t dt,  w *= 0.999,
 //   x += v dt,  q += 0.5 dt (w, 0) * q, then q normalised.

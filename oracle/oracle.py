@@ -291,6 +291,57 @@ class Ref:
         L.ref_sample_box.argtypes = [_f32p, _f32p, _f32p, C.c_float, C.c_void_p, C.c_int]
         L.ref_sample_sphere.argtypes = [C.c_float, _f32p, _f32p, C.c_float, C.c_void_p, C.c_int]
         L.ref_sample_plane.argtypes = [_f32p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_int]
+        L.ref_collide.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, C.c_int, _i32p]
+        L.ref_collide.restype = C.c_int
+        L.ref_sap.argtypes = [C.c_int, _f32p, _i32p, _i32p, C.c_int]
+        L.ref_sap.restype = C.c_int
+        L.ref_rigid_world_run.argtypes = [C.c_int, _f32p, C.c_int, _f32p, _f32p, _f32p, _f32p,
+                                          _f32p, C.c_float, C.c_int, _f32p, _f32p, _f32p, _f32p,
+                                          _i32p, _i32p]
+        L.ref_rigid_world_run.restype = C.c_int
+
+    # Shapes are packed as 19 floats (ref_harness.cpp, shape_from); contacts come back as
+    # rows of 11: position (3), normal (3), penetration, body_a, body_b,
+    # friction, restitution.
+    def collide(self, shape_a, pose_a, shape_b, pose_b):
+        """collide_shapes on two packed shapes at poses (x, y, z, qw, qx, qy, qz);
+        returns (hit, contacts[n, 11])."""
+        out = np.zeros((16, 11), np.float32)
+        hit = np.zeros(1, np.int32)
+        n = self.lib.ref_collide(_f32(shape_a, (19,)), _f32(pose_a, (7,)), _f32(shape_b, (19,)),
+                                 _f32(pose_b, (7,)), out, 16, hit)
+        return bool(hit[0]), out[:n]
+
+    def sap(self, boxes, fixed):
+        """SweepAndPrune pairs of boxes[n, 6] (min, max) with a static mask."""
+        boxes = _f32(boxes, (-1, 6))
+        fixed = np.ascontiguousarray(fixed, np.int32)
+        cap = max(1, len(boxes) * (len(boxes) - 1) // 2)
+        pairs = np.zeros((cap, 2), np.int32)
+        n = self.lib.ref_sap(len(boxes), boxes, fixed, pairs, cap)
+        return pairs[:n]
+
+    def rigid_world(self, bodies, shapes, lin, ang, settings, gravity, dt, nsteps):
+        """The reference World (contacts, solver, sleep) after nsteps steps.
+        bodies[n, 17] = mass, inertia (9), position, rotation (w, x, y, z);
+        shapes[m, 19] packed; settings = (velocity_iterations, baumgarte, slop,
+        warm_starting, sleep_enabled, sleep_energy_threshold,
+        sleep_time_required, sleep_ema_alpha).  Returns (pos, quat, lin_vel,
+        ang_vel, contacts per step, sleeping)."""
+        bodies = _f32(bodies, (-1, 17))
+        shapes = _f32(shapes, (-1, 19))
+        nb = len(bodies)
+        out = [np.zeros((nb, 3), np.float32), np.zeros((nb, 4), np.float32),
+               np.zeros((nb, 3), np.float32), np.zeros((nb, 3), np.float32),
+               np.zeros(max(nsteps, 1), np.int32), np.zeros(max(nb, 1), np.int32)]
+        rc = self.lib.ref_rigid_world_run(nb, bodies, len(shapes), shapes, _f32(lin, (-1, 3)),
+                                          _f32(ang, (-1, 3)), _f32(settings, (8,)),
+                                          _f32(gravity, (3,)), dt, nsteps, *out)
+        if rc:
+            raise ValueError("the reference World failed")
+        out[4] = out[4][:nsteps]
+        out[5] = out[5][:nb]
+        return tuple(out)
 
     def boundary_volumes(self, world, h):
         world = _f32(world, (-1, 3))

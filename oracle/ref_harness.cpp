@@ -12,6 +12,8 @@
 #include <cstring>
 #include <vector>
 
+#include "novaphy/collision/broadphase.h"
+#include "novaphy/collision/narrowphase.h"
 #include "novaphy/core/model_builder.h"
 #include "novaphy/fluid/boundary.h"
 #include "novaphy/fluid/fluid_world.h"
@@ -360,4 +362,132 @@ void ref_boundary_world_positions(int nb, const float* local3, const int* body, 
         for (int d = 0; d < 3; ++d) out3[3 * i + d] = w[(size_t)i](d);
 }
 
+// ---- rigid contact pipeline ----
+// A shape is 19 floats: type (0 box, 1 sphere, 2 plane), body index,
+// half extents (3), radius, plane normal (3), plane offset, local position
+// (3), local rotation (w, x, y, z), friction, restitution.  A contact is 11
+// floats: position (3), normal (3), penetration, body_a, body_b, friction,
+// restitution.
+static CollisionShape shape_from(const float* f) {
+    CollisionShape s;
+    s.type = f[0] == 0.0f ? ShapeType::Box : (f[0] == 1.0f ? ShapeType::Sphere : ShapeType::Plane);
+    s.body_index = (int)f[1];
+    s.box.half_extents = Vec3f(f[2], f[3], f[4]);
+    s.sphere.radius = f[5];
+    s.plane.normal = Vec3f(f[6], f[7], f[8]);
+    s.plane.offset = f[9];
+    s.local_transform = Transform(Vec3f(f[10], f[11], f[12]), Quatf(f[13], f[14], f[15], f[16]));
+    s.friction = f[17];
+    s.restitution = f[18];
+    return s;
+}
+
+static void contact_to(const ContactPoint& c, float* o) {
+    for (int d = 0; d < 3; ++d) {
+        o[d] = c.position(d);
+        o[3 + d] = c.normal(d);
+    }
+    o[6] = c.penetration;
+    o[7] = (float)c.body_a;
+    o[8] = (float)c.body_b;
+    o[9] = c.friction;
+    o[10] = c.restitution;
+}
+
+// collide_shapes on two shapes at poses (position 3, rotation w x y z).
+// Writes up to cap contacts; returns their count, with hit in *hit.
+int ref_collide(const float* sa, const float* pa7, const float* sb, const float* pb7, float* out,
+                int cap, int* hit) {
+    const Transform ta(Vec3f(pa7[0], pa7[1], pa7[2]), Quatf(pa7[3], pa7[4], pa7[5], pa7[6]));
+    const Transform tb(Vec3f(pb7[0], pb7[1], pb7[2]), Quatf(pb7[3], pb7[4], pb7[5], pb7[6]));
+    std::vector<ContactPoint> c;
+    *hit = collide_shapes(shape_from(sa), ta, shape_from(sb), tb, c) ? 1 : 0;
+    const int n = (int)c.size();
+    for (int k = 0; k < n && k < cap; ++k) contact_to(c[(size_t)k], out + 11 * k);
+    return n;
+}
+
+// SweepAndPrune over n boxes (min 3, max 3 each) and a static mask; writes
+// up to cap pairs (a, b); returns the pair count.
+int ref_sap(int n, const float* boxes6, const int* fixed, int* pairs2, int cap) {
+    std::vector<AABB> a((size_t)n);
+    std::vector<bool> m((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const float* b = boxes6 + 6 * i;
+        a[(size_t)i] = AABB(Vec3f(b[0], b[1], b[2]), Vec3f(b[3], b[4], b[5]));
+        m[(size_t)i] = fixed[i] != 0;
+    }
+    SweepAndPrune sap;
+    sap.update(a, m);
+    const auto& p = sap.get_pairs();
+    for (int k = 0; k < (int)p.size() && k < cap; ++k) {
+        pairs2[2 * k] = p[(size_t)k].body_a;
+        pairs2[2 * k + 1] = p[(size_t)k].body_b;
+    }
+    return (int)p.size();
+}
+
+// A rigid World of nb bodies (17 floats each: mass, inertia row-major (9),
+// position (3), rotation (w, x, y, z)) and ns shapes (19 floats each, as
+// above), with initial velocities lin3/ang3, solver settings (8 floats:
+// velocity_iterations, baumgarte, slop, warm_starting, sleep_enabled,
+// sleep_energy_threshold, sleep_time_required, sleep_ema_alpha) and gravity,
+// stepped nsteps times.  Writes the final poses and velocities, the contact
+// count of every step and the final sleep flags.  Returns 0, or -1.
+int ref_rigid_world_run(int nb, const float* bodies17, int ns, const float* shapes19,
+                        const float* lin3, const float* ang3, const float* settings8,
+                        const float* gravity3, float dt, int nsteps, float* body_pos3,
+                        float* body_quat4, float* body_v3, float* body_w3, int* contacts_per_step,
+                        int* sleeping) {
+    try {
+        ModelBuilder mb;
+        for (int k = 0; k < nb; ++k) {
+            const float* b = bodies17 + 17 * k;
+            RigidBody rb;
+            rb.mass = b[0];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) rb.inertia(r, c) = b[1 + 3 * r + c];
+            mb.add_body(rb, Transform(Vec3f(b[10], b[11], b[12]), Quatf(b[13], b[14], b[15], b[16])));
+        }
+        for (int k = 0; k < ns; ++k) mb.add_shape(shape_from(shapes19 + 19 * k));
+        SolverSettings st;
+        st.velocity_iterations = (int)settings8[0];
+        st.baumgarte = settings8[1];
+        st.slop = settings8[2];
+        st.warm_starting = settings8[3] != 0.0f;
+        st.sleep_enabled = settings8[4] != 0.0f;
+        st.sleep_energy_threshold = settings8[5];
+        st.sleep_time_required = settings8[6];
+        st.sleep_ema_alpha = settings8[7];
+        World w(mb.build(), st);
+        w.set_gravity(Vec3f(gravity3[0], gravity3[1], gravity3[2]));
+        for (int k = 0; k < nb; ++k) {
+            w.state().set_linear_velocity(k, Vec3f(lin3[3 * k], lin3[3 * k + 1], lin3[3 * k + 2]));
+            w.state().set_angular_velocity(k, Vec3f(ang3[3 * k], ang3[3 * k + 1], ang3[3 * k + 2]));
+        }
+        for (int s = 0; s < nsteps; ++s) {
+            w.step(dt);
+            contacts_per_step[s] = (int)w.contacts().size();
+        }
+        const SimState& ss = w.state();
+        for (int k = 0; k < nb; ++k) {
+            const Transform& t = ss.transforms[(size_t)k];
+            for (int d = 0; d < 3; ++d) {
+                body_pos3[3 * k + d] = t.position(d);
+                body_v3[3 * k + d] = ss.linear_velocities[(size_t)k](d);
+                body_w3[3 * k + d] = ss.angular_velocities[(size_t)k](d);
+            }
+            body_quat4[4 * k] = t.rotation.w();
+            body_quat4[4 * k + 1] = t.rotation.x();
+            body_quat4[4 * k + 2] = t.rotation.y();
+            body_quat4[4 * k + 3] = t.rotation.z();
+            sleeping[k] = ss.sleeping[(size_t)k];
+        }
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
 }  // extern "C"
+

@@ -186,14 +186,19 @@ def test_monitor_trace_json_and_reset(tmp_path):
     assert {"world.total", "world.integrate_velocity", "world.integrate_position"} <= set(phases)
     assert phases["world.total"].samples == 3 and phases["world.total"].last_ms > 0.0
     metrics = {m.name: m.value for m in mon.last_frame_metrics()}
-    assert metrics == {"bodies": 2.0, "dynamic_bodies": 2.0, "shapes": 3.0}
+    assert set(metrics) == {"bodies", "dynamic_bodies", "shapes", "candidate_pairs", "contacts",
+                            "solver_iterations"}
+    assert (metrics["bodies"], metrics["dynamic_bodies"], metrics["shapes"]) == (2.0, 2.0, 3.0)
+    # ground-box, ground-box and box-box overlap; the resting stack touches
+    assert metrics["candidate_pairs"] == 3.0 and metrics["contacts"] >= 4.0
+    assert metrics["solver_iterations"] == 30.0
     path = tmp_path / "trace.json"
     mon.write_trace_json(path)
     ev = json.loads(path.read_text())["traceEvents"]
     xs = [e for e in ev if e["ph"] == "X"]
     cs = [e for e in ev if e["ph"] == "C"]
-    # two frames kept: one world.total each, three counters each
-    assert sum(e["name"] == "world.total" for e in xs) == 2 and len(cs) == 6
+    # two frames kept: one world.total each, six counters each
+    assert sum(e["name"] == "world.total" for e in xs) == 2 and len(cs) == 12
     assert all(e["dur"] >= 0.0 and e["ts"] >= 0.0 for e in xs)
     tot = [e for e in xs if e["name"] == "world.total"][-1]
     inner = [e for e in xs if e["name"] == "world.integrate_velocity"][-1]

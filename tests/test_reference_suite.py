@@ -2,12 +2,11 @@
 unmodified against this package under the name ``novaphy``, on CPU where the
 reference tree is present.
 
-Selected: every test of the fluid, coupling, PBF and performance-monitor
-files that needs neither a CUDA device (this package steps fluid only on the
-GPU) nor the rigid contact pipeline (broadphase, contacts and the velocity
-solver are outside the PBF path; the host World integrates free bodies only).
-The run writes nothing into the reference tree: no byte-code, no cache, and
-its temporary files go to pytest's own tmp directory.
+Selected: every test of the fluid, coupling, PBF, performance-monitor,
+collision and free-body files that needs no CUDA device (this package steps
+fluid only on the GPU; those tests run in the GPU suite instead).  The run
+writes nothing into the reference tree: no byte-code, no cache, and its
+temporary files go to pytest's own tmp directory.
 """
 import os
 import subprocess
@@ -28,9 +27,8 @@ NEEDS_DEVICE = [
     "test_fluid_world_step", "test_fluid_world_no_fluid", "test_fluid_world_inherits_world",
     "test_fluid_world_monitor_reports_rigid_and_fluid_phases",
 ]
-# Tests of the rigid contact pipeline (broadphase phase, contact counts).
-NEEDS_CONTACTS = ["test_world_monitor_reports_phases_and_metrics"]
-FILES = ["test_fluid.py", "test_coupling.py", "test_pbf.py", "test_performance_monitor.py"]
+FILES = ["test_fluid.py", "test_coupling.py", "test_pbf.py", "test_performance_monitor.py",
+         "test_collision.py", "test_free_body_sim.py"]
 
 RUNNER = r"""
 import sys
@@ -46,7 +44,7 @@ def test_reference_python_suite_passes(tmp_path):
     tests_dir = os.path.join(build_oracle.REFERENCE_ROOT, "tests", "python")
     if not os.path.isdir(tests_dir):
         pytest.skip("reference tests not present on this host")
-    deselect = " or ".join(NEEDS_DEVICE + NEEDS_CONTACTS)
+    deselect = " or ".join(NEEDS_DEVICE)
     args = [os.path.join(tests_dir, f) for f in FILES] + [
         "-q", "-p", "no:cacheprovider", "--rootdir", str(tmp_path), "--basetemp",
         str(tmp_path / "base"), "-k", f"not ({deselect})", "-rf"]
