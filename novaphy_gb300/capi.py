@@ -338,6 +338,19 @@ class Scene:
         check(self._L.pbf_scene_stream(self._h, C.byref(p)))
         return p.value or 0
 
+    def device_array(self, field: int) -> "DeviceArray":
+        """Zero-copy view of a field in device memory: positions and
+        velocities as (n, 3) float32 with row stride 16 bytes (float4 storage),
+        densities and lambdas as (n,).  Waits for the scene's stream first, so
+        the view holds the state after every step issued so far; it stays live
+        (later steps show through once synchronised) until the scene is reset
+        to more particles than it holds, restored from a larger snapshot, or
+        closed.  Any consumer of __cuda_array_interface__ takes it, e.g.
+        torch.as_tensor(view, device="cuda")."""
+        ptr = self.device_field(field)
+        self.sync()
+        return DeviceArray(self, field, ptr, self.n)
+
     def check_finite(self) -> int:
         return self._L.pbf_scene_check_finite(self._h)
 
@@ -391,6 +404,25 @@ def scene_device_bytes(scene: "Scene") -> int:
     out = C.c_size_t(0)
     check(load().pbf_scene_device_bytes(scene.handle, C.byref(out)))
     return int(out.value)
+
+
+class DeviceArray:
+    """A scene field in device memory, exported through
+    __cuda_array_interface__ (version 3).  Holds a reference to its scene."""
+
+    def __init__(self, scene: "Scene", field: int, ptr: int, n: int):
+        if field not in (FIELD_POSITIONS, FIELD_VELOCITIES, FIELD_DENSITIES, FIELD_LAMBDAS):
+            raise ValueError("unknown field")
+        self.scene = scene
+        vec = field in (FIELD_POSITIONS, FIELD_VELOCITIES)
+        self.shape = (n, 3) if vec else (n,)
+        self.strides = (16, 4) if vec else (4,)
+        self.ptr = ptr if n > 0 else 0
+
+    @property
+    def __cuda_array_interface__(self):
+        return {"shape": self.shape, "typestr": "<f4", "data": (self.ptr, False),
+                "strides": self.strides, "version": 3}
 
 
 class Batch:

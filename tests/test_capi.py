@@ -97,3 +97,17 @@ def test_server_defaults_and_no_device(capi):
     with pytest.raises(capi.PbfError) as e:
         capi.Server(cfg)
     assert e.value.code == capi.PBF_ERR_NO_DEVICE
+
+
+def test_device_array_interface_layout(capi):
+    # No device needed: the exported layout of positions (float4 rows) and
+    # of a scalar field.
+    v = capi.DeviceArray(object(), capi.FIELD_POSITIONS, 0x1000, 5)
+    cai = v.__cuda_array_interface__
+    assert cai["shape"] == (5, 3) and cai["strides"] == (16, 4) and cai["typestr"] == "<f4"
+    assert cai["data"] == (0x1000, False) and cai["version"] == 3
+    d = capi.DeviceArray(object(), capi.FIELD_LAMBDAS, 0x2000, 7).__cuda_array_interface__
+    assert d["shape"] == (7,) and d["strides"] == (4,)
+    assert capi.DeviceArray(object(), capi.FIELD_DENSITIES, 0x3000, 0).ptr == 0
+    with pytest.raises(ValueError):
+        capi.DeviceArray(object(), 9, 0x1000, 1)
