@@ -156,10 +156,52 @@ def fluid_world_fixture():
     print("fluid_world.npz written:", len(x), "particles")
 
 
+# Bodies resting on the ground under a falling fluid block: a sphere pressed
+# into the plane, a box standing on an edge (two corner contacts), and from
+# the sixth step on the fluid pushes them into each other (box-sphere), so
+# the reference's contact solver acts every step.  The scene is stored in the
+# fixture with the results.
+FLUID_WORLD_CONTACTS = dict(
+    lower=[0.0, 0.15, 0.0], upper=[0.3, 0.4, 0.3], spacing=0.05, plane_y=0.0,
+    boundary_extent=0.5, steps=8,
+    bodies=[("sphere", (0.08, 0.0, 0.0), 0.5, (0.1, 0.075, 0.1), (1.0, 0.0, 0.0, 0.0)),
+            ("box", (0.04, 0.04, 0.04), 0.8, (0.22, 0.05, 0.2),
+             (0.9238795, 0.0, 0.0, 0.3826834))],
+)
+
+
+def fluid_world_contacts_fixture():
+    R = Ref()
+    c = FLUID_WORLD_CONTACTS
+    s = Settings.make(kernel_radius=0.2, solver_iterations=2)
+    dt = float(np.float32(1 / 60))
+    x, v, rho, lam, bp, bq, bv, bw = R.fluid_world(
+        s, c["lower"], c["upper"], c["spacing"], c["bodies"], plane_y=c["plane_y"],
+        boundary_extent=c["boundary_extent"], dt=dt, nsteps=c["steps"])
+    b = c["bodies"]
+    np.savez_compressed(
+        os.path.join(HERE, "fluid_world_contacts.npz"), x=x, v=v, rho=rho, lam=lam,
+        body_pos=bp, body_quat=bq, body_v=bv, body_w=bw,
+        scene_kind=np.array([0 if k[0] == "sphere" else 1 for k in b], np.int32),
+        scene_size=np.array([k[1] for k in b], np.float32),
+        scene_mass=np.array([k[2] for k in b], np.float32),
+        scene_pos=np.array([k[3] for k in b], np.float32),
+        scene_quat=np.array([k[4] for k in b], np.float32),
+        scene_block=np.array([c["lower"], c["upper"]], np.float32),
+        scene_scalars=np.array([c["spacing"], c["plane_y"], c["boundary_extent"], c["steps"], dt],
+                               np.float32))
+    print("fluid_world_contacts.npz written:", len(x), "particles")
+
+
 if __name__ == "__main__":
     # With names, only those fixtures: python tests/golden/make_golden.py fluid_world
-    if sys.argv[1:] == ["fluid_world"]:
-        fluid_world_fixture()
+    names = sys.argv[1:]
+    if names:
+        if "fluid_world" in names:
+            fluid_world_fixture()
+        if "fluid_world_contacts" in names:
+            fluid_world_contacts_fixture()
     else:
         main()
         fluid_world_fixture()
+        fluid_world_contacts_fixture()

@@ -248,3 +248,51 @@ def test_fluid_world_matches_reference_fixture():
                               g["body_v"][k]), k
         assert np.array_equal(np.asarray(fw.state.angular_velocities[k], np.float32),
                               g["body_w"][k]), k
+
+
+def test_fluid_world_with_contacts_matches_reference_fixture():
+    """Eight FluidWorld steps with the host contact pipeline at work every
+    step (a sphere pressed into the ground, a box on an edge, then the fluid
+    pushing them together) against the reference's own FluidWorld
+    (tests/golden/fluid_world_contacts.npz, which stores the scene too): fluid
+    state and both bodies, bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "fluid_world_contacts.npz"))
+    spacing, plane_y, extent, steps, dt = (float(t) for t in g["scene_scalars"])
+    mb = novaphy.ModelBuilder()
+    mb.add_ground_plane(y=plane_y)
+    for kind, size, mass, pos, q in zip(g["scene_kind"], g["scene_size"], g["scene_mass"],
+                                        g["scene_pos"], g["scene_quat"]):
+        tr = novaphy.Transform(pos, [float(q[1]), float(q[2]), float(q[3]), float(q[0])])
+        if kind == 0:
+            i = mb.add_body(novaphy.RigidBody.from_sphere(float(mass), float(size[0])), tr)
+            mb.add_shape(novaphy.CollisionShape.make_sphere(float(size[0]), i))
+        else:
+            i = mb.add_body(novaphy.RigidBody.from_box(float(mass), size), tr)
+            mb.add_shape(novaphy.CollisionShape.make_box(size, i))
+    pbf = novaphy.PBFSettings()
+    pbf.kernel_radius = 0.2
+    pbf.solver_iterations = 2
+    blk = novaphy.FluidBlockDef()
+    blk.lower, blk.upper = g["scene_block"][0], g["scene_block"][1]
+    blk.particle_spacing = spacing
+    fw = novaphy.FluidWorld(mb.build(), [blk], novaphy.SolverSettings(), pbf,
+                            boundary_extent=extent)
+    kinds = set()
+    for _ in range(int(steps)):
+        fw.step(dt)
+        assert len(fw.contacts) >= 3
+        kinds |= {(c.body_a, c.body_b) for c in fw.contacts}
+    assert kinds >= {(-1, 0), (-1, 1)} and len(kinds) == 3  # ground-sphere, ground-box, box-sphere
+    fs = fw.fluid_state
+    assert np.array_equal(fs.positions_array, g["x"])
+    assert np.array_equal(fs.velocities_array, g["v"])
+    assert np.array_equal(fs.densities_array, g["rho"])
+    assert np.array_equal(np.asarray(fs.lambdas, np.float32), g["lam"])
+    for k in range(len(g["scene_kind"])):
+        tr = fw.state.transforms[k]
+        q = np.asarray(tr.rotation, np.float32)  # x, y, z, w
+        got = [np.asarray(tr.position, np.float32), np.array([q[3], q[0], q[1], q[2]], np.float32),
+               np.asarray(fw.state.linear_velocities[k], np.float32),
+               np.asarray(fw.state.angular_velocities[k], np.float32)]
+        for name, a in zip(("body_pos", "body_quat", "body_v", "body_w"), got):
+            assert np.array_equal(a.view(np.uint32), g[name][k].view(np.uint32)), (name, k)
