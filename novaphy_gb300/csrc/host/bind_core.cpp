@@ -145,6 +145,52 @@ PYBIND11_MODULE(_core, m) {
         .def("update", &SweepAndPrune::update, py::arg("aabbs"), py::arg("static_mask"))
         .def("get_pairs", &SweepAndPrune::get_pairs);
 
+    // World vertices of per-instance local vertices: out[i*V + j] =
+    // R(quats[b]) local[i, j] + positions[b] with b = body_indices[i]
+    // (bind_sim.cpp's batched transform for rendering).  Shapes and indices
+    // are checked; the GIL is released for the loop.
+    m.def(
+        "batch_transform_vertices",
+        [](py::array_t<float, py::array::c_style | py::array::forcecast> positions,
+           py::array_t<float, py::array::c_style | py::array::forcecast> quats,
+           py::array_t<int32_t, py::array::c_style | py::array::forcecast> body_indices,
+           py::array_t<float, py::array::c_style | py::array::forcecast> local_verts,
+           py::array_t<float, py::array::c_style> out_verts) {
+            if (positions.ndim() != 2 || positions.shape(1) != 3 || quats.ndim() != 2 ||
+                quats.shape(1) != 4 || quats.shape(0) != positions.shape(0))
+                throw py::value_error("positions (B, 3) and quats (B, 4) expected");
+            const py::ssize_t nb = positions.shape(0);
+            if (body_indices.ndim() != 1 || local_verts.ndim() != 3 || local_verts.shape(2) != 3 ||
+                local_verts.shape(0) != body_indices.shape(0))
+                throw py::value_error("body_indices (N,) and local_verts (N, V, 3) expected");
+            const py::ssize_t n = body_indices.shape(0), nv = local_verts.shape(1);
+            if (out_verts.ndim() != 2 || out_verts.shape(1) != 3 || out_verts.shape(0) < n * nv)
+                throw py::value_error("out_vertices (N*V, 3) expected");
+            const int32_t* idx = body_indices.data();
+            for (py::ssize_t i = 0; i < n; ++i)
+                if (idx[i] < 0 || idx[i] >= nb) throw py::index_error("body index out of range");
+            const float* P = positions.data();
+            const float* Q = quats.data();
+            const float* L = local_verts.data();
+            float* O = out_verts.mutable_data();
+            py::gil_scoped_release release;
+            for (py::ssize_t i = 0; i < n; ++i) {
+                const py::ssize_t b = idx[i];
+                const Quat q{Q[4 * b + 3], Q[4 * b], Q[4 * b + 1], Q[4 * b + 2]};
+                const Mat3 r = q.rotation_matrix();
+                const Vec3 p(P[3 * b], P[3 * b + 1], P[3 * b + 2]);
+                for (py::ssize_t j = 0; j < nv; ++j) {
+                    const float* v = L + 3 * (i * nv + j);
+                    float* o = O + 3 * (i * nv + j);
+                    o[0] = r[0] * v[0] + r[1] * v[1] + r[2] * v[2] + p.x;
+                    o[1] = r[3] * v[0] + r[4] * v[1] + r[5] * v[2] + p.y;
+                    o[2] = r[6] * v[0] + r[7] * v[1] + r[8] * v[2] + p.z;
+                }
+            }
+        },
+        py::arg("positions"), py::arg("quats"), py::arg("body_indices"), py::arg("local_verts"),
+        py::arg("out_vertices"));
+
     m.def(
         "collide_shapes",
         [](const CollisionShape& a, const Transform& ta, const CollisionShape& b,
@@ -221,6 +267,38 @@ PYBIND11_MODULE(_core, m) {
              py::arg("velocity"))
         .def("apply_force", &SimState::apply_force, py::arg("body_index"), py::arg("force"))
         .def("apply_torque", &SimState::apply_torque, py::arg("body_index"), py::arg("torque"))
+        .def("get_transforms_numpy",
+             [](const SimState& s) {
+                 // (N, 3) positions and (N, 4) quaternions [x, y, z, w], one call
+                 const py::ssize_t n = (py::ssize_t)s.transforms.size();
+                 py::array_t<float> pos({n, (py::ssize_t)3}), quat({n, (py::ssize_t)4});
+                 float* p = pos.mutable_data();
+                 float* q = quat.mutable_data();
+                 for (py::ssize_t i = 0; i < n; ++i) {
+                     const Transform& t = s.transforms[(size_t)i];
+                     p[3 * i] = t.position.x, p[3 * i + 1] = t.position.y, p[3 * i + 2] = t.position.z;
+                     q[4 * i] = t.rotation.x, q[4 * i + 1] = t.rotation.y;
+                     q[4 * i + 2] = t.rotation.z, q[4 * i + 3] = t.rotation.w;
+                 }
+                 return py::make_tuple(pos, quat);
+             })
+        .def("get_transforms_into",
+             [](const SimState& s, py::array_t<float, py::array::c_style> pos,
+                py::array_t<float, py::array::c_style> quat) {
+                 const py::ssize_t n = (py::ssize_t)s.transforms.size();
+                 if (pos.ndim() != 2 || pos.shape(0) < n || pos.shape(1) != 3 || quat.ndim() != 2 ||
+                     quat.shape(0) < n || quat.shape(1) != 4)
+                     throw py::value_error("need float32 arrays of shape (N, 3) and (N, 4)");
+                 float* p = pos.mutable_data();
+                 float* q = quat.mutable_data();
+                 for (py::ssize_t i = 0; i < n; ++i) {
+                     const Transform& t = s.transforms[(size_t)i];
+                     p[3 * i] = t.position.x, p[3 * i + 1] = t.position.y, p[3 * i + 2] = t.position.z;
+                     q[4 * i] = t.rotation.x, q[4 * i + 1] = t.rotation.y;
+                     q[4 * i + 2] = t.rotation.z, q[4 * i + 3] = t.rotation.w;
+                 }
+             },
+             py::arg("out_positions"), py::arg("out_quats"))
         .def_readonly("sleeping", &SimState::sleeping)
         .def_readonly("island_id", &SimState::island_id)
         .def("is_sleeping", &SimState::is_sleeping, py::arg("body_index"));

@@ -248,3 +248,44 @@ def test_host_world_free_bodies_match_reference_build(ref):
         assert np.array_equal(np.array([q[3], q[0], q[1], q[2]], np.float32), rq[k]), k
         assert np.array_equal(np.asarray(w.state.linear_velocities[k], np.float32), rv[k]), k
         assert np.array_equal(np.asarray(w.state.angular_velocities[k], np.float32), rw[k]), k
+
+
+def test_transform_exports_and_batch_vertex_transform():
+    mb = novaphy.ModelBuilder()
+    q = np.array([0.1, 0.7, -0.2, 0.68], np.float32)  # x, y, z, w
+    for k in range(3):
+        mb.add_body(novaphy.RigidBody.from_sphere(1.0, 0.1),
+                    novaphy.Transform(np.array([k, 2.0 * k, -1.0], np.float32), q))
+    w = novaphy.World(mb.build(), novaphy.SolverSettings())
+    pos, quat = w.state.get_transforms_numpy()
+    assert pos.shape == (3, 3) and quat.shape == (3, 4)
+    for k, t in enumerate(w.state.transforms):
+        assert np.array_equal(pos[k], np.asarray(t.position, np.float32))
+        assert np.array_equal(quat[k], np.asarray(t.rotation, np.float32))
+    p2, q2 = np.zeros((3, 3), np.float32), np.zeros((3, 4), np.float32)
+    w.state.get_transforms_into(p2, q2)
+    assert np.array_equal(p2, pos) and np.array_equal(q2, quat)
+    with pytest.raises(ValueError):
+        w.state.get_transforms_into(np.zeros((2, 3), np.float32), q2)
+
+    rng = np.random.default_rng(5)
+    idx = np.array([2, 0, 2, 1], np.int32)
+    local = rng.normal(size=(4, 5, 3)).astype(np.float32)
+    out = np.zeros((20, 3), np.float32)
+    novaphy.batch_transform_vertices(pos, quat, idx, local, out)
+    # the same float operations in numpy float32: rotation from (x, y, z, w),
+    # then r0 v0 + r1 v1 + r2 v2 + p left to right
+    one, two = np.float32(1), np.float32(2)
+    for i, b in enumerate(idx):
+        x, y, z, s = quat[b]
+        r = np.array([[one - two * (y * y + z * z), two * (x * y - s * z), two * (x * z + s * y)],
+                      [two * (x * y + s * z), one - two * (x * x + z * z), two * (y * z - s * x)],
+                      [two * (x * z - s * y), two * (y * z + s * x), one - two * (x * x + y * y)]],
+                     np.float32)
+        for j in range(5):
+            v = local[i, j]
+            want = [((r[d, 0] * v[0] + r[d, 1] * v[1]) + r[d, 2] * v[2]) + pos[b, d]
+                    for d in range(3)]
+            assert np.array_equal(out[5 * i + j], np.array(want, np.float32)), (i, j)
+    with pytest.raises(IndexError):
+        novaphy.batch_transform_vertices(pos, quat, np.array([3], np.int32), local[:1], out)
