@@ -7,7 +7,6 @@
 // library's own.  Compiled with -ffp-contract=off.
 #include <algorithm>
 #include <limits>
-#include <map>
 
 #include "novaphy_host.hpp"
 
@@ -404,7 +403,11 @@ void SimState::build_islands(const std::vector<ContactPoint>& contacts) {
 // brought to rest; bodies outside any island stay awake.
 void SimState::evaluate_sleep(float dt, float energy_threshold, float time_threshold) {
     const int n = (int)sleeping.size();
-    std::map<int, bool> can_sleep;
+    int islands = 0;
+    for (int i = 0; i < n; ++i) islands = std::max(islands, island_id[(size_t)i] + 1);
+    // per island: some member above the energy threshold / every member's
+    // timer at least time_threshold (one pass each instead of a scan per body)
+    std::vector<char> awake((size_t)islands, 0), timed((size_t)islands, 1);
     for (int i = 0; i < n; ++i) {
         const int isl = island_id[(size_t)i];
         if (isl < 0) continue;
@@ -412,21 +415,16 @@ void SimState::evaluate_sleep(float dt, float energy_threshold, float time_thres
             sleep_timer[(size_t)i] += dt;
         } else {
             sleep_timer[(size_t)i] = 0.0f;
-            can_sleep[isl] = false;
+            awake[(size_t)isl] = 1;
         }
     }
     for (int i = 0; i < n; ++i) {
         const int isl = island_id[(size_t)i];
-        if (isl < 0 || can_sleep.count(isl)) continue;
-        bool all = true;
-        for (int j = 0; j < n && all; ++j)
-            if (island_id[(size_t)j] == isl && sleep_timer[(size_t)j] < time_threshold) all = false;
-        if (all) can_sleep[isl] = true;
+        if (isl >= 0 && sleep_timer[(size_t)i] < time_threshold) timed[(size_t)isl] = 0;
     }
     for (int i = 0; i < n; ++i) {
         const int isl = island_id[(size_t)i];
-        const auto it = isl < 0 ? can_sleep.end() : can_sleep.find(isl);
-        if (it != can_sleep.end() && it->second) {
+        if (isl >= 0 && !awake[(size_t)isl] && timed[(size_t)isl]) {
             sleeping[(size_t)i] = 1;
             linear_velocities[(size_t)i] = Vec3{};
             angular_velocities[(size_t)i] = Vec3{};

@@ -298,3 +298,23 @@ def test_world_defaults_match_reference_settings():
     assert abs(s.baumgarte - 0.3) < 1e-7 and abs(s.slop - 0.005) < 1e-9
     assert abs(s.sleep_energy_threshold - 0.01) < 1e-9
     assert abs(s.sleep_time_required - 0.5) < 1e-9 and abs(s.sleep_ema_alpha - 0.8) < 1e-7
+
+
+def test_scattered_pile_sleeps_island_by_island(ref):
+    # ten bodies dropped over a 4 m square: several islands, some asleep at
+    # the end while others still move
+    rng = np.random.default_rng(11)
+    bodies, shapes = [], [GROUND]
+    for k in range(10):
+        pos = (rng.uniform(-2, 2), 0.3 + 0.8 * k, rng.uniform(-2, 2))
+        if k % 2:
+            r = float(rng.uniform(0.15, 0.35))
+            bodies.append(body(1.0, sphere_inertia(1.0, r), pos, random_quat(rng)))
+            shapes.append(shape(SPHERE, k, radius=r, friction=0.8))
+        else:
+            he = tuple(rng.uniform(0.15, 0.35, 3))
+            bodies.append(body(1.5, box_inertia(1.5, he), pos, random_quat(rng)))
+            shapes.append(shape(BOX, k, half=he, friction=0.8, restitution=0.1))
+    got = check_world(ref, bodies, shapes, settings=(20, 0.3, 0.005, 1, 1, 0.05, 0.3, 0.8),
+                      nsteps=600)
+    assert 1 <= got[5].sum() < len(bodies)
