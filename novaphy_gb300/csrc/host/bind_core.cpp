@@ -45,6 +45,12 @@ struct type_caster<Vec3> {
 
 namespace {
 
+py::array_t<float> mat3_array(const Mat3& m) {
+    py::array_t<float> a({3, 3});
+    std::memcpy(a.mutable_data(), m.data(), 9 * sizeof(float));
+    return a;
+}
+
 py::array_t<float> positions_array(const std::vector<Vec3>& v) {
     py::array_t<float> a({(py::ssize_t)v.size(), (py::ssize_t)3});
     if (!v.empty()) std::memcpy(a.mutable_data(), &v[0].x, v.size() * sizeof(Vec3));
@@ -82,10 +88,40 @@ PYBIND11_MODULE(_core, m) {
                                   q[2].cast<float>()};
             })
         .def("transform_point", &Transform::transform_point, py::arg("point"))
+        .def("transform_vector", &Transform::transform_vector, py::arg("vector"))
+        .def("inverse", &Transform::inverse)
+        .def("rotation_matrix", [](const Transform& t) { return mat3_array(t.rotation_matrix()); })
+        .def("__mul__", &Transform::operator*, py::arg("other"))
+        .def("__repr__",
+             [](const Transform& t) {
+                 return "Transform(pos=[" + std::to_string(t.position.x) + ", " +
+                        std::to_string(t.position.y) + ", " + std::to_string(t.position.z) +
+                        "], rot=[" + std::to_string(t.rotation.w) + ", " +
+                        std::to_string(t.rotation.x) + ", " + std::to_string(t.rotation.y) +
+                        ", " + std::to_string(t.rotation.z) + "])";
+             })
         .def_static("identity", &Transform::identity)
+        .def_static(
+            "from_rotation",
+            [](py::sequence q) {
+                if (q.size() != 4) throw py::value_error("rotation must be [x, y, z, w]");
+                return Transform(Vec3{}, Quat{q[3].cast<float>(), q[0].cast<float>(),
+                                              q[1].cast<float>(), q[2].cast<float>()});
+            },
+            py::arg("q"))
         .def_static("from_translation", &Transform::from_translation, py::arg("translation"))
         .def_static("from_axis_angle", &Transform::from_axis_angle, py::arg("axis"),
                     py::arg("angle"));
+
+    // math_utils.h helpers: [v]x with skew(a) b = a x b, and angle conversions
+    m.def(
+        "skew",
+        [](const Vec3& v) {
+            return mat3_array(Mat3{0.0f, -v.z, v.y, v.z, 0.0f, -v.x, -v.y, v.x, 0.0f});
+        },
+        py::arg("v"));
+    m.def("deg2rad", [](float deg) { return deg * kPi / 180.0f; }, py::arg("deg"));
+    m.def("rad2deg", [](float rad) { return rad * 180.0f / kPi; }, py::arg("rad"));
 
     py::enum_<ShapeType>(m, "ShapeType")
         .value("Box", ShapeType::Box)

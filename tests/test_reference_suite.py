@@ -3,8 +3,9 @@ unmodified against this package under the name ``novaphy``, on CPU where the
 reference tree is present.
 
 Selected: every test of the fluid, coupling, PBF, performance-monitor,
-collision and free-body files that needs no CUDA device (this package steps
-fluid only on the GPU; those tests run in the GPU suite instead).  The run
+collision, free-body and math files that needs no CUDA device (this package
+steps fluid only on the GPU; those tests run in the GPU suite instead), less
+the math file's three tests of the articulated solver's spatial algebra.  The run
 writes nothing into the reference tree: no byte-code, no cache, and its
 temporary files go to pytest's own tmp directory.
 """
@@ -24,11 +25,15 @@ NEEDS_DEVICE = [
     "test_coupling_sphere_in_fluid", "test_fluid_world_no_coupling_backward_compat",
     "test_pbf_solver_step_runs", "test_pbf_particles_fall", "test_pbf_zero_gravity",
     "test_pbf_density_reasonable", "test_pbf_velocities_updated", "test_fluid_world_creation",
-    "test_fluid_world_step", "test_fluid_world_no_fluid", "test_fluid_world_inherits_world",
+    "test_fluid_world_step", "test_fluid_world_inherits_world",
     "test_fluid_world_monitor_reports_rigid_and_fluid_phases",
 ]
+# Spatial (6D) algebra of the articulated-body solver, which is not part of
+# this package.
+SPATIAL = ["test_spatial_transform_identity", "test_spatial_cross_motion",
+           "test_spatial_inertia_matrix"]
 FILES = ["test_fluid.py", "test_coupling.py", "test_pbf.py", "test_performance_monitor.py",
-         "test_collision.py", "test_free_body_sim.py"]
+         "test_collision.py", "test_free_body_sim.py", "test_math.py"]
 
 RUNNER = r"""
 import sys
@@ -44,7 +49,7 @@ def test_reference_python_suite_passes(tmp_path):
     tests_dir = os.path.join(build_oracle.REFERENCE_ROOT, "tests", "python")
     if not os.path.isdir(tests_dir):
         pytest.skip("reference tests not present on this host")
-    deselect = " or ".join(NEEDS_DEVICE)
+    deselect = " or ".join(NEEDS_DEVICE + SPATIAL)
     args = [os.path.join(tests_dir, f) for f in FILES] + [
         "-q", "-p", "no:cacheprovider", "--rootdir", str(tmp_path), "--basetemp",
         str(tmp_path / "base"), "-k", f"not ({deselect})", "-rf"]
