@@ -3,7 +3,7 @@ unmodified against this package under the name ``novaphy``, on CPU where the
 reference tree is present.
 
 Selected: every test of the fluid, coupling, PBF, performance-monitor,
-collision, free-body and math files that needs no CUDA device (this package
+collision, free-body, math and performance-demo files that needs no CUDA device (this package
 steps fluid only on the GPU; those tests run in the GPU suite instead), less
 the math file's three tests of the articulated solver's spatial algebra.  The run
 writes nothing into the reference tree: no byte-code, no cache, and its
@@ -27,13 +27,15 @@ NEEDS_DEVICE = [
     "test_pbf_density_reasonable", "test_pbf_velocities_updated", "test_fluid_world_creation",
     "test_fluid_world_step", "test_fluid_world_inherits_world",
     "test_fluid_world_monitor_reports_rigid_and_fluid_phases",
+    "test_performance_demo_fluid_outputs",
 ]
 # Spatial (6D) algebra of the articulated-body solver, which is not part of
 # this package.
 SPATIAL = ["test_spatial_transform_identity", "test_spatial_cross_motion",
            "test_spatial_inertia_matrix"]
 FILES = ["test_fluid.py", "test_coupling.py", "test_pbf.py", "test_performance_monitor.py",
-         "test_collision.py", "test_free_body_sim.py", "test_math.py"]
+         "test_collision.py", "test_free_body_sim.py", "test_math.py",
+         "test_demo_performance_monitor.py"]
 
 RUNNER = r"""
 import sys
