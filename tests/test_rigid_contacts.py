@@ -318,3 +318,19 @@ def test_scattered_pile_sleeps_island_by_island(ref):
     got = check_world(ref, bodies, shapes, settings=(20, 0.3, 0.005, 1, 1, 0.05, 0.3, 0.8),
                       nsteps=600)
     assert 1 <= got[5].sum() < len(bodies)
+
+
+def test_thousand_box_stacks(ref):
+    # 10 x 10 columns of 10 boxes settling (about 2,000 contacts a step):
+    # the broad phase, the contact order and the solver sweep at scale
+    rng = np.random.default_rng(3)
+    bodies, shapes = [], [GROUND]
+    he = (0.2, 0.2, 0.2)
+    for i in range(10):
+        for j in range(10):
+            for k in range(10):
+                bodies.append(body(1.0, box_inertia(1.0, he),
+                                   (i * 0.5 + rng.uniform(0, 0.05), 0.25 + k * 0.41, j * 0.5)))
+                shapes.append(shape(BOX, len(bodies) - 1, half=he))
+    got = check_world(ref, bodies, shapes, settings=(10, *DEFAULT[1:]), nsteps=60)
+    assert got[4][-1] > 1500
