@@ -332,3 +332,47 @@ def test_fluid_world_fluid_state_over_steps_matches_reference_build(port, ref):
                               np.array([0, -9.81, 0], np.float32), m, 4)
     for a, b in ((x, rx), (v, rv), (lam, rlam)):
         assert np.array_equal(a, b)
+
+
+def _edge_scenes():
+    """Small inputs at the edges of the step's arithmetic and of the hash grid."""
+    h = 0.1
+    rng = np.random.default_rng(17)
+    scenes = {
+        "one particle": np.array([[0.3, 0.4, 0.5]], np.float32),
+        "coincident pair": np.array([[0.2, 0.2, 0.2], [0.2, 0.2, 0.2], [0.25, 0.2, 0.2]],
+                                    np.float32),
+        # every coordinate a multiple of h: each particle on a cell corner
+        "cell corners": (np.stack(np.meshgrid(*[np.arange(4)] * 3, indexing="ij"), -1)
+                         .reshape(-1, 3) * np.float32(h)).astype(np.float32),
+        # straddling the origin, where the XOR hash merges mirrored cells
+        "around the axes": rng.uniform(-0.15, 0.15, (120, 3)).astype(np.float32),
+        # far from the origin: large cell coordinates
+        "far away": (rng.uniform(0, 0.3, (80, 3)) + np.array([1e3, -2e3, 5e2])).astype(
+            np.float32),
+        # isolated particles beside a dense clump
+        "isolated": np.concatenate([rng.uniform(0, 0.1, (60, 3)),
+                                    np.array([[5.0, 5.0, 5.0], [-3.0, 1.0, 2.0]])]).astype(
+            np.float32),
+    }
+    return h, scenes
+
+
+@pytest.mark.parametrize("name", ["one particle", "coincident pair", "cell corners",
+                                  "around the axes", "far away", "isolated"])
+def test_port_matches_reference_build_on_edge_cases(port, ref, name):
+    h, scenes = _edge_scenes()
+    x = scenes[name]
+    n = len(x)
+    for clamp in (0, 1):
+        s = Settings.make(kernel_radius=h, particle_radius=h / 4, use_domain_bounds=clamp,
+                          domain_lower=[-0.05, -0.05, -0.05], domain_upper=[0.3, 0.3, 0.3],
+                          solver_iterations=3, corr_k=0.1, corr_delta_q=0.2)
+        rng = np.random.default_rng(n)
+        v0 = rng.normal(scale=0.5, size=(n, 3)).astype(np.float32)
+        z = np.zeros(n, np.float32)
+        g = np.array([0.0, -9.81, 0.0], np.float32)
+        a = port.steps(s, x, v0, z, z, 1.0 / 120.0, g, 0.125, 2)
+        b = ref.steps(s, x, v0, z, z, 1.0 / 120.0, g, 0.125, 2)
+        for what, u, t in zip("x v rho lam".split(), a, b):
+            assert np.array_equal(u.view(np.uint32), t.view(np.uint32)), (name, clamp, what)
