@@ -27,10 +27,11 @@ timed calls.  Under torchrun each rank runs an independent replica on its own
 GPU (the single-scene path does not shard); `value` sums the ranks'
 particle-steps over the slowest rank's time.
 
-reference: the reference's CPU PBF (its own sources built in oracle/_ref
-where the reference tree is present, else the oracle restatement), single
-threaded as the reference is, each step on the seeded state of a bounded
-sample of the same workload.
+reference: the reference's CPU PBF step on the same 1M workload and config,
+each step from the seeded state.  What runs is the oracle's C restatement,
+which the tests pin bit for bit to the reference's own sources built from its
+tree (the tree is absent on the GPU host), with its per-particle loops spread
+over every host thread.  This arm imports no native code of the package.
 """
 from __future__ import annotations
 
@@ -162,58 +163,71 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_backend():
-    """The reference build where present, else the restatement: (object, kind)."""
-    from oracle import build_oracle
-    from oracle.oracle import Port, Ref
+def cpu_port(threads=None):
+    """The oracle restatement (bit-identical to the reference build, which is
+    pinned against it by the tests) with `threads` host threads on its
+    per-particle loops (default: every host core)."""
+    from oracle.oracle import Port
 
-    try:
-        if build_oracle.build_ref() is not None:
-            return Ref(), "reference"
-    except Exception:
-        pass
-    return Port(), "port"
+    port = Port()
+    used = port.set_threads(threads or os.cpu_count() or 1)
+    return port, used
 
 
-def cpu_sample_workload(counts):
-    w = workloads.scaled_dam_break(counts)
-    return w
+CPU_KIND_NOTE = ("the oracle's C restatement of the reference's PBF step, bit-identical to "
+                 "the reference's own sources built from its tree (the tests pin it); the "
+                 "reference tree is absent on the GPU host, so the restatement is what runs, "
+                 "with its per-particle loops spread over the host threads (the reference "
+                 "itself is single-threaded)")
 
 
-def time_cpu(counts, nsteps, warmup):
-    """Reference CPU steps, each from the seeded state of a counts-block sample."""
+def time_cpu_1m(nsteps, warmup, vorticity):
+    """Reference CPU steps of the full 1M dam break, each from the seeded state
+    (the copy of the seeded arrays is inside the timed step)."""
     from oracle.oracle import Settings
 
-    be, kind = cpu_backend()
-    w = cpu_sample_workload(counts)
+    port, threads = cpu_port()
+    w = workloads.dam_break_1m(vorticity=vorticity)
     s = Settings.make(**w.settings)
     z = np.zeros(w.n, np.float32)
     for _ in range(warmup):
-        be.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
+        port.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
     el = 0.0
     for _ in range(nsteps):
         t0 = time.perf_counter()
-        be.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
+        port.steps(s, w.x, w.v, z, z, w.dt, w.gravity, w.mass, 1)
         el += time.perf_counter() - t0
-    return w.n * nsteps / el, kind, w.n, el
+    return w, w.n * nsteps / el, threads, el
+
+
+def headline_config(w, ws, vorticity):
+    """The `config` of the headline line, the same for both arms."""
+    return {"workload": "dam_break_1m", "particles": w.n, "lattice": "100x100x100",
+            "r": 0.01, "h": w.settings["kernel_radius"],
+            "iterations": w.settings["solver_iterations"], "dt": w.dt,
+            "vorticity_epsilon": vorticity,
+            "arithmetic": "f32, the reference's operation order (bit-identical)",
+            "hash_compat": 1,
+            "step": "one PBF step from the seeded state (state restored inside the timed "
+                    "region)",
+            "l2": "per-step working set ~300 MB > 129 MB L2",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "one scene"}
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
-    counts = (32, 32, 32)
-    val, kind, n, el = time_cpu(counts, args.steps, args.warmup)
+    w, val, threads, el = time_cpu_1m(args.steps, args.warmup, args.vorticity)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "dam_break_1m", "sample": f"{n}-particle block "
-                   f"{counts[0]}x{counts[1]}x{counts[2]} of the 1M case's lattice, box and "
-                   "parameters", "threads": 1},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": kind,
-                         "sample": f"{n} particles x {args.steps} steps, each from the seeded "
-                         "state, 1 thread (the reference CPU PBF has no threading)"},
+        "config": headline_config(w, ws, args.vorticity),
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"the full workload: {w.n} particles x {args.steps} steps, "
+                                   f"each from the seeded state, {threads} host threads",
+                         "kind_note": CPU_KIND_NOTE},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -461,8 +475,9 @@ def run_served(args, device, ws=1, rank=0, dist=None):
         wl = [wl[i] for i in shard.rank_scenes([w.n for w in wl], ws, rank)]
     dt = np.float32(wl[0].dt)
     T = float(args.serve_seconds)
+    T_side = float(args.serve_side_seconds)
 
-    def make_plans(mean_s, seed):
+    def make_plans(mean_s, seed, T=T):
         rng = np.random.default_rng(seed)
         out = []
         for k in range(len(wl)):
@@ -482,9 +497,12 @@ def run_served(args, device, ws=1, rank=0, dist=None):
     demand = demand_of(plans)
     coupled = [sphere_boundary(w, device) for w in wl]
 
-    deadline_after = T + 90.0  # stop waiting for stragglers 90 s after the last arrival
+    # Both arms stop waiting for stragglers 30 s after the last arrival; a
+    # run's value is the particle-steps it completed over its wall time.
+    drain_s = 30.0
 
-    def served_run(budget=None, session_mean=None, max_batch=16 << 20, plans=plans):
+    def served_run(budget=None, session_mean=None, max_batch=16 << 20, plans=plans, T=T):
+        deadline_after = T + drain_s
         cfg = capi.server_config(max_batch_particles=max_batch)
         if budget is not None:
             cfg.hbm_budget_bytes = int(budget)
@@ -561,7 +579,8 @@ def run_served(args, device, ws=1, rank=0, dist=None):
                 "hbm_bytes_scratch": stats["hbm_bytes_scratch"],
                 "budget_bytes": int(cfg.hbm_budget_bytes)}
 
-    def plain_run():
+    def plain_run(T=T):
+        deadline_after = T + drain_s
         scenes, rigid = [], []
         for k, w in enumerate(wl):
             sc = capi.Scene(capi.default_settings(**w.settings), w.x, w.v, mass=w.mass,
@@ -638,12 +657,12 @@ def run_served(args, device, ws=1, rank=0, dist=None):
     # that latencies show service time rather than the backlog of an overload.
     own_rate = full["particle_steps"] / max(full["wall_s"], 1e-9)
     mean_half = 0.512 * (demand / T) / max(0.5 * own_rate, 1.0)
-    plans_half = make_plans(mean_half, 45)
+    plans_half = make_plans(mean_half, 45, T=T_side)
     progress("served: half load")
-    half = served_run(max_batch=args.served_max_batch, plans=plans_half)
-    half["arrivals"] = (f"per-client Poisson, mean {mean_half * 1e3:.0f} ms, "
+    half = served_run(max_batch=args.served_max_batch, plans=plans_half, T=T_side)
+    half["arrivals"] = (f"per-client Poisson, mean {mean_half * 1e3:.0f} ms over {T_side:.0f} s, "
                         f"{sum(len(p) for p in plans_half)} requests")
-    half["offered_fraction_of_capacity"] = demand_of(plans_half) / T / max(own_rate, 1.0)
+    half["offered_fraction_of_capacity"] = demand_of(plans_half) / T_side / max(own_rate, 1.0)
     if args.served_full_only:
         return {"value": full["value"], "unit": UNIT, "full_budget": full, "half_load": half,
                 "max_batch_particles": args.served_max_batch}
@@ -654,7 +673,8 @@ def run_served(args, device, ws=1, rank=0, dist=None):
     probe.close()
     progress("served: reduced budget")
     reduced = served_run(budget=scratch + total_charge // 2, session_mean=8,
-                         max_batch=small_batch)
+                         max_batch=small_batch, plans=make_plans(0.512, 46, T=T_side), T=T_side)
+    reduced["arrivals"] = f"per-client Poisson, mean 512 ms over {T_side:.0f} s"
     progress("served: plain")
     plain = plain_run()
     cpu = None
@@ -672,7 +692,7 @@ def run_served(args, device, ws=1, rank=0, dist=None):
                     f"k in {{1, 4, 16}}; {sum(len(p) for p in plans)} requests, "
                     f"{demand} particle-steps offered",
         "state_bytes_per_particle": capi.state_bytes_per_particle(),
-        "value": full["value"], "unit": UNIT,
+        "value": full["value"], "unit": UNIT, "seconds": T,
         "step_ms_p50": full["step_ms_p50"], "step_ms_p99": full["step_ms_p99"],
         "request_ms_p50": full["request_ms_p50"], "request_ms_p99": full["request_ms_p99"],
         "speedup_vs_plain": full["value"] / plain["value"],
@@ -745,6 +765,20 @@ def run_coupled(args, device):
         world.step(dt)
     el = time.perf_counter() - t0
     n, nb = world.num_particles, world.num_boundary_particles
+    # Device time of every phase over 3 more steps (the monitor runs the same
+    # step as separate launches with CUDA events between the phases).
+    mon = world.performance_monitor
+    mon.reset()
+    mon.enabled = True
+    for _ in range(3):
+        world.step(dt)
+    mon.enabled = False
+    phases = {p.name: p.avg_ms for p in mon.phase_stats()}
+    iters = 4
+    dom = max(ALG_BYTES, key=lambda q: phases.get(q, 0.0))
+    launch_ms = phases[dom] / iters
+    peak, peak_kind = measured_peak_hbm()
+    achieved = ALG_BYTES[dom] * n / (launch_ms / 1e3) / 1e9
     return {"workload": f"coupled pool: {n} fluid + {nb} boundary particles, 8 bodies "
                         f"(4 boxes, 4 spheres) and a floor plane, r = 0.015, h = 4r, "
                         f"4 iterations, dt = 1/240",
@@ -752,7 +786,13 @@ def run_coupled(args, device):
             "fluid_particles": n, "boundary_particles": nb,
             "step": "FluidWorld.step: PBF step, boundary density, coupling forces/torques "
                     "(device, per-body serial reduction), host rigid step",
-            "timing": "host clock over consecutive steps after 2 warm-up steps"}
+            "timing": f"host clock over {k} consecutive steps after 2 warm-up steps",
+            "roofline": {"bound": "hbm", "kernel": KERNEL_OF_PHASE[dom], "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "alg_bytes_per_launch": ALG_BYTES[dom] * n, "launch_ms": launch_ms,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "timing": "monitor device phases, 3 steps after the timed ones"},
+            "phases_ms": {q: round(v, 4) for q, v in sorted(phases.items())}}
 
 
 # FP32 (non-tensor) issue peak of a GB300: 152 SMs x 128 FP32 lanes x 2 FLOP
@@ -772,6 +812,55 @@ def fp32_roof(particle_steps_per_s, iters, candidates=1728, neighbours=250):
     return {"achieved": achieved, "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
             "frac": achieved / FP32_PEAK_TFLOPS_NOMINAL, "flop_per_particle_step": flop,
             "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)"}
+
+
+def summary_of(value, e2e, fast, roofline, coupled, batched, served):
+    """The headline figures of every section in a few short keys."""
+    def r(x, nd=4):
+        return None if x is None else float(f"{x:.{nd}g}")
+
+    def get(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict) or d.get(k) is None:
+                return None
+            d = d[k]
+        return d
+
+    out = {"1m": {"exact": r(value), "e2e": r(get(e2e, "value")), "fast": r(get(fast, "value")),
+                  "hbm_frac": r(roofline["frac"], 3),
+                  "issue_frac": r(get(roofline, "issue", "frac"), 3)}}
+    if coupled:
+        out["coupled"] = {"value": r(get(coupled, "value")), "steps": get(coupled, "steps"),
+                          "hbm_frac": r(get(coupled, "roofline", "frac"), 3),
+                          "error": get(coupled, "error")}
+    if batched:
+        out["batched"] = {"value": r(get(batched, "value")),
+                          "plain_async": r(get(batched, "plain_value")),
+                          "x_plain_async": r(get(batched, "speedup_vs_plain"), 3),
+                          "plain_sync": r(get(batched, "plain_sync_value")),
+                          "x_plain_sync": r(get(batched, "speedup_vs_plain_sync"), 3),
+                          "p50_ms": r(get(batched, "step_ms_p50")),
+                          "p99_ms": r(get(batched, "step_ms_p99")),
+                          "error": get(batched, "error")}
+    if served:
+        out["served"] = {"value": r(get(served, "value")),
+                         "seconds": get(served, "seconds"),
+                         "plain": r(get(served, "plain", "value")),
+                         "x_plain": r(get(served, "speedup_vs_plain"), 3),
+                         "step_p50_ms": r(get(served, "step_ms_p50")),
+                         "step_p99_ms": r(get(served, "step_ms_p99")),
+                         "req_p50_ms": r(get(served, "request_ms_p50")),
+                         "req_p99_ms": r(get(served, "request_ms_p99")),
+                         "half_load": {"value": r(get(served, "half_load", "value")),
+                                       "step_p50_ms": r(get(served, "half_load", "step_ms_p50")),
+                                       "step_p99_ms": r(get(served, "half_load", "step_ms_p99"))},
+                         "error": get(served, "error")}
+    for sec in out.values():
+        if isinstance(sec, dict) and sec.get("error") is None:
+            sec.pop("error", None)
+    out["plain_arm"] = ("plain = the drop-in per-scene call on each scene's own stream, all "
+                        "issued before one wait (asynchronous); plain_sync waits for each step")
+    return out
 
 
 def side_section(ws, fn):
@@ -945,12 +1034,11 @@ def run_ours(args, ws, rank, local):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         progress("cpu baseline")
-        counts = (50, 50, 50)
-        val, kind, n, el = time_cpu(counts, 1, 0)
-        cpu = {"value": val, "unit": UNIT, "cores": 1, "kind": kind,
-               "sample": f"{n}-particle {counts[0]}x{counts[1]}x{counts[2]} block of the 1M case's "
-                         f"lattice/box/parameters, 1 step from the seeded state, 1 thread "
-                         f"({el:.1f} s)"}
+        _, val, threads, el = time_cpu_1m(1, 0, args.vorticity)
+        cpu = {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"one step of the full workload ({w.n} particles) from the seeded "
+                         f"state, {threads} host threads ({el:.1f} s)",
+               "kind_note": CPU_KIND_NOTE}
 
     if rank == 0:
         line = {
@@ -958,25 +1046,20 @@ def run_ours(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "dam_break_1m", "particles": w.n, "lattice": "100x100x100",
-                       "r": 0.01, "h": w.settings["kernel_radius"], "iterations": iters,
-                       "dt": w.dt, "vorticity_epsilon": args.vorticity,
-                       "arithmetic": "exact (bit-identical to the reference)", "hash_compat": 1,
-                       "step": "one PBF step from the seeded batch (device snapshot restore "
-                               "inside the timed region)",
-                       "l2": "per-step working set ~300 MB > 129 MB L2",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "config": headline_config(w, ws, args.vorticity),
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks,
+            "phases_ms": {k: round(v, 4) for k, v in phases.items()},
             "fast": fast,
             "consecutive": consecutive,
+            "coupled": coupled,
             "batched": batched,
             "served": served,
-            "coupled": coupled,
-            "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+            # Last, so that a reader of the line's tail sees it whole.
+            "summary": summary_of(value, e2e, fast, roofline, coupled, batched, served),
         }
         print(json.dumps(line), flush=True)
     seed.close()
@@ -1009,8 +1092,11 @@ def main():
                     help="skip the plain per-scene arms and CPU pool of the batched run")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-coupled", action="store_true")
-    ap.add_argument("--coupled-steps", type=int, default=10)
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--coupled-steps", type=int, default=300)
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="arrival window of the full-budget served run and its plain arm")
+    ap.add_argument("--serve-side-seconds", type=float, default=10.0,
+                    help="arrival window of the half-load and reduced-budget served runs")
     ap.add_argument("--served-max-batch", type=int, default=16 << 20,
                     help="particles per launch of the full-budget serving run")
     ap.add_argument("--served-full-only", action="store_true",

@@ -242,9 +242,12 @@ int pbf_sort_pairs_host(int device, int n, const unsigned* keys, int key_bits,
  * fixed static device array (about 4.2 MB held on every GPU that loads the
  * library, until exit), so at most 262,144 keys (PBF_ERR_CAPACITY beyond).
  * The first call on a device looks up the array's address with that device
- * current; make it before any stream capture.  Calls share the array: calls
- * whose work overlaps on the GPU race and must be serialized.  Returns after
- * the sort on `stream` (a cudaStream_t, NULL for the default stream) is done. */
+ * current.  d_keys, d_out_keys and d_out_vals must not overlap (an in-place
+ * sort is refused with PBF_ERR_INVALID_ARG).  Calls share the array: calls
+ * whose work overlaps on the GPU race and must be serialized.  The call
+ * blocks until the sort on `stream` (a cudaStream_t, NULL for the default
+ * stream) is done and its status is read back, so it cannot be recorded into
+ * a CUDA graph: on a stream under capture it returns PBF_ERR_INVALID_ARG. */
 int pbf_sort_pairs_noalloc(int device, int n, const unsigned* d_keys, int key_bits,
                            unsigned* d_out_keys, unsigned* d_out_vals, void* stream);
 

@@ -14,12 +14,16 @@
 // kNoAllocScratchBytes reserved until the process exits.  Host code cannot use
 // the array's name as a device address; the first call on each device, with
 // that device current, looks the address up with cudaGetSymbolAddress and
-// caches it.  Do that first call before any stream capture begins.
+// caches it.
+//
+// The call blocks: it waits for the sort on the caller's stream and reads the
+// sort's error word back.  A stream that is being captured is refused.
 //
 // All calls share the one array and it keeps whatever the last call left in
 // it: this entry clears the words that must start at zero on every call, and
 // two calls whose work overlaps on the GPU (different streams or threads at
 // the same time) race on the array and must be serialized by the caller.
+// The keys and the two outputs must not overlap (no in-place sort).
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -31,12 +35,9 @@ namespace {
 
 // Largest key count the static scratch can sort.
 constexpr int kNoAllocMaxKeys = 1 << 18;  // 262,144 keys
-constexpr int kNoAllocTiles = (kNoAllocMaxKeys + pbf::kSortTile - 1) / pbf::kSortTile;
-// Upper bound of pbf::sort_scratch_bytes(kNoAllocMaxKeys), checked at set-up.
-constexpr size_t kNoAllocScratchBytes =
-    (size_t)kNoAllocMaxKeys * 8 + (size_t)kNoAllocMaxKeys * 4 + 512 +
-    (size_t)pbf::kSortMaxPasses * 256 * 4 + 128 +
-    (size_t)pbf::kSortMaxPasses * (size_t)kNoAllocTiles * 256 * 4 + 512;
+// Exactly the scratch the sort carves for that many keys (sort_scratch_bind).
+constexpr size_t kNoAllocScratchBytes = pbf::sort_scratch_bytes(kNoAllocMaxKeys);
+static_assert(kNoAllocScratchBytes < (size_t)8 << 20, "static sort scratch above 8 MB");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -80,6 +81,31 @@ extern "C" int pbf_sort_pairs_noalloc(int device, int n, const unsigned* d_keys,
         return PBF_ERR_INVALID_ARG;
     }
     if (n == 0) return PBF_OK;
+    // The first digit pass writes the outputs while other tiles still read
+    // the keys, so the keys may not share memory with either output.
+    const auto overlaps = [n](const void* a, const void* b) {
+        const uintptr_t pa = reinterpret_cast<uintptr_t>(a), pb = reinterpret_cast<uintptr_t>(b);
+        const uintptr_t len = (uintptr_t)n * sizeof(unsigned);
+        return pa < pb + len && pb < pa + len;
+    };
+    if (overlaps(d_keys, d_out_keys) || overlaps(d_keys, d_out_vals) ||
+        overlaps(d_out_keys, d_out_vals)) {
+        g_noalloc_error = "pbf_sort_pairs_noalloc: d_keys, d_out_keys and d_out_vals must not "
+                          "overlap (no in-place sort)";
+        return PBF_ERR_INVALID_ARG;
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    {
+        // The call waits for the sort and copies its error word back, which a
+        // stream under capture does not allow: refuse instead of breaking the
+        // caller's capture.
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            g_noalloc_error = "pbf_sort_pairs_noalloc: the stream is being captured; this call "
+                              "blocks until the sort is done and cannot be captured";
+            return PBF_ERR_INVALID_ARG;
+        }
+    }
     int prev = -1;
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     cudaError_t e = cudaSetDevice(device);
@@ -100,9 +126,6 @@ extern "C" int pbf_sort_pairs_noalloc(int device, int n, const unsigned* d_keys,
                 g_noalloc_error = std::string("pbf_sort_pairs_noalloc: cudaGetSymbolAddress: ") +
                                   cudaGetErrorString(e);
                 rc = PBF_ERR_CUDA;
-            } else if (pbf::sort_scratch_bytes(kNoAllocMaxKeys) > kNoAllocScratchBytes) {
-                g_noalloc_error = "pbf_sort_pairs_noalloc: static scratch smaller than the sort needs";
-                rc = PBF_ERR_CAPACITY;
             } else {
                 g_scratch_addr[device] = p;
             }
@@ -110,7 +133,6 @@ extern "C" int pbf_sort_pairs_noalloc(int device, int n, const unsigned* d_keys,
         base = g_scratch_addr[device];
     }
     if (rc == PBF_OK) {
-        cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
         pbf::SortScratch s;
         pbf::sort_scratch_bind(s, base, kNoAllocMaxKeys);
         // The array keeps the previous call's contents: the error word must

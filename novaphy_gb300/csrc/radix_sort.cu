@@ -200,27 +200,15 @@ k_onesweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
 
 }  // namespace
 
-size_t sort_scratch_bytes(int capacity) {
-    const int cap = capacity > 0 ? capacity : 1;
-    const int tiles = (cap + kSortTile - 1) / kSortTile;
-    size_t b = 0;
-    b += (size_t)cap * 8 + (size_t)cap * 4 + 256;           // alt keys (64-bit) + vals
-    b += (size_t)kSortMaxPasses * 256 * 4;                  // hist
-    b += 64;                                                // tile counters
-    b += (size_t)kSortMaxPasses * (size_t)tiles * 256 * 4;  // look-back
-    b += 64;                                                // error word
-    return b + 256;
-}
-
 void sort_scratch_bind(SortScratch& s, void* base, int capacity) {
     const int cap = capacity > 0 ? capacity : 1;
     s.capacity = cap;
     s.tiles = (cap + kSortTile - 1) / kSortTile;
     char* p = reinterpret_cast<char*>(base);
     s.keys_alt = reinterpret_cast<void*>(p);
-    p += ((size_t)cap * 8 + 255) / 256 * 256;
+    p += sort_scratch_round((size_t)cap * 8);
     s.vals_alt = reinterpret_cast<uint32_t*>(p);
-    p += ((size_t)cap * 4 + 255) / 256 * 256;
+    p += sort_scratch_round((size_t)cap * 4);
     s.zeroed = reinterpret_cast<uint32_t*>(p);
     s.hist = reinterpret_cast<uint32_t*>(p);
     p += (size_t)kSortMaxPasses * 256 * 4;

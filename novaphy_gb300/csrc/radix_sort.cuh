@@ -38,7 +38,20 @@ struct SortScratch {
     int tiles = 0;
 };
 
-size_t sort_scratch_bytes(int capacity);
+// Bytes of one device allocation that sort_scratch_bind() carves into a
+// sorter's scratch for `capacity` keys; each part starts on a 256-byte
+// boundary.  constexpr, so a static array can be sized with it.
+constexpr size_t sort_scratch_round(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t sort_scratch_bytes(int capacity) {
+    const size_t cap = capacity > 0 ? (size_t)capacity : 1;
+    const size_t tiles = (cap + kSortTile - 1) / kSortTile;
+    return sort_scratch_round(cap * 8)                      // alt keys (room for 64-bit)
+           + sort_scratch_round(cap * 4)                    // alt values
+           + (size_t)kSortMaxPasses * 256 * 4               // hist
+           + 64                                             // tile counters
+           + 64                                             // error word
+           + (size_t)kSortMaxPasses * tiles * 256 * 4;      // look-back
+}
 // Carves the scratch out of one device allocation of sort_scratch_bytes().
 void sort_scratch_bind(SortScratch& s, void* base, int capacity);
 

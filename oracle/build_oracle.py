@@ -4,7 +4,7 @@
   ``oracle/_build/liboracle_pbf.so`` with ``-O2 -ffp-contract=off`` (no fused
   multiply-add, so the operation order is the reference's on x86 and Arm).
 * ``build_ref()`` compiles the reference's own, unmodified fluid sources from
-  ``/root/reference`` (the fluid sources, src/sim/performance_monitor.cpp and
+  the NovaPhy tree named by ``$NOVAPHY_REFERENCE_ROOT`` (the fluid sources, src/sim/performance_monitor.cpp and
   the rigid World that FluidWorld inherits; see REF_SOURCES) with the C-ABI
   harness ``oracle/ref_harness.cpp`` against the Eigen-API subset in
   ``oracle/eigen_shim`` into ``oracle/_ref/libref_pbf.so``.  The reference's
@@ -19,7 +19,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_ROOT = "/root/reference"
+# The NovaPhy source tree; $NOVAPHY_REFERENCE_ROOT overrides where it is read.
+REFERENCE_ROOT = os.environ.get("NOVAPHY_REFERENCE_ROOT", "/root/reference")
 REF_SOURCES = [
     "src/fluid/pbf_solver.cpp",
     "src/fluid/neighbor_search.cpp",
@@ -60,10 +61,13 @@ def build_port(verbose: bool = False) -> str:
     if _newer(PORT_LIB, [src, hdr]):
         return PORT_LIB
     os.makedirs(os.path.dirname(PORT_LIB), exist_ok=True)
-    cmd = ["gcc", "-std=c11", *FP_FLAGS, src, "-lm", "-o", PORT_LIB]
+    cmd = ["gcc", "-std=c11", *FP_FLAGS, "-fopenmp", src, "-lm", "-o", PORT_LIB]
     if verbose:
         print(" ".join(cmd))
-    subprocess.check_call(cmd)
+    if subprocess.call(cmd) != 0:
+        # A host without OpenMP gets the single-threaded build.
+        cmd.remove("-fopenmp")
+        subprocess.check_call(cmd)
     return PORT_LIB
 
 

@@ -84,6 +84,8 @@ class Port:
         L.orc_pbf_step.argtypes = [C.POINTER(Settings), C.c_int, _f32p, _f32p, _f32p, _f32p,
                                    C.c_float, _f32p, C.c_float]
         L.orc_pbf_step.restype = C.c_int
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_max_threads.restype = C.c_int
         L.orc_poly6.argtypes = [C.c_float, C.c_float]
         L.orc_poly6.restype = C.c_float
         L.orc_spiky.argtypes = [C.c_float, C.c_float]
@@ -174,6 +176,13 @@ class Port:
         return xs, vo
 
     # -- PBF step --
+    def set_threads(self, t: int) -> int:
+        """Host threads of the step's per-particle loops (results do not
+        depend on it); returns the count used."""
+        t = max(1, min(int(t), self.lib.orc_max_threads()))
+        self.lib.orc_set_threads(t)
+        return t
+
     def steps(self, settings: Settings, x, v, rho, lam, dt, g, mass, nsteps=1):
         x = _f32(x, (-1, 3)).copy()
         v = _f32(v, (-1, 3)).copy()

@@ -12,6 +12,30 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Host threads of the per-particle loops of orc_pbf_step (1 by default, as
+ * the reference is single-threaded).  Every particle's sums keep their
+ * sequential order, so results do not depend on the thread count. */
+static int g_threads = 1;
+
+void orc_set_threads(int t) { g_threads = t > 0 ? t : 1; }
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_num_procs();
+#else
+    return 1;
+#endif
+}
+
+#ifdef _OPENMP
+#define ORC_PARALLEL_FOR _Pragma("omp parallel for schedule(dynamic, 512) num_threads(g_threads)")
+#else
+#define ORC_PARALLEL_FOR
+#endif
 
 #define ORC_PI 3.14159265358979323846f /* math_utils.h:53 */
 
@@ -334,12 +358,17 @@ static int build_candidates(cand_t* ct, const float* xs, int n, float h) {
         grid_free(&g);
         return -1;
     }
-    long long tot = 0;
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         int c[3];
         world_to_cell(xs + 3 * i, g.inv, c);
+        ct->off[i + 1] = grid_candidates(&g, c, NULL, 0);
+    }
+    long long tot = 0;
+    for (int i = 0; i < n; ++i) {
+        long long m = ct->off[i + 1];
         ct->off[i] = tot;
-        tot += grid_candidates(&g, c, NULL, 0);
+        tot += m;
     }
     ct->off[n] = tot;
     ct->idx = (int*)malloc(sizeof(int) * (size_t)(tot > 0 ? tot : 1));
@@ -348,6 +377,7 @@ static int build_candidates(cand_t* ct, const float* xs, int n, float h) {
         grid_free(&g);
         return -1;
     }
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         int c[3];
         world_to_cell(xs + 3 * i, g.inv, c);
@@ -365,6 +395,7 @@ static void free_candidates(cand_t* ct) {
 static void compute_density(const cand_t* ct, int n, const float* xs, float* rho, float mass,
                             float h) {
     /* pbf_solver.cpp:129-142 (self included) */
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         float density = 0.0f;
         for (long long k = ct->off[i]; k < ct->off[i + 1]; ++k) {
@@ -386,6 +417,7 @@ static void compute_lambda(const cand_t* ct, int n, const float* xs, const float
     float rho0 = s->rest_density;
     float eps = s->epsilon;
     float inv_rho0 = 1.0f / rho0;
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         float C_i = rho[i] * inv_rho0 - 1.0f;
         if (C_i < 0.0f) {
@@ -420,6 +452,7 @@ static void compute_delta_position(const cand_t* ct, int n, const float* xs, con
     float inv_rho0 = 1.0f / rho0;
     float delta_q = s->corr_delta_q * h;
     float w_delta_q = orc_poly6(delta_q * delta_q, h);
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         float d[3] = {0.0f, 0.0f, 0.0f};
         for (long long k = ct->off[i]; k < ct->off[i + 1]; ++k) {
@@ -465,6 +498,7 @@ static void compute_delta_position(const cand_t* ct, int n, const float* xs, con
  * after the XSPH correction. */
 static void vorticity_omega(const cand_t* ct, int n, const float* xs, const float* v,
                             const float* rho, float mass, float rho0, float h, float* omega) {
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         float w[3] = {0.0f, 0.0f, 0.0f};
         for (long long k = ct->off[i]; k < ct->off[i + 1]; ++k) {
@@ -494,6 +528,7 @@ static void vorticity_apply(const cand_t* ct, int n, const float* xs, const floa
     float h = s->kernel_radius;
     float rho0 = s->rest_density;
     float eps_v = s->vorticity_epsilon;
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         float wi = sqrtf(sqn3(omega[3 * i], omega[3 * i + 1], omega[3 * i + 2]));
         float eta[3] = {0.0f, 0.0f, 0.0f};
@@ -561,6 +596,7 @@ int orc_pbf_step(const orc_settings* s, int n, float* x, float* v, float* rho, f
     float inv_dt = 1.0f / dt;
     float max_speed = h / dt;
     float max_speed_sq = max_speed * max_speed;
+    ORC_PARALLEL_FOR
     for (int i = 0; i < n; ++i) {
         float a = (xs[3 * i] - x[3 * i]) * inv_dt;
         float b = (xs[3 * i + 1] - x[3 * i + 1]) * inv_dt;
@@ -583,6 +619,7 @@ int orc_pbf_step(const orc_settings* s, int n, float* x, float* v, float* rho, f
     if (s->xsph_viscosity > 0.0f) {
         float cx = s->xsph_viscosity;
         float rho0 = s->rest_density;
+        ORC_PARALLEL_FOR
         for (int i = 0; i < n; ++i) {
             float vc[3] = {0.0f, 0.0f, 0.0f};
             for (long long k = ct.off[i]; k < ct.off[i + 1]; ++k) {

@@ -43,6 +43,12 @@ typedef struct orc_settings {
 
 void orc_default_settings(orc_settings* s);
 
+/* Host threads of orc_pbf_step's per-particle loops (default 1); results do
+ * not depend on it.  orc_max_threads: the processors OpenMP sees (1 when the
+ * library was built without OpenMP). */
+void orc_set_threads(int t);
+int orc_max_threads(void);
+
 /* SPH kernels, include/novaphy/fluid/sph_kernel.h:24-80. */
 float orc_poly6(float r_sq, float h);
 void orc_spiky_grad(const float* r, float h, float* out);
