@@ -707,63 +707,28 @@ def run_coupled(args, device):
     floor of a 2 x 2 x 2 m box), 4 boxes (edge 0.2 m) and 4 spheres (radius
     0.12 m) of density U(300, 1500) dropped from 0.5-1.0 m above the pool, at
     x-y positions in 8 of the 9 cells of a 3 x 3 grid over the pool (seed 2),
-    a floor plane; Akinci
-    boundary particles at spacing r; h = 4r, 4 iterations, dt = 1/240, s_corr
-    k = 0.1, XSPH 0.01, vorticity 1e-4.  One step = FluidWorld.step: the PBF
-    step, boundary density, coupling forces and torques reduced per body on
-    the device, the host rigid step.  Timed on the host clock over consecutive
-    steps after warm-up."""
-    import novaphy_gb300 as nv
-
-    rng = np.random.default_rng(2)
-    r = 0.015
-    counts = np.array([50, 50, 100])
-    lower = np.array([(2.0 - 50 * r) / 2, (2.0 - 50 * r) / 2, r / 2], np.float32)
-    upper = lower + (counts - 0.5).astype(np.float32) * np.float32(r)
-    mb = nv.ModelBuilder()
-    mb.add_shape(nv.CollisionShape.make_plane([0.0, 0.0, 1.0], 0.0))
-    # x-y: 8 of the 9 cells (0.25 m) of a 3 x 3 grid over the pool footprint,
-    # chosen and jittered from the seed, so no two bodies overlap.
-    cells = rng.permutation(9)[:8]
-    for k in range(8):
-        dens = float(rng.uniform(300.0, 1500.0))
-        cx, cy = divmod(int(cells[k]), 3)
-        xy = lower[:2] + (np.array([cx, cy]) + 0.5) * 0.25 + rng.uniform(-0.005, 0.005, 2)
-        z = float(upper[2] + rng.uniform(0.5, 1.0))
-        t = nv.Transform.from_translation([float(xy[0]), float(xy[1]), z])
-        if k < 4:
-            bi = mb.add_body(nv.RigidBody.from_box(dens * 0.2 ** 3, [0.1, 0.1, 0.1]), t)
-            mb.add_shape(nv.CollisionShape.make_box([0.1, 0.1, 0.1], bi))
-        else:
-            rad = 0.12
-            bi = mb.add_body(nv.RigidBody.from_sphere(dens * 4.0 / 3.0 * np.pi * rad ** 3, rad), t)
-            mb.add_shape(nv.CollisionShape.make_sphere(rad, bi))
-    model = mb.build()
-    blk = nv.FluidBlockDef()
-    blk.lower = lower.tolist()
-    blk.upper = upper.tolist()
-    blk.particle_spacing = r
-    st = nv.PBFSettings()
-    st.kernel_radius = float(np.float32(4 * r))
-    st.particle_radius = float(np.float32(r / 2))
-    st.solver_iterations = 4
-    st.corr_k = 0.1
-    st.corr_delta_q = 0.2
-    st.xsph_viscosity = 0.01
-    st.vorticity_epsilon = 1e-4
-    st.use_domain_bounds = True
-    st.domain_lower = [0.0, 0.0, 0.0]
-    st.domain_upper = [2.0, 2.0, 2.0]
-    world = nv.FluidWorld(model, [blk], nv.SolverSettings(), st, 1.0)
-    world.set_gravity([0.0, 0.0, -9.81])
+    a floor plane; Akinci boundary particles at spacing r; h = 4r, 4
+    iterations, dt = 1/240, PBFSettings' s_corr (k = 0.001, dq = 0.3h), XSPH
+    0.01, vorticity 1e-4.  One step = FluidWorld.step: the PBF step, boundary
+    density, coupling forces and torques reduced per body on the device, the
+    host rigid step.  Timed on the host clock over consecutive steps after
+    warm-up."""
+    spec = workloads.coupled_pool(scorr=args.coupled_scorr)
+    world = workloads.fluid_world_of(spec)
+    st = world.pbf_settings
     dt = float(np.float32(1.0 / 240.0))
     for _ in range(2):
         world.step(dt)
     k = max(1, args.coupled_steps)
+    marks = []
     t0 = time.perf_counter()
-    for _ in range(k):
+    for i in range(k):
         world.step(dt)
+        if (i + 1) % max(1, k // 4) == 0:
+            marks.append(time.perf_counter())
     el = time.perf_counter() - t0
+    seg = k // 4 if k >= 4 else 1
+    quarters = [round((b - a) * 1e3 / seg, 3) for a, b in zip([t0] + marks[:-1], marks)][:4]
     n, nb = world.num_particles, world.num_boundary_particles
     # Device time of every phase over 3 more steps (the monitor runs the same
     # step as separate launches with CUDA events between the phases).
@@ -787,6 +752,10 @@ def run_coupled(args, device):
             "step": "FluidWorld.step: PBF step, boundary density, coupling forces/torques "
                     "(device, per-body serial reduction), host rigid step",
             "timing": f"host clock over {k} consecutive steps after 2 warm-up steps",
+            "ms_per_step_by_quarter": quarters,
+            "s_corr": {"k": float(st.corr_k), "delta_q": float(st.corr_delta_q),
+                       "source": "PBFSettings default" if args.coupled_scorr != "config0"
+                       else "the 8k dam break's"},
             "roofline": {"bound": "hbm", "kernel": KERNEL_OF_PHASE[dom], "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "alg_bytes_per_launch": ALG_BYTES[dom] * n, "launch_ms": launch_ms,
@@ -1093,6 +1062,8 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-coupled", action="store_true")
     ap.add_argument("--coupled-steps", type=int, default=300)
+    ap.add_argument("--coupled-scorr", choices=["default", "config0"], default="default",
+                    help="s_corr of the coupled pool: PBFSettings' own or the dam break's k = 0.1")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the full-budget served run and its plain arm")
     ap.add_argument("--serve-side-seconds", type=float, default=10.0,

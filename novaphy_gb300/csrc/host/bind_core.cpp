@@ -410,6 +410,9 @@ PYBIND11_MODULE(_core, m) {
                                [](const ParticleState& s) { return positions_array(s.velocities); })
         .def_property_readonly("densities_array", [](const ParticleState& s) {
             return py::array_t<float>((py::ssize_t)s.densities.size(), s.densities.data());
+        })
+        .def_property_readonly("lambdas_array", [](const ParticleState& s) {
+            return py::array_t<float>((py::ssize_t)s.lambdas.size(), s.lambdas.data());
         });
 
     py::class_<SpatialHashGrid>(m, "SpatialHashGrid")

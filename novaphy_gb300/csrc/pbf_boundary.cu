@@ -170,6 +170,57 @@ __global__ void k_body_reduce(const float4* __restrict__ Fb, const float4* __res
     torque3[3 * k + 2] = t2;
 }
 
+// Segmented tree reduction of the same sums: one block per body.  Thread t
+// adds the list entries t, t + kTreeThreads, ... of its body in that order,
+// then the block folds its partial sums pairwise (partial[t] += partial[t + s]
+// for s = 128, 64, ..., 1), so every run adds the same floats in the same
+// order: the result is deterministic, whatever the schedule.  It rounds
+// differently from the serial sum above (the reference's order), by at most
+// 2 (m - 1) 2^-24 sum_b |term_b| per component over a body's m terms.
+constexpr int kTreeThreads = 256;
+
+__global__ void __launch_bounds__(kTreeThreads)
+k_body_reduce_tree(const float4* __restrict__ Fb, const float4* __restrict__ bworld,
+                   const int* __restrict__ list_off, const int* __restrict__ list,
+                   const float4* __restrict__ body_pos, int nbodies, float* __restrict__ force3,
+                   float* __restrict__ torque3) {
+    __shared__ float part[6][kTreeThreads];
+    const int k = blockIdx.x;
+    if (k >= nbodies) return;
+    const int t = threadIdx.x;
+    const float4 c = body_pos[k];
+    float a[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const int j1 = list_off[k + 1];
+    for (int j = list_off[k] + t; j < j1; j += kTreeThreads) {
+        const int b = __ldg(list + j);
+        const float4 F = __ldg(Fb + b);
+        if (F.w == 0.0f) continue;
+        const float4 x = __ldg(bworld + b);
+        const float r0 = x.x - c.x, r1 = x.y - c.y, r2 = x.z - c.z;
+        a[0] += F.x;
+        a[1] += F.y;
+        a[2] += F.z;
+        a[3] += r1 * F.z - r2 * F.y;
+        a[4] += r2 * F.x - r0 * F.z;
+        a[5] += r0 * F.y - r1 * F.x;
+    }
+#pragma unroll
+    for (int d = 0; d < 6; ++d) part[d][t] = a[d];
+    __syncthreads();
+#pragma unroll 1
+    for (int s = kTreeThreads / 2; s > 0; s >>= 1) {
+        if (t < s) {
+#pragma unroll
+            for (int d = 0; d < 6; ++d) part[d][t] += part[d][t + s];
+        }
+        __syncthreads();
+    }
+    if (t < 3) {
+        force3[3 * k + t] += part[t][0];
+        torque3[3 * k + t] += part[3 + t][0];
+    }
+}
+
 // One thread per body (rigid_step.hpp on the device).
 __global__ void k_rigid_step(pbf_rigid_body* __restrict__ bodies, int nbodies,
                              const float* __restrict__ force3, const float* __restrict__ torque3,
@@ -282,11 +333,15 @@ cudaError_t coupling_forces(const float4* bworld, const int* body, const int* bo
 
 cudaError_t body_reduce(const float4* Fb, const float4* bworld, const int* list_off,
                         const int* list, const float4* body_pos, int nbodies, float* force3,
-                        float* torque3, cudaStream_t st) {
+                        float* torque3, bool tree, cudaStream_t st) {
     using namespace bnd;
     if (nbodies <= 0) return cudaSuccess;
-    k_body_reduce<<<grid_of(nbodies, 32), 32, 0, st>>>(Fb, bworld, list_off, list, body_pos,
-                                                       nbodies, force3, torque3);
+    if (tree)
+        k_body_reduce_tree<<<nbodies, kTreeThreads, 0, st>>>(Fb, bworld, list_off, list, body_pos,
+                                                             nbodies, force3, torque3);
+    else
+        k_body_reduce<<<grid_of(nbodies, 32), 32, 0, st>>>(Fb, bworld, list_off, list, body_pos,
+                                                           nbodies, force3, torque3);
     return cudaGetLastError();
 }
 

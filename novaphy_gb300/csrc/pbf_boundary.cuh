@@ -66,11 +66,15 @@ cudaError_t coupling_forces(const float4* bworld, const int* body, const int* bo
                             int nb, int nbodies, const QuerySet& Q, const PointIndex& fidx,
                             float4* Fb, const StepConsts& C, cudaStream_t st);
 
-// force/torque[k] += F_b, (x_b - p_k) x F_b over body k's boundary particles in
-// ascending b (fluid_world.cpp:163-172 + World::apply_force/torque order).
+// force/torque[k] += F_b, (x_b - p_k) x F_b over body k's boundary particles.
+// tree = false: one thread per body adds them in ascending b, the reference's
+// order (fluid_world.cpp:163-172 + World::apply_force/torque), bit for bit.
+// tree = true: a deterministic segmented tree reduction (one block per body,
+// fixed pairing), within 2 (m - 1) 2^-24 sum_b |term_b| of the serial sum for
+// a body of m terms.
 cudaError_t body_reduce(const float4* Fb, const float4* bworld, const int* list_off,
                         const int* list, const float4* body_pos, int nbodies, float* force3,
-                        float* torque3, cudaStream_t st);
+                        float* torque3, bool tree, cudaStream_t st);
 
 // Rigid step of the bodies with inv_mass > 0 under gravity g and the coupling
 // force/torque of the step (force3/torque3 hold the first nforce bodies; the

@@ -1332,8 +1332,10 @@ int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
             e = torque_in ? cudaMemcpyAsync(b.torque3, torque_in, bytes, cudaMemcpyHostToDevice, st)
                           : cudaMemsetAsync(b.torque3, 0, bytes, st);
         if (e == cudaSuccess)
+            // The exact build keeps the reference's serial order; the fast
+            // build reduces each body's terms as a tree.
             e = body_reduce(b.Fb, b.world, b.list_off, b.list, b.body_pos, nbodies, b.force3,
-                            b.torque3, st);
+                            b.torque3, !s->settings.exact_arithmetic, st);
     }
     if (e == cudaSuccess) e = mark(3);
     if (e != cudaSuccess) return cuda_fail(e, "coupling forces");

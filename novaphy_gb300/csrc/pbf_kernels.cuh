@@ -421,20 +421,225 @@ __device__ __forceinline__ T ld_step(const T* p) {
     else return __ldg(p);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-cooperative candidate walk (single scenes).
+//
+// The 32 particles of a warp usually sit in one cell, or in two or three
+// cells next to each other along x.  When every lane is clean (no merged
+// reference bucket near it) and the lanes' cells share one (y, z) row and
+// span at most three cells in x, the lanes' candidate sequences are
+// sub-sequences of one sequence: the 9 rows (dz, dy) of cells
+// [xmin - 1, xmax + 1], each in slot order, which is the reference's order
+// (cells in (dz, dy, dx) order, ascending particle index inside a cell).  A
+// lane's own sequence is that one restricted to the cells within one of its
+// own in x.  The warp walks it in chunks:
+//
+//  1. each lane loads one candidate per round of 32 (coalesced); a candidate
+//     farther from the bounding box of the warp's positions than the kernel
+//     support adds an exact zero to every lane and is dropped, the rest are
+//     compacted into shared memory in order, up to CH per chunk;
+//  2. each lane tests the chunk's candidates in order and lists those in its
+//     support (and in its own 27 cells), one byte each;
+//  3. each lane evaluates its listed terms in order.
+//
+// Every lane thus adds exactly the nonzero terms of the one-thread walk, in
+// the same order, so the sums are bit-identical.  The terms (two IEEE
+// divisions and a square root in the exact build) run with the lanes of a
+// step busy instead of waiting on the few in-support lanes of each
+// candidate, and the distance test runs on the surviving candidates only.
+// Only single scenes of at least kBigScene particles walk cooperatively (see
+// CoopBlock).
+
+// Candidates staged per chunk: shared memory is CH * (49 or 65) bytes per
+// warp, under the 48 KB static limit for each block size.
+constexpr int coop_chunk(int bs) { return bs <= 64 ? 256 : bs <= 128 ? 128 : 64; }
+
+template <int CH, bool kExtra>
+struct CoopSmem {
+    float4 x[CH];                 // staged x* (w: lambda or unused)
+    float4 e[kExtra ? CH : 1];    // staged per-candidate extras of the pass
+    unsigned char list[CH * 32];  // list[t * 32 + lane]: t-th term of the lane
+    unsigned char c[CH];          // cell of the candidate among [xmin - 1, xmax + 1]
+};
+
+// Shared memory of a kernel's warps: real for the kernels of a single large
+// scene (those with the 8-way row loop, see kBigScene), one byte otherwise.
+// Small scenes and batches keep the one-thread walk: the shared memory costs
+// them occupancy, and many small scenes side by side measured slower with it.
+template <class P, int BS, bool kExtra, int U>
+struct CoopBlock {
+    static constexpr bool kOn = std::is_same<P, OneScene>::value && U == 8;
+    using Smem = CoopSmem<kOn ? coop_chunk(BS) : 1, kExtra>;
+    static constexpr int kWarps = kOn ? BS / 32 : 1;
+};
+
+// The warp's shared row: cells y = cy, z = cz, x in [xmin, xmin + W - 3];
+// wx0 = wrapped x slot of xmin - 1.
+struct CoopRow {
+    int cy, cz, xmin, W, wx0;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Warp-collective (every lane of the warp must call it): whether the warp
+// walks cooperatively, and its row.  `cell` is the lane's step-start cell
+// with w = its owner row (0 = clean).
+__device__ __forceinline__ bool coop_row(bool active, const int4 cell, const GridDesc& Gd,
+                                         CoopRow& R) {
+    const unsigned full = 0xffffffffu;
+    if (!__all_sync(full, active)) return false;
+    const int cy0 = __shfl_sync(full, cell.y, 0);
+    const int cz0 = __shfl_sync(full, cell.z, 0);
+    if (!__all_sync(full, cell.w == 0 && cell.y == cy0 && cell.z == cz0)) return false;
+    const int xmin = __reduce_min_sync(full, cell.x);
+    const int xmax = __reduce_max_sync(full, cell.x);
+    if ((long long)xmax - (long long)xmin > 2 || xmin <= -(1 << 30) || xmax >= (1 << 30))
+        return false;
+    const int W = xmax - xmin + 3;
+    const int wx0 = wrap(xmin - 1, Gd.ox, Gd.gx);
+    if (wx0 + W > Gd.gx) return false;  // the row range would wrap: one-thread walk
+    R = CoopRow{cy0, cz0, xmin, W, wx0};
+    return true;
+}
+
+// The cooperative walk (see above) of a warp for which coop_row held.  xi is
+// the lane's x*, ci its cell x; `cut` the support test r_sq < cut of the
+// pass.  stage_e(q) returns the extras of candidate q (kExtra); body(xj, ej)
+// adds one in-support term.
+template <int CH, bool kExtra, bool kPersist, class StageE, class Body>
+__device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRow& R, int ci,
+                                          const float4 xi, const float4* xin, float cut,
+                                          const GridDesc& Gd, const uint32_t* __restrict__ off,
+                                          StageE&& stage_e, Body&& body) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    float lx = xi.x, ly = xi.y, lz = xi.z, hx = xi.x, hy = xi.y, hz = xi.z;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(full, lx, o));
+        ly = fminf(ly, __shfl_xor_sync(full, ly, o));
+        lz = fminf(lz, __shfl_xor_sync(full, lz, o));
+        hx = fmaxf(hx, __shfl_xor_sync(full, hx, o));
+        hy = fmaxf(hy, __shfl_xor_sync(full, hy, o));
+        hz = fmaxf(hz, __shfl_xor_sync(full, hz, o));
+    }
+    // A candidate in some lane's support is within sqrt(cut) of the box; the
+    // margin covers the rounding of both distance computations.
+    const float lim = cut * 1.001f;
+    const bool all_member = R.W == 3;  // one cell: every staged candidate is in it
+    const int myc = ci - R.xmin + 1;   // the lane's cell among the row's cells
+    const uint32_t lt = lanemask_lt();
+    int nst = 0;
+
+    auto process = [&]() {
+        __syncwarp();
+        int cnt = 0;
+        if (all_member) {
+#pragma unroll 4
+            for (int k = 0; k < nst; ++k) {
+                const float4 xj = sm.x[k];
+                float rx, ry, rz;
+                if (rel_sq(xi, xj, rx, ry, rz) < cut) {
+                    sm.list[cnt * 32 + lane] = (unsigned char)k;
+                    ++cnt;
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (int k = 0; k < nst; ++k) {
+                const float4 xj = sm.x[k];
+                float rx, ry, rz;
+                const bool in = rel_sq(xi, xj, rx, ry, rz) < cut;
+                if (in && (unsigned)((int)sm.c[k] - myc + 1) <= 2u) {
+                    sm.list[cnt * 32 + lane] = (unsigned char)k;
+                    ++cnt;
+                }
+            }
+        }
+        const int most = __reduce_max_sync(full, (unsigned)cnt);
+        for (int t = 0; t < most; ++t) {
+            if (t < cnt) {
+                const int k = sm.list[t * 32 + lane];
+                if constexpr (kExtra) body(sm.x[k], sm.e[k]);
+                else body(sm.x[k], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+            }
+        }
+        __syncwarp();
+        nst = 0;
+    };
+
+    for (int rr = 0; rr < 9; ++rr) {
+        const int dz = rr / 3 - 1;
+        const int dy = rr - (rr / 3) * 3 - 1;
+        const uint32_t row = Gd.base + (uint32_t)R.wx0 +
+                             (uint32_t)Gd.gx * ((uint32_t)wrap(R.cy + dy, Gd.oy, Gd.gy) +
+                                                (uint32_t)Gd.gy * (uint32_t)wrap(R.cz + dz, Gd.oz, Gd.gz));
+        const uint32_t q0 = __ldg(off + row);
+        const uint32_t q1 = __ldg(off + row + R.W);
+        // Cell boundaries inside the row (cells 1.. W-1 start here).
+        uint32_t b1 = q1, b2 = q1, b3 = q1, b4 = q1;
+        if (!all_member) {
+            b1 = __ldg(off + row + 1);
+            b2 = __ldg(off + row + 2);
+            b3 = __ldg(off + row + 3);
+            if (R.W > 4) b4 = __ldg(off + row + 4);
+        }
+        for (uint32_t qb = q0; qb < q1; qb += 32) {
+            const uint32_t q = qb + (uint32_t)lane;
+            bool pass = false;
+            float4 xj = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (q < q1) {
+                xj = ld_step<kPersist>(xin + q);
+                const float ex = fmaxf(0.0f, fmaxf(lx - xj.x, xj.x - hx));
+                const float ey = fmaxf(0.0f, fmaxf(ly - xj.y, xj.y - hy));
+                const float ez = fmaxf(0.0f, fmaxf(lz - xj.z, xj.z - hz));
+                pass = ex * ex + (ey * ey + ez * ez) < lim;
+            }
+            const uint32_t m = __ballot_sync(full, pass);
+            if (pass) {
+                const int k = nst + __popc(m & lt);
+                sm.x[k] = xj;
+                if constexpr (kExtra) sm.e[k] = stage_e(q);
+                sm.c[k] = (unsigned char)((q >= b1) + (q >= b2) + (q >= b3) + (q >= b4));
+            }
+            nst += __popc(m);
+            if (nst > CH - 32) process();
+        }
+    }
+    if (nst > 0) process();
+}
+
+// Scene of sorted particle p (0 for a single scene).
+__device__ __forceinline__ uint32_t scene_at(const Grid& G, uint32_t p) {
+    return G.spid ? __ldg(G.spid + p) : 0u;
+}
+
 // compute_density + compute_lambda (pbf_solver.cpp:129-179) in one candidate
 // pass for sorted particle p.  Reads x* from xin, writes (x*, lambda) to xout
 // and rho to srho.  Scenes whose `iters` are done by iteration `it` are left
-// untouched.
-template <bool kPersist, int U, class P>
-__device__ __forceinline__ void density_lambda_at(uint32_t p, const float4* xin, float4* xout,
-                                                  float* __restrict__ srho, int it, const Grid& G,
-                                                  const P& prm) {
-    const StepConsts& C = prm.at(G.spid, p);
-    if (it >= C.iters) return;
+// untouched.  Warp-collective: every lane of the warp calls it, with
+// `active` false past the last particle.
+template <bool kPersist, int U, class P, int CH>
+__device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const float4* xin,
+                                                  float4* xout, float* __restrict__ srho, int it,
+                                                  const Grid& G, const P& prm,
+                                                  CoopSmem<CH, false>& sm) {
+    constexpr bool kCoop = CoopBlock<P, 32, false, U>::kOn;
+    const uint32_t pa = active ? p : 0u;
+    const StepConsts& C = prm.at(G.spid, pa);
+    const bool live = active && it < C.iters;
+    const int4 cell = cell_at(G, pa);
+    CoopRow R;
+    bool coop = false;
+    if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R);
+    if (!live) return;
     const float4 xi = xin[p];
     float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
-    for_each_candidate<U>(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        const float4 xj = ld_step<kPersist>(xin + q);
+    auto term = [&](const float4& xj) {
         float rx, ry, rz;
         const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
@@ -448,7 +653,17 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, const float4* xin,
             giy += gy;
             giz += gz;
         }
-    });
+    };
+    if constexpr (kCoop) {
+        if (coop) {
+            coop_walk<CH, false, kPersist>(
+                sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, [](uint32_t) { return float4{}; },
+                [&](const float4& xj, const float4&) { term(xj); });
+        }
+    }
+    if (!coop)
+        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
+                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q)); });
     sum_grad_sq += sqn(gix, giy, giz);
     const float Ci = density * C.inv_rho0 - 1.0f;
     const float lam = (Ci < 0.0f) ? 0.0f : -Ci / (sum_grad_sq + C.eps);
@@ -460,9 +675,11 @@ template <int BS, class P, int U = 4>
 __global__ void __launch_bounds__(BS)
 k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
                  int it, int n, const Grid G, const P prm) {
+    using B = CoopBlock<P, BS, false, U>;
+    __shared__ typename B::Smem sm[B::kWarps];
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)n) return;
-    density_lambda_at<false, U>(p, xin, xout, srho, it, G, prm);
+    density_lambda_at<false, U>(p, p < (uint32_t)n, xin, xout, srho, it, G, prm,
+                                sm[B::kOn ? threadIdx.x >> 5 : 0]);
 }
 
 // Velocity update with speed clamp (pbf_solver.cpp:81-93) for sorted p; w is
@@ -486,17 +703,25 @@ __device__ __forceinline__ float4 update_velocity(float px, float py, float pz, 
 // compute_delta_position + apply_delta (pbf_solver.cpp:181-223, :74-76) for
 // sorted particle p.  Reads (x*, lambda) from xin, writes (x* + dp, lambda_i)
 // to xout; on the scene's last iteration also the updated velocity into sv.
-template <bool kPersist, int U, class P>
-__device__ __forceinline__ void delta_at(uint32_t p, const float4* xin, float4* xout,
+// Warp-collective like density_lambda_at.
+template <bool kPersist, int U, class P, int CH>
+__device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* xin, float4* xout,
                                          const float4* __restrict__ sx,
                                          const float* __restrict__ srho, float4* __restrict__ sv,
-                                         int it, const Grid& G, const P& prm) {
-    const StepConsts& C = prm.at(G.spid, p);
-    if (it >= C.iters) return;
+                                         int it, const Grid& G, const P& prm,
+                                         CoopSmem<CH, false>& sm) {
+    constexpr bool kCoop = CoopBlock<P, 32, false, U>::kOn;
+    const uint32_t pa = active ? p : 0u;
+    const StepConsts& C = prm.at(G.spid, pa);
+    const bool live = active && it < C.iters;
+    const int4 cell = cell_at(G, pa);
+    CoopRow R;
+    bool coop = false;
+    if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R);
+    if (!live) return;
     const float4 xi = xin[p];
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-    for_each_candidate<U>(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        const float4 xj = ld_step<kPersist>(xin + q);
+    auto term = [&](const float4& xj) {
         float rx, ry, rz, lambda_sum;
         const float r_sq = rel_sq<true>(xi, xj, rx, ry, rz, &lambda_sum);
         if (r_sq < C.cut) {
@@ -514,7 +739,17 @@ __device__ __forceinline__ void delta_at(uint32_t p, const float4* xin, float4* 
             dy += a * (c * ry);
             dz += a * (c * rz);
         }
-    });
+    };
+    if constexpr (kCoop) {
+        if (coop) {
+            coop_walk<CH, false, kPersist>(
+                sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, [](uint32_t) { return float4{}; },
+                [&](const float4& xj, const float4&) { term(xj); });
+        }
+    }
+    if (!coop)
+        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
+                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q)); });
     const float px = xi.x + dx * C.inv_rho0;
     const float py = xi.y + dy * C.inv_rho0;
     const float pz = xi.z + dz * C.inv_rho0;
@@ -527,9 +762,11 @@ __global__ void __launch_bounds__(BS)
 k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
         const float* __restrict__ srho, float4* __restrict__ sv, int it, int n, const Grid G,
         const P prm) {
+    using B = CoopBlock<P, BS, false, U>;
+    __shared__ typename B::Smem sm[B::kWarps];
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)n) return;
-    delta_at<false, U>(p, xin, xout, sx, srho, sv, it, G, prm);
+    delta_at<false, U>(p, p < (uint32_t)n, xin, xout, sx, srho, sv, it, G, prm,
+                       sm[B::kOn ? threadIdx.x >> 5 : 0]);
 }
 
 // ---------------------------------------------------------------------------
@@ -590,14 +827,22 @@ __global__ void __launch_bounds__(kBlock)
 k_iterate(float4* xa, float4* xb, float* __restrict__ srho, const float4* __restrict__ sx,
           float4* __restrict__ sv, int max_iters, int n, const Grid G, const P prm,
           const GridSync S) {
+    using B = CoopBlock<P, kBlock, false, 4>;
+    __shared__ typename B::Smem sm[B::kWarps];
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t p0 = blockIdx.x * blockDim.x + threadIdx.x;
+    // The warp strides as a whole, so that its lanes meet in every
+    // warp-collective pass call.
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    auto& my = sm[B::kOn ? threadIdx.x >> 5 : 0];
     for (int it = 0; it < max_iters; ++it) {
-        for (uint32_t p = p0; p < (uint32_t)n; p += stride)
-            density_lambda_at<true, 4>(p, xa, xb, srho, it, G, prm);
+        for (uint32_t pw = w0; pw < (uint32_t)n; pw += stride)
+            density_lambda_at<true, 4>(pw + lane, pw + lane < (uint32_t)n, xa, xb, srho, it, G,
+                                       prm, my);
         if (!grid_sync(S)) return;
-        for (uint32_t p = p0; p < (uint32_t)n; p += stride)
-            delta_at<true, 4>(p, xb, xa, sx, srho, sv, it, G, prm);
+        for (uint32_t pw = w0; pw < (uint32_t)n; pw += stride)
+            delta_at<true, 4>(pw + lane, pw + lane < (uint32_t)n, xb, xa, sx, srho, sv, it, G,
+                              prm, my);
         if (it + 1 < max_iters && !grid_sync(S)) return;
     }
 }
@@ -643,27 +888,46 @@ template <int BS, class P, int U = 4>
 __global__ void __launch_bounds__(BS)
 k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, const float4* __restrict__ sx,
               const float* __restrict__ srho, int n, int skip_vort, const Grid G, const P prm) {
+    using B = CoopBlock<P, BS, true, U>;
+    __shared__ typename B::Smem sm[B::kWarps];
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)n) return;
-    const StepConsts& C = prm.at(G.spid, p);
-    if (skip_vort && C.vort_on) return;
+    const bool active = p < (uint32_t)n;
+    const uint32_t pa = active ? p : 0u;
+    const StepConsts& C = prm.at(G.spid, pa);
+    const bool live = active && !(skip_vort && C.vort_on);
+    const int4 cell = cell_at(G, pa);
+    CoopRow R;
+    bool coop = false;
+    if constexpr (B::kOn) coop = coop_row(live && C.xsph_on, cell, C.grid, R);
+    if (!live) return;
     const float4 xi = xin[p];
     const float4 vi = sv[p];
     float vx = vi.x, vy = vi.y, vz = vi.z;
     if (C.xsph_on) {
         float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-        for_each_candidate<U>(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-            const float4 xj = __ldg(xin + q);
+        auto term = [&](const float4& xj, const float4& vj) {
             float rx, ry, rz;
             const float r_sq = rel_sq(xi, xj, rx, ry, rz);
             if (r_sq < C.h2) {
-                const float4 vj = __ldg(sv + q);
                 const float w = poly6(r_sq, C);
                 cx += vj.w * (vj.x - vi.x) * w;
                 cy += vj.w * (vj.y - vi.y) * w;
                 cz += vj.w * (vj.z - vi.z) * w;
             }
-        });
+        };
+        if constexpr (B::kOn) {
+            if (coop)
+                coop_walk<coop_chunk(BS), true, false>(
+                    sm[threadIdx.x >> 5], R, cell.x, xi, xin, C.h2, C.grid, G.off,
+                    [&](uint32_t q) { return __ldg(sv + q); }, term);
+        }
+        if (!coop) {
+            for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+                const float4 xj = __ldg(xin + q);
+                float rx, ry, rz;
+                if (rel_sq(xi, xj, rx, ry, rz) < C.h2) term(xj, __ldg(sv + q));
+            });
+        }
         vx = vi.x + C.xsph_c * cx;
         vy = vi.y + C.xsph_c * cy;
         vz = vi.z + C.xsph_c * cz;
@@ -679,19 +943,25 @@ template <int BS, class P, int U = 4>
 __global__ void __launch_bounds__(BS)
 k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, float4* __restrict__ sv2,
              float4* __restrict__ som, int n, const Grid G, const P prm) {
+    using B = CoopBlock<P, BS, true, U>;
+    __shared__ typename B::Smem sm[B::kWarps];
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)n) return;
-    const StepConsts& C = prm.at(G.spid, p);
-    if (!C.vort_on) return;
+    const bool active = p < (uint32_t)n;
+    const uint32_t pa = active ? p : 0u;
+    const StepConsts& C = prm.at(G.spid, pa);
+    const bool live = active && C.vort_on;
+    const int4 cell = cell_at(G, pa);
+    CoopRow R;
+    bool coop = false;
+    if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R);
+    if (!live) return;
     const float4 xi = xin[p];
     const float4 vi = sv[p];
     float cx = 0.0f, cy = 0.0f, cz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
-    for_each_candidate<U>(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        const float4 xj = __ldg(xin + q);
+    auto term = [&](const float4& xj, const float4& vj) {
         float rx, ry, rz;
         const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
-            const float4 vj = __ldg(sv + q);
             const float ux = vj.x - vi.x;
             const float uy = vj.y - vi.y;
             const float uz = vj.z - vi.z;
@@ -705,7 +975,20 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
             wy += vj.w * (gz * ux - gx * uz);
             wz += vj.w * (gx * uy - gy * ux);
         }
-    });
+    };
+    if constexpr (B::kOn) {
+        if (coop)
+            coop_walk<coop_chunk(BS), true, false>(sm[threadIdx.x >> 5], R, cell.x, xi, xin,
+                                                   C.cut, C.grid, G.off,
+                                                   [&](uint32_t q) { return __ldg(sv + q); }, term);
+    }
+    if (!coop) {
+        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+            const float4 xj = __ldg(xin + q);
+            float rx, ry, rz;
+            if (rel_sq(xi, xj, rx, ry, rz) < C.cut) term(xj, __ldg(sv + q));
+        });
+    }
     float vx = vi.x, vy = vi.y, vz = vi.z;
     if (C.xsph_on) {
         vx = vi.x + C.xsph_c * cx;
@@ -725,25 +1008,50 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
                    const float4* __restrict__ sv2, const float4* __restrict__ som,
                    const float4* __restrict__ sx, const float* __restrict__ srho, int n,
                    const Grid G, const P prm) {
+    using B = CoopBlock<P, BS, true, U>;
+    __shared__ typename B::Smem sm[B::kWarps];
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (uint32_t)n) return;
-    const StepConsts& C = prm.at(G.spid, p);
-    if (!C.vort_on) return;
+    const bool active = p < (uint32_t)n;
+    const uint32_t pa = active ? p : 0u;
+    const StepConsts& C = prm.at(G.spid, pa);
+    const bool live = active && C.vort_on;
+    const int4 cell = cell_at(G, pa);
+    CoopRow R;
+    bool coop = false;
+    if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R);
+    if (!live) return;
     const float4 xi = xin[p];
     const float4 wi = som[p];
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for_each_candidate<U>(cell_at(G, p), G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
-        const float4 xj = __ldg(xin + q);
+    // e = (m / rho_j', |omega_j|) of the candidate.
+    auto term = [&](const float4& xj, const float4& e) {
         float rx, ry, rz;
         const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
             const float c = spiky_coeff(r_sq, C);
-            const float a = __ldg(sv + q).w * (__ldg(som + q).w - wi.w);
+            const float a = e.x * (e.y - wi.w);
             ex += a * (c * rx);
             ey += a * (c * ry);
             ez += a * (c * rz);
         }
-    });
+    };
+    if constexpr (B::kOn) {
+        if (coop)
+            coop_walk<coop_chunk(BS), true, false>(
+                sm[threadIdx.x >> 5], R, cell.x, xi, xin, C.cut, C.grid, G.off,
+                [&](uint32_t q) {
+                    return make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f);
+                },
+                term);
+    }
+    if (!coop) {
+        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+            const float4 xj = __ldg(xin + q);
+            float rx, ry, rz;
+            if (rel_sq(xi, xj, rx, ry, rz) < C.cut)
+                term(xj, make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f));
+        });
+    }
     const float el = sqrtf(sqn(ex, ey, ez));
     float nx = 0.0f, ny = 0.0f, nz = 0.0f;
     if (el > 1e-9f) {

@@ -162,3 +162,83 @@ def served_scenes(nclients=256, seed=4, n_lo=1000, n_hi=200_000, r=0.02, dt=1.0 
         w.meta["spheres"] = spheres
         out.append(w)
     return out
+
+
+def coupled_pool(seed=2, scorr="default") -> dict:
+    """The two-way coupled pool: a 50 x 50 x 100 lattice (250,000 particles) at
+    r = 0.015 m centred on the floor of a 2 x 2 x 2 m box, 4 boxes (edge 0.2 m)
+    and 4 spheres (radius 0.12 m) of density U(300, 1500) from ``default_rng(
+    seed)``, dropped from 0.5-1.0 m above the pool at x-y positions in 8 of the
+    9 cells (0.25 m) of a 3 x 3 grid over the pool footprint (jittered by up to
+    5 mm, so no two bodies overlap), a floor plane (normal +z, offset 0),
+    Akinci boundary particles at spacing r over a boundary extent of 1 m; h =
+    4r, 4 iterations, dt = 1/240 s, XSPH 0.01, vorticity 1e-4, gravity -9.81 z,
+    domain clamp on [0, 2]^3 with particle_radius = r/2.  s_corr: PBFSettings'
+    own (k = 0.001, dq = 0.3 h) with scorr="default" (the pool's configuration
+    does not set it), or the dam break's k = 0.1, dq = 0.2 h with "config0".
+
+    Returns a dict: block (lower, upper, spacing), bodies as (kind, size3,
+    mass, pos3, quat4 (w, x, y, z)) with kind "box" (half extents) or "sphere"
+    (size3[0] = radius), plane (normal3, offset), boundary_extent, settings
+    (PBFSettings fields), gravity, dt.  Masses and positions are float32."""
+    rng = np.random.default_rng(seed)
+    r = 0.015
+    counts = np.array([50, 50, 100])
+    lower = np.array([(2.0 - 50 * r) / 2, (2.0 - 50 * r) / 2, r / 2], np.float32)
+    upper = lower + (counts - 0.5).astype(np.float32) * np.float32(r)
+    cells = rng.permutation(9)[:8]
+    bodies = []
+    for k in range(8):
+        dens = float(rng.uniform(300.0, 1500.0))
+        cx, cy = divmod(int(cells[k]), 3)
+        xy = lower[:2] + (np.array([cx, cy]) + 0.5) * 0.25 + rng.uniform(-0.005, 0.005, 2)
+        z = float(upper[2] + rng.uniform(0.5, 1.0))
+        pos = tuple(float(t) for t in np.array([xy[0], xy[1], z], np.float32))
+        if k < 4:
+            bodies.append(("box", (0.1, 0.1, 0.1), float(np.float32(dens * 0.2 ** 3)), pos,
+                           (1.0, 0.0, 0.0, 0.0)))
+        else:
+            rad = 0.12
+            m = float(np.float32(dens * 4.0 / 3.0 * np.pi * rad ** 3))
+            bodies.append(("sphere", (rad, 0.0, 0.0), m, pos, (1.0, 0.0, 0.0, 0.0)))
+    settings = dict(
+        rest_density=1000.0, kernel_radius=float(np.float32(4 * r)),
+        particle_radius=float(np.float32(r / 2)), solver_iterations=4, epsilon=100.0,
+        xsph_viscosity=0.01, vorticity_epsilon=1e-4, corr_delta_q=0.3, corr_k=0.001, corr_n=4,
+        use_domain_bounds=1, domain_lower=(0.0, 0.0, 0.0), domain_upper=(2.0, 2.0, 2.0))
+    if scorr == "config0":
+        settings.update(corr_k=0.1, corr_delta_q=0.2)
+    return dict(block=(tuple(float(t) for t in lower), tuple(float(t) for t in upper), r),
+                bodies=bodies, plane=((0.0, 0.0, 1.0), 0.0), boundary_extent=1.0,
+                settings=settings, gravity=np.array([0.0, 0.0, -9.81], np.float32),
+                dt=float(np.float32(1.0 / 240.0)), r=r)
+
+
+def fluid_world_of(spec):
+    """The package's FluidWorld of a coupled_pool spec (the native module)."""
+    import novaphy_gb300 as nv
+
+    mb = nv.ModelBuilder()
+    normal, offset = spec["plane"]
+    mb.add_shape(nv.CollisionShape.make_plane(list(normal), offset))
+    for kind, size, mass, pos, quat in spec["bodies"]:
+        t = nv.Transform.from_translation(list(pos))
+        if kind == "box":
+            bi = mb.add_body(nv.RigidBody.from_box(mass, list(size)), t)
+            mb.add_shape(nv.CollisionShape.make_box(list(size), bi))
+        else:
+            bi = mb.add_body(nv.RigidBody.from_sphere(mass, size[0]), t)
+            mb.add_shape(nv.CollisionShape.make_sphere(size[0], bi))
+    lower, upper, spacing = spec["block"]
+    blk = nv.FluidBlockDef()
+    blk.lower = list(lower)
+    blk.upper = list(upper)
+    blk.particle_spacing = spacing
+    st = nv.PBFSettings()
+    for k, v in spec["settings"].items():
+        if k == "use_domain_bounds":
+            v = bool(v)
+        setattr(st, k, list(v) if isinstance(v, tuple) else v)
+    world = nv.FluidWorld(mb.build(), [blk], nv.SolverSettings(), st, spec["boundary_extent"])
+    world.set_gravity([float(g) for g in spec["gravity"]])
+    return world

@@ -293,6 +293,11 @@ class Ref:
                                           C.c_float, C.c_float, C.c_int, C.c_int, _f32p, _f32p,
                                           _f32p, _f32p, _f32p, _f32p, _f32p, _f32p]
         L.ref_fluid_world_run.restype = C.c_int
+        L.ref_fluid_world_run_ex.argtypes = [
+            C.POINTER(Settings), _f32p, _f32p, C.c_float, C.c_int, _i32p, _f32p, _f32p, _f32p,
+            _f32p, C.c_int, _f32p, C.c_float, C.c_float, _f32p, C.c_float, C.c_int, C.c_int,
+            _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p]
+        L.ref_fluid_world_run_ex.restype = C.c_int
         L.ref_world_run.argtypes = [C.c_int, _i32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
                                     C.c_void_p, C.c_void_p, C.c_float, C.c_int, _f32p, _f32p,
                                     _f32p, _f32p]
@@ -392,6 +397,35 @@ class Ref:
             C.byref(settings), _f32(lower, (3,)), _f32(upper, (3,)), spacing, nb, kind, size,
             mass, pos, quat, 0 if plane_y is None else 1, 0.0 if plane_y is None else plane_y,
             boundary_extent, dt, nsteps, cap, x, v, rho, lam, bp, bq, bv, bw)
+        if n < 0:
+            raise ValueError("the reference FluidWorld failed")
+        return x[:n], v[:n], rho[:n], lam[:n], bp[:nb], bq[:nb], bv[:nb], bw[:nb]
+
+    def fluid_world_ex(self, settings: Settings, lower, upper, spacing, bodies, plane=None,
+                       gravity=(0.0, -9.81, 0.0), boundary_extent=1.0, dt=1.0 / 60.0, nsteps=1,
+                       cap=1 << 20):
+        """As fluid_world, with plane = (normal3, offset) or None and the
+        world's gravity set to `gravity`."""
+        nb = len(bodies)
+        kind = np.array([0 if b[0] == "sphere" else 1 for b in bodies] or [0], np.int32)
+        size = _f32([list(b[1]) for b in bodies] or [[0, 0, 0]], (-1, 3))
+        mass = _f32([b[2] for b in bodies] or [0])
+        pos = _f32([list(b[3]) for b in bodies] or [[0, 0, 0]], (-1, 3))
+        quat = _f32([list(b[4]) for b in bodies] or [[1, 0, 0, 0]], (-1, 4))
+        x = np.zeros((cap, 3), np.float32)
+        v = np.zeros((cap, 3), np.float32)
+        rho = np.zeros(cap, np.float32)
+        lam = np.zeros(cap, np.float32)
+        bp = np.zeros((max(nb, 1), 3), np.float32)
+        bq = np.zeros((max(nb, 1), 4), np.float32)
+        bv = np.zeros((max(nb, 1), 3), np.float32)
+        bw = np.zeros((max(nb, 1), 3), np.float32)
+        normal = _f32(plane[0] if plane else (0.0, 1.0, 0.0), (3,))
+        offset = float(plane[1]) if plane else 0.0
+        n = self.lib.ref_fluid_world_run_ex(
+            C.byref(settings), _f32(lower, (3,)), _f32(upper, (3,)), spacing, nb, kind, size,
+            mass, pos, quat, 1 if plane else 0, normal, offset, boundary_extent,
+            _f32(gravity, (3,)), dt, nsteps, cap, x, v, rho, lam, bp, bq, bv, bw)
         if n < 0:
             raise ValueError("the reference FluidWorld failed")
         return x[:n], v[:n], rho[:n], lam[:n], bp[:nb], bq[:nb], bv[:nb], bw[:nb]

@@ -209,18 +209,23 @@ int ref_sample_plane(const float* normal, float offset, float spacing, float ext
 // FluidWorld::step (fluid_world.cpp:46-99) over nsteps steps of a world with
 // one fluid block and nb bodies: kind[k] 0 = sphere (size[3k] = radius),
 // 1 = box (size[3k..3k+2] = half extents), mass[k], pose pos3/quat4 (w, x, y,
-// z; normalised), plus a ground plane at y = plane_y when with_plane.  Gravity is the
-// World default (0, -9.81, 0).  Writes the fluid state (n particles, as
-// ParticleState) and the bodies' poses and velocities; returns n, or -1.
-int ref_fluid_world_run(const ref_settings* st, const float* lower, const float* upper,
-                        float spacing, int nb, const int* kind, const float* size,
-                        const float* mass, const float* pos3, const float* quat4, int with_plane,
-                        float plane_y, float boundary_extent, float dt, int nsteps, int cap,
-                        float* x3, float* v3, float* rho, float* lam, float* body_pos3,
-                        float* body_quat4, float* body_v3, float* body_w3) {
+// z; normalised), plus, when with_plane, a plane make_plane(plane_normal3,
+// plane_offset) with the default friction and restitution.  The world's
+// gravity is gravity3 (null: the World default (0, -9.81, 0)).  Writes the
+// fluid state (n particles, as ParticleState) and the bodies' poses and
+// velocities; returns n, or -1.
+int ref_fluid_world_run_ex(const ref_settings* st, const float* lower, const float* upper,
+                           float spacing, int nb, const int* kind, const float* size,
+                           const float* mass, const float* pos3, const float* quat4,
+                           int with_plane, const float* plane_normal3, float plane_offset,
+                           float boundary_extent, const float* gravity3, float dt, int nsteps,
+                           int cap, float* x3, float* v3, float* rho, float* lam,
+                           float* body_pos3, float* body_quat4, float* body_v3, float* body_w3) {
     try {
         ModelBuilder mb;
-        if (with_plane) mb.add_ground_plane(plane_y);
+        if (with_plane)
+            mb.add_shape(CollisionShape::make_plane(
+                Vec3f(plane_normal3[0], plane_normal3[1], plane_normal3[2]), plane_offset));
         for (int k = 0; k < nb; ++k) {
             // Transform(p, q) normalises q, as the reference's Python API does.
             const Transform t(Vec3f(pos3[3 * k], pos3[3 * k + 1], pos3[3 * k + 2]),
@@ -240,6 +245,7 @@ int ref_fluid_world_run(const ref_settings* st, const float* lower, const float*
         blk.upper = Vec3f(upper[0], upper[1], upper[2]);
         blk.particle_spacing = spacing;
         FluidWorld fw(mb.build(), {blk}, SolverSettings{}, to_settings(st), boundary_extent);
+        if (gravity3) fw.set_gravity(Vec3f(gravity3[0], gravity3[1], gravity3[2]));
         for (int s = 0; s < nsteps; ++s) fw.step(dt);
         const ParticleState& ps = fw.fluid_state();
         const int n = ps.num_particles();
@@ -269,6 +275,20 @@ int ref_fluid_world_run(const ref_settings* st, const float* lower, const float*
     } catch (...) {
         return -1;
     }
+}
+
+// ref_fluid_world_run_ex with the ground plane of add_ground_plane(plane_y)
+// (normal +y, model_builder.cpp:42-46) and the World's default gravity.
+int ref_fluid_world_run(const ref_settings* st, const float* lower, const float* upper,
+                        float spacing, int nb, const int* kind, const float* size,
+                        const float* mass, const float* pos3, const float* quat4, int with_plane,
+                        float plane_y, float boundary_extent, float dt, int nsteps, int cap,
+                        float* x3, float* v3, float* rho, float* lam, float* body_pos3,
+                        float* body_quat4, float* body_v3, float* body_w3) {
+    const float up[3] = {0.0f, 1.0f, 0.0f};
+    return ref_fluid_world_run_ex(st, lower, upper, spacing, nb, kind, size, mass, pos3, quat4,
+                                  with_plane, up, plane_y, boundary_extent, nullptr, dt, nsteps,
+                                  cap, x3, v3, rho, lam, body_pos3, body_quat4, body_v3, body_w3);
 }
 
 // World::step (world.cpp) over nsteps steps of nb free bodies (kind, size,

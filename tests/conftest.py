@@ -21,6 +21,17 @@ def port():
 
 
 @pytest.fixture(scope="session")
+def port_mt():
+    """The oracle restatement with its per-particle loops on every host core
+    (results do not depend on the thread count), for large parity cases."""
+    from oracle.oracle import Port
+
+    p = Port()
+    p.set_threads(os.cpu_count() or 1)
+    return p
+
+
+@pytest.fixture(scope="session")
 def ref():
     from oracle import build_oracle
     from oracle.oracle import Ref

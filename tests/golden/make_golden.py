@@ -7,7 +7,8 @@ oracle restatement (oracle/pbf_oracle.c) reproduces every fixture bit for
 bit, so the fixtures pin the restatement.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(fluid_world.npz alone: python tests/golden/make_golden.py fluid_world)
+(fluid_world.npz alone: python tests/golden/make_golden.py fluid_world; the
+digests at the benchmarked sizes alone: ... make_golden.py large)
 """
 from __future__ import annotations
 
@@ -193,6 +194,81 @@ def fluid_world_contacts_fixture():
     print("fluid_world_contacts.npz written:", len(x), "particles")
 
 
+def field_digests(x, v, rho, lam) -> dict:
+    return {"x": digest(x), "v": digest(v), "rho": digest(rho), "lam": digest(lam)}
+
+
+# The 32 scenes of the batched workload that the large digests cover: every
+# 32nd of the 1,024.
+BATCH_SUBSET = slice(0, 1024, 32)
+
+
+def large_digests():
+    """Digests at the benchmarked sizes.  The reference has no vorticity
+    confinement, so the reference build runs each case with vorticity 0 (the
+    restatement must equal it bit for bit there), and the restatement alone
+    gives the digests with the configured vorticity (1e-4):
+      * one seeded step of the 1M-particle dam break (workloads.dam_break_1m):
+        reference build at vorticity 0, restatement at 1e-4;
+      * one FluidWorld.step of the coupled pool (workloads.coupled_pool: 250,000
+        fluid particles, 8 bodies, a floor plane), fluid state and bodies, from
+        the reference build at vorticity 0;
+      * one step of each of 32 scenes of workloads.batched_scenes(): reference
+        build at vorticity 0, restatement at each scene's own vorticity."""
+    R = Ref()
+    P = Port()
+    P.set_threads(os.cpu_count() or 1)
+    out = {}
+
+    def both(sw, vort):
+        st = dict(sw.settings, vorticity_epsilon=vort)
+        s = Settings.make(**st)
+        z = np.zeros(sw.n, np.float32)
+        return (R.steps(s, sw.x, sw.v, z, z, sw.dt, sw.gravity, sw.mass, 1),
+                P.steps(s, sw.x, sw.v, z, z, sw.dt, sw.gravity, sw.mass, 1))
+
+    def mine_only(sw):
+        s = Settings.make(**sw.settings)
+        z = np.zeros(sw.n, np.float32)
+        return P.steps(s, sw.x, sw.v, z, z, sw.dt, sw.gravity, sw.mass, 1)
+
+    w = workloads.dam_break_1m()
+    got, mine = both(w, 0.0)
+    for a, b in zip(got, mine):
+        assert np.array_equal(a, b), "restatement differs from the reference build (1M)"
+    out["dam_break_1m_input"] = digest(w.x)
+    out["dam_break_1m_step1_vort0_ref"] = field_digests(*got)
+    assert w.settings["vorticity_epsilon"] > 0
+    out["dam_break_1m_step1_port"] = field_digests(*mine_only(w))
+    print("1M done", flush=True)
+
+    spec = workloads.coupled_pool()
+    spec["settings"]["vorticity_epsilon"] = 0.0
+    lower, upper, spacing = spec["block"]
+    x, v, rho, lam, bp, bq, bv, bw = R.fluid_world_ex(
+        Settings.make(**spec["settings"]), lower, upper, spacing, spec["bodies"],
+        plane=spec["plane"], gravity=spec["gravity"], boundary_extent=spec["boundary_extent"],
+        dt=spec["dt"], nsteps=1)
+    d = field_digests(x, v, rho, lam)
+    d.update(n=int(len(x)), body_pos=digest(bp), body_quat=digest(bq), body_v=digest(bv),
+             body_w=digest(bw))
+    out["coupled_pool_step1_vort0_ref"] = d
+    print("coupled pool done", len(x), flush=True)
+
+    scenes = workloads.batched_scenes()[BATCH_SUBSET]
+    per = []
+    for sw in scenes:
+        got, mine = both(sw, 0.0)
+        for a, b in zip(got, mine):
+            assert np.array_equal(a, b), "restatement differs from the reference build (batch)"
+        per.append(dict(name=sw.name, n=int(sw.n), vort0_ref=field_digests(*got),
+                        port=field_digests(*mine_only(sw))))
+    out["batched_subset_step1"] = per
+    with open(os.path.join(HERE, "digests_large.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("digests_large.json written")
+
+
 if __name__ == "__main__":
     # With names, only those fixtures: python tests/golden/make_golden.py fluid_world
     names = sys.argv[1:]
@@ -201,7 +277,10 @@ if __name__ == "__main__":
             fluid_world_fixture()
         if "fluid_world_contacts" in names:
             fluid_world_contacts_fixture()
+        if "large" in names:
+            large_digests()
     else:
         main()
         fluid_world_fixture()
         fluid_world_contacts_fixture()
+        large_digests()

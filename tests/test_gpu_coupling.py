@@ -134,3 +134,57 @@ def test_batched_step_then_couple_equals_coupled_step(port):
     for a, c in zip(ref.state(), sc.state()):
         assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
     assert np.array_equal(f, rf) and np.array_equal(t, rt)
+
+
+@pytest.mark.parametrize("radius,spacing", [(0.06, 0.025), (0.1, 0.008)])
+def test_fast_build_tree_wrench_within_its_bound(port, radius, spacing):
+    """The fast build reduces each body's coupling terms as a deterministic
+    segmented tree instead of the reference's serial sum.  Per component the
+    two sums of a body's m terms differ by at most 2 (m - 1) 2^-24 sum |term|;
+    the terms themselves are the oracle's, one boundary particle at a time.
+    The boundary density stays bit-exact, and two runs give the same bits."""
+    w = workloads.dam_break((10, 10, 10), 0.025, (1.0, 1.0, 1.0), dt=1.0 / 120.0, seed=0,
+                            vorticity=0.0)
+    ident = np.array([1, 0, 0, 0], np.float32)
+    local = port.sample_sphere(radius, (0, 0, 0), ident, np.float32(spacing)).astype(np.float32)
+    body = np.zeros(len(local), np.int32)
+    bp = np.array([[0.12, 0.12, 0.12]], np.float32)
+    bq = ident[None, :]
+    dyn = np.array([1], np.int32)
+    h = np.float32(w.settings["kernel_radius"])
+    world0 = port.boundary_world_positions(local, body, bp, bq)
+    psi = port.boundary_volumes(world0, h)
+    f0 = np.array([[0.1, -0.2, 0.3]], np.float32)
+    t0 = np.array([[0.01, 0.02, -0.03]], np.float32)
+    runs = []
+    for _ in range(2):
+        sc = capi.Scene(capi.default_settings(**w.settings, exact_arithmetic=0), w.x, w.v,
+                        mass=w.mass)
+        sc.set_gravity(w.gravity)
+        sc.set_boundary(local, body, psi)
+        sc.set_bodies(bp, bq, dyn)
+        sc.step(w.dt, 1)
+        x, _, rho_pre, _ = sc.state()
+        f, t = sc.couple(w.dt, f0, t0)
+        runs.append((x, rho_pre, sc.state()[2], f, t))
+        sc.close()
+    x, rho_pre, rho, f, t = runs[0]
+    assert all(np.array_equal(a, b) for a, b in zip(runs[0], runs[1])), "not deterministic"
+    rho_b = port.boundary_density(x, rho_pre, world0, psi, h, np.float32(1000.0))
+    assert np.array_equal(rho, rho_b)
+    want_f, want_t = port_coupling_accumulated(port, x, rho_b, w.mass, world0, body, psi, dyn,
+                                               bp, h, f0, t0)
+    terms_f, terms_t = [], []
+    for b in range(len(local)):
+        tf, tt = port.coupling_forces(x, rho_b, w.mass, world0[b:b + 1], body[b:b + 1],
+                                      psi[b:b + 1], dyn, bp, h, np.float32(1000.0))
+        terms_f.append(tf[0])
+        terms_t.append(tt[0])
+    terms_f, terms_t = np.array(terms_f, np.float64), np.array(terms_t, np.float64)
+    m = int((np.abs(terms_f).sum(1) > 0).sum())
+    assert m > 10, "the sphere must sit in the fluid"
+    u = 2.0 ** -24
+    tol_f = 2 * (m + 1) * u * (np.abs(terms_f).sum(0) + np.abs(f0[0]))
+    tol_t = 2 * (m + 1) * u * (np.abs(terms_t).sum(0) + np.abs(t0[0]))
+    assert (np.abs(f[0].astype(np.float64) - want_f[0]) <= tol_f).all(), (f, want_f, tol_f)
+    assert (np.abs(t[0].astype(np.float64) - want_t[0]) <= tol_t).all(), (t, want_t, tol_t)

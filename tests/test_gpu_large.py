@@ -1,0 +1,69 @@
+"""Parity of large single scenes (at least 2^18 particles), where the
+constraint, XSPH and vorticity passes take the warp-cooperative neighbour
+walk: the exact build must still equal the oracle bit for bit.
+
+The cases cover warps that sit in one cell (a lattice whose cells hold 4 x 4 x 4
+particles), warps that straddle two or three cells of a row (h = 3.5 r, so
+cells hold 27 to 64 particles), the second step of the configured dam break
+(the first one scatters the lattice, so warps straddle rows and cells fill
+unevenly), the plain 27-cell neighbourhood (hash_compat 0) and the reference's
+hash buckets near the axes (a block at the origin).
+"""
+import numpy as np
+import pytest
+
+from novaphy_gb300 import capi, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(port_mt, w, nsteps, **kw):
+    from oracle.oracle import Settings
+
+    st = dict(w.settings)
+    st.update(kw)
+    sc = capi.Scene(capi.default_settings(**st, exact_arithmetic=1), w.x, w.v, mass=w.mass)
+    sc.set_gravity(w.gravity)
+    sc.step(w.dt, nsteps)
+    got = sc.state()
+    sc.close()
+    ost = {k: v for k, v in st.items() if k not in ("exact_arithmetic", "hash_compat")}
+    z = np.zeros(w.n, np.float32)
+    want = port_mt.steps(Settings.make(**ost), w.x, w.v, z, z, w.dt, w.gravity, w.mass, nsteps)
+    return got, want
+
+
+def assert_equal(got, want, tag):
+    for name, a, b in zip("x v rho lam".split(), got, want):
+        bad = np.flatnonzero(~((a == b) | (np.isnan(a) & np.isnan(b))).reshape(len(a), -1).all(1))
+        assert bad.size == 0, (tag, name, bad[:5], bad.size)
+
+
+@pytest.mark.parametrize("nsteps", [1, 2])
+def test_lattice_block_one_cell_per_warp(port_mt, nsteps):
+    w = workloads.dam_break((64, 64, 64), 0.01, (4.0, 2.0, 2.0), dt=1.0 / 240.0, jitter=1e-5,
+                            seed=5, vorticity=1e-4)
+    assert w.n >= 1 << 18
+    assert_equal(*run_both(port_mt, w, nsteps), ("lattice", nsteps))
+
+
+def test_warps_straddle_cells(port_mt):
+    # h = 3.5 r: cells of 27 to 64 particles, so warps span two or three
+    # cells of a row, or two rows.
+    w = workloads.dam_break((66, 64, 64), 0.01, (4.0, 2.0, 2.0), h_factor=3.5, dt=1.0 / 240.0,
+                            jitter=1e-5, seed=6, vorticity=1e-4)
+    assert w.n >= 1 << 18
+    assert_equal(*run_both(port_mt, w, 2), "straddle")
+
+
+@pytest.mark.parametrize("kw", [dict(hash_compat=0), dict(vorticity_epsilon=0.0),
+                                dict(corr_k=0.001, corr_delta_q=0.3, xsph_viscosity=0.0)])
+def test_large_settings_variants(port_mt, kw):
+    w = workloads.dam_break((64, 64, 65), 0.01, (4.0, 2.0, 2.0), dt=1.0 / 240.0, jitter=1e-5,
+                            seed=7, vorticity=1e-4)
+    if kw.get("hash_compat") == 0:
+        # Away from the axes the reference's buckets are the plain 27 cells.
+        shift = np.array([0.5, 0.25, 0.25], np.float32)
+        w.x = (w.x + shift).astype(np.float32)
+        assert port_mt.hash_collisions(w.x, np.float32(w.settings["kernel_radius"])) == 0
+    assert_equal(*run_both(port_mt, w, 2, **kw), kw)
