@@ -144,6 +144,14 @@ int pbf_scene_device_field(pbf_scene* scene, int field, void** dptr);
 /* The CUDA stream (cudaStream_t) the scene's work is ordered on. */
 int pbf_scene_stream(pbf_scene* scene, void** stream);
 
+/* Page-locked (pinned) host memory, usable from every device: pbf_scene_read
+ * into it is a single DMA, and the host World's array views of the fluid state
+ * sit in it.  No counterpart in the reference, whose ParticleState accessors
+ * return list copies (python/bindings/bind_fluid.cpp:120-131).  bytes == 0
+ * gives NULL; pbf_host_free(NULL) is a no-op. */
+int pbf_host_alloc(size_t bytes, void** out);
+int pbf_host_free(void* p);
+
 /* Host-array drop-in of PBFSolver::step(ParticleState&, dt, gravity, mass)
  * (include/novaphy/fluid/pbf_solver.h:72, pbf_solver.cpp:18-127): uploads x,
  * v, densities and lambdas, runs one step, downloads them in place.  The

@@ -4,6 +4,7 @@
 // callers use (bind_sim.cpp, bind_core.cpp, bind_math.cpp,
 // bind_performance.cpp).  Vector3 values are float32 numpy arrays of shape
 // (3,), like the reference's Eigen binding; any length-3 sequence is accepted.
+#include <cstdint>
 #include <cstring>
 
 #include <pybind11/numpy.h>
@@ -56,6 +57,31 @@ py::array_t<float> positions_array(const std::vector<Vec3>& v) {
     if (!v.empty()) std::memcpy(a.mutable_data(), &v[0].x, v.size() * sizeof(Vec3));
     return a;
 }
+
+// A fluid field in device memory, handed to other libraries through
+// __cuda_array_interface__ (version 3) without a copy.  Keeps its world alive.
+struct DeviceFieldView {
+    uintptr_t ptr = 0;
+    py::ssize_t n = 0;
+    bool vec = false;
+    py::object owner;
+    py::dict interface() const {
+        py::dict d;
+        if (vec) {
+            d["shape"] = py::make_tuple(n, 3);
+            d["strides"] = py::make_tuple(16, 4);  // float4 rows on the device
+        } else {
+            d["shape"] = py::make_tuple(n);
+            d["strides"] = py::make_tuple(4);
+        }
+        d["typestr"] = "<f4";
+        d["data"] = py::make_tuple(n > 0 ? ptr : (uintptr_t)0, false);
+        d["version"] = 3;
+        return d;
+    }
+};
+
+const char* const kFieldNames[4] = {"positions", "velocities", "densities", "lambdas"};
 
 }  // namespace
 
@@ -471,7 +497,57 @@ PYBIND11_MODULE(_core, m) {
         .def_property_readonly("boundary_particles", &FluidWorld::boundary_particles,
                                py::return_value_policy::reference_internal)
         .def_property_readonly("pbf_settings", &FluidWorld::pbf_settings,
-                               py::return_value_policy::reference_internal);
+                               py::return_value_policy::reference_internal)
+        // Zero-copy state access (the reference's accessors copy into lists).
+        .def(
+            "fluid_arrays",
+            [](py::object self) {
+                FluidWorld& w = self.cast<FluidWorld&>();
+                py::dict out;
+                const py::ssize_t n = w.num_particles();
+                for (int f = 0; f < 4; ++f) {
+                    const float* p = w.fluid_pinned(f);
+                    const bool vec = f < 2;
+                    std::vector<py::ssize_t> shape = vec ? std::vector<py::ssize_t>{n, 3}
+                                                         : std::vector<py::ssize_t>{n};
+                    static float empty = 0.0f;
+                    py::array_t<float> a(shape, p ? p : &empty, self);
+                    a.attr("setflags")(py::arg("write") = false);
+                    out[kFieldNames[f]] = a;
+                }
+                return out;
+            },
+            "The fluid state as numpy arrays that view page-locked host memory owned by the "
+            "world: positions and velocities (n, 3), densities and lambdas (n,), float32. Each "
+            "field is read from the device by one DMA, only when a step ran since its last "
+            "read; the arrays are read-only views, so the next call after a step rewrites them "
+            "in place.")
+        .def(
+            "fluid_device_arrays",
+            [](py::object self) {
+                FluidWorld& w = self.cast<FluidWorld&>();
+                py::dict out;
+                for (int f = 0; f < 4; ++f) {
+                    DeviceFieldView v;
+                    v.ptr = reinterpret_cast<uintptr_t>(w.fluid_device_field(f));
+                    v.n = w.num_particles();
+                    v.vec = f < 2;
+                    v.owner = self;
+                    out[kFieldNames[f]] = v;
+                }
+                return out;
+            },
+            "The fluid state in device memory as __cuda_array_interface__ views (no copy): "
+            "positions and velocities (n, 3) with 16-byte rows, densities and lambdas (n,), "
+            "float32, e.g. torch.as_tensor(view, device='cuda'). The world's stream is idle when "
+            "this returns; later steps show through once they are synchronised.");
+
+    py::class_<DeviceFieldView>(m, "DeviceFieldView")
+        .def_property_readonly("__cuda_array_interface__", &DeviceFieldView::interface)
+        .def_property_readonly("shape", [](const DeviceFieldView& v) -> py::tuple {
+            if (v.vec) return py::make_tuple(v.n, 3);
+            return py::make_tuple(v.n);
+        });
 
     m.def("generate_fluid_block", &generate_fluid_block, py::arg("block_def"));
     m.def("sample_model_boundaries", &sample_model_boundaries, py::arg("model"),

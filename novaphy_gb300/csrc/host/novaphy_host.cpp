@@ -707,7 +707,44 @@ FluidWorld::FluidWorld(const Model& model, const std::vector<FluidBlockDef>& blo
 }
 
 FluidWorld::~FluidWorld() {
+    for (auto& f : pinned_) pbf_host_free(f.p);
     if (scene_) pbf_scene_destroy(scene_);
+}
+
+const float* FluidWorld::fluid_pinned(int field) {
+    if (field < PBF_FIELD_POSITIONS || field > PBF_FIELD_LAMBDAS)
+        throw std::invalid_argument("unknown fluid field");
+    PinnedField& f = pinned_[field];
+    const bool vec = field == PBF_FIELD_POSITIONS || field == PBF_FIELD_VELOCITIES;
+    const size_t floats = (size_t)n_ * (vec ? 3 : 1);
+    if (floats == 0) return nullptr;
+    if (!f.p || f.floats != floats) {
+        pbf_host_free(f.p);
+        f.p = nullptr;
+        void* p = nullptr;
+        check_pbf(pbf_host_alloc(floats * sizeof(float), &p));
+        f.p = static_cast<float*>(p);
+        f.floats = floats;
+        f.stale = true;
+    }
+    if (f.stale && scene_) {
+        check_pbf(pbf_scene_read(scene_, field, f.p));
+    } else if (f.stale) {
+        // No device scene (no particles): nothing to read.
+        std::fill(f.p, f.p + floats, 0.0f);
+    }
+    f.stale = false;
+    return f.p;
+}
+
+void* FluidWorld::fluid_device_field(int field) {
+    if (field < PBF_FIELD_POSITIONS || field > PBF_FIELD_LAMBDAS)
+        throw std::invalid_argument("unknown fluid field");
+    if (!scene_ || n_ == 0) return nullptr;
+    void* p = nullptr;
+    check_pbf(pbf_scene_device_field(scene_, field, &p));
+    check_pbf(pbf_scene_sync(scene_));
+    return p;
 }
 
 ParticleState& FluidWorld::fluid_state() {
@@ -802,6 +839,7 @@ void FluidWorld::step(float dt) {
                 state_.torques[(size_t)k] = t[(size_t)k];
             }
             host_dirty_ = true;
+            for (auto& pf : pinned_) pf.stale = true;
         }
         {
             Scope r(monitor_, "fluid.rigid_step");

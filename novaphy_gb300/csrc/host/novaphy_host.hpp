@@ -522,8 +522,25 @@ public:
     int num_particles() const { return n_; }
     int num_boundary_particles() const { return (int)boundary_.size(); }
     const std::vector<BoundaryParticle>& boundary_particles() const { return boundary_; }
+    // Zero-copy state access (no counterpart in the reference, whose
+    // accessors copy).  fluid_pinned(field): the field (PBF_FIELD_*) read by
+    // one DMA into page-locked host memory that the world owns, 3n floats for
+    // positions and velocities, n for densities and lambdas; it is re-read
+    // only when a step ran since the last read of that field, and stays valid
+    // until the world is destroyed (later reads overwrite it).
+    // fluid_device_field(field): the device pointer of the field (float4 rows
+    // for positions and velocities, floats otherwise) once the scene's stream
+    // is idle; valid until the world is destroyed.
+    const float* fluid_pinned(int field);
+    void* fluid_device_field(int field);
 
 private:
+    struct PinnedField {
+        float* p = nullptr;
+        size_t floats = 0;
+        bool stale = true;
+    };
+    PinnedField pinned_[4];
     PBFSettings pbf_;
     std::vector<BoundaryParticle> boundary_;
     ParticleState host_;

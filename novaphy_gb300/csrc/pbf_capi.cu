@@ -937,6 +937,26 @@ int pbf_scene_stream(pbf_scene* s, void** stream) {
     return PBF_OK;
 }
 
+int pbf_host_alloc(size_t bytes, void** out) {
+    if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (bytes == 0) return PBF_OK;
+    void* p = nullptr;
+    const cudaError_t e = cudaHostAlloc(&p, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return fail(PBF_ERR_OOM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+    *out = p;
+    return PBF_OK;
+}
+
+int pbf_host_free(void* p) {
+    if (!p) return PBF_OK;
+    PBF_CUDA(cudaFreeHost(p));
+    return PBF_OK;
+}
+
 int pbf_solver_step_host(pbf_scene* s, int n, float* x3, float* v3, float* densities,
                          float* lambdas, float dt, const float* g3, float mass) {
     if (!s) return fail(PBF_ERR_INVALID_ARG, "scene is NULL");

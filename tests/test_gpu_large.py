@@ -61,9 +61,15 @@ def test_warps_straddle_cells(port_mt):
 def test_large_settings_variants(port_mt, kw):
     w = workloads.dam_break((64, 64, 65), 0.01, (4.0, 2.0, 2.0), dt=1.0 / 240.0, jitter=1e-5,
                             seed=7, vorticity=1e-4)
+    nsteps = 2
     if kw.get("hash_compat") == 0:
         # Away from the axes the reference's buckets are the plain 27 cells.
+        # One step only: the configured s_corr scatters the block over the
+        # whole box in the first step, and particles that reach the walls at
+        # the axes fall into merged buckets in the second.
         shift = np.array([0.5, 0.25, 0.25], np.float32)
         w.x = (w.x + shift).astype(np.float32)
-        assert port_mt.hash_collisions(w.x, np.float32(w.settings["kernel_radius"])) == 0
-    assert_equal(*run_both(port_mt, w, 2, **kw), kw)
+        xp = port_mt.predict(w.x, w.v, w.dt, w.gravity)[0]
+        assert port_mt.hash_collisions(xp, np.float32(w.settings["kernel_radius"])) == 0
+        nsteps = 1
+    assert_equal(*run_both(port_mt, w, nsteps, **kw), kw)
