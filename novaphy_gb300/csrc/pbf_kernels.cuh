@@ -432,34 +432,47 @@ __device__ __forceinline__ T ld_step(const T* p) {
 // [xmin - 1, xmax + 1], each in slot order, which is the reference's order
 // (cells in (dz, dy, dx) order, ascending particle index inside a cell).  A
 // lane's own sequence is that one restricted to the cells within one of its
-// own in x.  The warp walks it in chunks:
+// own in x.  The warp walks it in two phases:
 //
-//  1. each lane loads one candidate per round of 32 (coalesced); a candidate
-//     farther from the bounding box of the warp's positions than the kernel
-//     support adds an exact zero to every lane and is dropped, the rest are
-//     compacted into shared memory in order, up to CH per chunk;
-//  2. each lane tests the chunk's candidates in order and lists those in its
-//     support (and in its own 27 cells), one byte each;
-//  3. each lane evaluates its listed terms in order.
+//  1. listing, chunk by chunk: each lane loads one candidate per round of 32
+//     (coalesced); a candidate farther from the bounding box of the warp's
+//     positions than the kernel support adds an exact zero to every lane and
+//     is dropped, the rest are staged in shared memory in order, up to CH per
+//     chunk, and their positions appended to the warp's survivor list.  Each
+//     lane then tests the chunk's candidates in order and sets a bit in its
+//     own mask over the survivor list for each one in its support (and in its
+//     own 27 cells);
+//  2. evaluation, once the list holds up to CAP survivors or the walk ends:
+//     each lane evaluates the terms of its set bits in order, loading each
+//     candidate by its position.
 //
 // Every lane thus adds exactly the nonzero terms of the one-thread walk, in
 // the same order, so the sums are bit-identical.  The terms (two IEEE
 // divisions and a square root in the exact build) run with the lanes of a
 // step busy instead of waiting on the few in-support lanes of each
 // candidate, and the distance test runs on the surviving candidates only.
-// Only single scenes of at least kBigScene particles walk cooperatively (see
-// CoopBlock).
+// The list spans the whole walk rather than one chunk because the candidate
+// order is spatially coherent: a chunk covers a few rows, which lie in the
+// support of some lanes and not of others, so evaluating chunk by chunk
+// left about half the lanes of each term step idle (482 term steps per warp
+// for 242 terms per lane on the seeded 1M dam break, against 253 over the
+// whole walk).  Only single scenes of at least kBigScene particles walk
+// cooperatively (see CoopBlock).
 
-// Candidates staged per chunk: shared memory is CH * (49 or 65) bytes per
-// warp, under the 48 KB static limit for each block size.
-constexpr int coop_chunk(int bs) { return bs <= 64 ? 256 : bs <= 128 ? 128 : 64; }
+// Candidates staged per chunk, and survivors listed before an evaluation:
+// shared memory is CH * 17 + CAP * 8 bytes per warp (9.3 KB), six blocks of
+// four warps per SM.  The seeded 1M dam break lists about 700 survivors per
+// warp, so nearly every warp evaluates once, at the end of its walk.
+constexpr int coop_chunk(int) { return 64; }
+constexpr int kCoopCap = 1024;
 
 template <int CH, bool kExtra>
 struct CoopSmem {
-    float4 x[CH];                 // staged x* (w: lambda or unused)
-    float4 e[kExtra ? CH : 1];    // staged per-candidate extras of the pass
-    unsigned char list[CH * 32];  // list[t * 32 + lane]: t-th term of the lane
-    unsigned char c[CH];          // cell of the candidate among [xmin - 1, xmax + 1]
+    static constexpr int kCap = CH > 1 ? kCoopCap : 1;
+    float4 x[CH];                     // staged x* of the chunk (w: lambda or unused)
+    unsigned char c[CH];              // cell of the candidate among [xmin - 1, xmax + 1]
+    uint32_t q[kCap];                 // candidate position of each listed survivor
+    uint32_t mask[(kCap + 31) / 32][32];  // mask[w][lane] bit b: survivor 32 w + b is a term of the lane
 };
 
 // Shared memory of a kernel's warps: real for the kernels of a single large
@@ -508,13 +521,15 @@ __device__ __forceinline__ bool coop_row(bool active, const int4 cell, const Gri
 
 // The cooperative walk (see above) of a warp for which coop_row held.  xi is
 // the lane's x*, ci its cell x; `cut` the support test r_sq < cut of the
-// pass.  stage_e(q) returns the extras of candidate q (kExtra); body(xj, ej)
-// adds one in-support term.
-template <int CH, bool kExtra, bool kPersist, class StageE, class Body>
+// pass.  extra(q) returns the per-candidate extras of candidate q (kExtra);
+// body(xj, ej) adds one in-support term.
+template <int CH, bool kExtra, bool kPersist, class Extra, class Body>
 __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRow& R, int ci,
                                           const float4 xi, const float4* xin, float cut,
                                           const GridDesc& Gd, const uint32_t* __restrict__ off,
-                                          StageE&& stage_e, Body&& body) {
+                                          Extra&& extra, Body&& body) {
+    constexpr int CAP = CoopSmem<CH, kExtra>::kCap;
+    static_assert(CH % 32 == 0 && CAP % 32 == 0 && CAP >= 2 * CH, "coop walk sizes");
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     float lx = xi.x, ly = xi.y, lz = xi.z, hx = xi.x, hy = xi.y, hz = xi.z;
@@ -533,43 +548,60 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
     const bool all_member = R.W == 3;  // one cell: every staged candidate is in it
     const int myc = ci - R.xmin + 1;   // the lane's cell among the row's cells
     const uint32_t lt = lanemask_lt();
-    int nst = 0;
+    int nst = 0;   // staged in the current chunk
+    int base = 0;  // survivors listed so far (a multiple of 32)
+    int cnt = 0;   // the lane's listed terms
 
-    auto process = [&]() {
-        __syncwarp();
-        int cnt = 0;
-        if (all_member) {
-#pragma unroll 4
-            for (int k = 0; k < nst; ++k) {
-                const float4 xj = sm.x[k];
-                float rx, ry, rz;
-                if (rel_sq(xi, xj, rx, ry, rz) < cut) {
-                    sm.list[cnt * 32 + lane] = (unsigned char)k;
-                    ++cnt;
-                }
-            }
-        } else {
-#pragma unroll 4
-            for (int k = 0; k < nst; ++k) {
-                const float4 xj = sm.x[k];
-                float rx, ry, rz;
-                const bool in = rel_sq(xi, xj, rx, ry, rz) < cut;
-                if (in && (unsigned)((int)sm.c[k] - myc + 1) <= 2u) {
-                    sm.list[cnt * 32 + lane] = (unsigned char)k;
-                    ++cnt;
-                }
-            }
-        }
-        const int most = __reduce_max_sync(full, (unsigned)cnt);
+    // Phase 2: every lane evaluates its listed terms in list order.
+    auto evaluate = [&]() {
+        const int most = (int)__reduce_max_sync(full, (unsigned)cnt);
+        int w = 0;
+        uint32_t bits = sm.mask[0][lane];
         for (int t = 0; t < most; ++t) {
             if (t < cnt) {
-                const int k = sm.list[t * 32 + lane];
-                if constexpr (kExtra) body(sm.x[k], sm.e[k]);
-                else body(sm.x[k], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+                while (bits == 0) bits = sm.mask[++w][lane];
+                const int k = 32 * w + __ffs(bits) - 1;
+                bits &= bits - 1u;
+                const uint32_t q = sm.q[k];
+                if constexpr (kExtra) body(ld_step<kPersist>(xin + q), extra(q));
+                else body(ld_step<kPersist>(xin + q), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
             }
         }
         __syncwarp();
+        cnt = 0;
+        base = 0;
+    };
+
+    // Phase 1b: the lane's support tests over the staged chunk, one mask word
+    // per 32 candidates.
+    auto test_chunk = [&]() {
+        __syncwarp();
+        const int words = (nst + 31) >> 5;
+        for (int wd = 0; wd < words; ++wd) {
+            const int k0 = wd << 5;
+            const int kn = min(32, nst - k0);
+            uint32_t bits = 0u;
+            if (all_member) {
+#pragma unroll 4
+                for (int b = 0; b < kn; ++b) {
+                    float rx, ry, rz;
+                    if (rel_sq(xi, sm.x[k0 + b], rx, ry, rz) < cut) bits |= 1u << b;
+                }
+            } else {
+#pragma unroll 4
+                for (int b = 0; b < kn; ++b) {
+                    float rx, ry, rz;
+                    const bool in = rel_sq(xi, sm.x[k0 + b], rx, ry, rz) < cut;
+                    if (in && (unsigned)((int)sm.c[k0 + b] - myc + 1) <= 2u) bits |= 1u << b;
+                }
+            }
+            sm.mask[(base >> 5) + wd][lane] = bits;
+            cnt += __popc(bits);
+        }
+        base += words << 5;
         nst = 0;
+        __syncwarp();
+        if (base > CAP - CH) evaluate();
     };
 
     for (int rr = 0; rr < 9; ++rr) {
@@ -603,14 +635,15 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
             if (pass) {
                 const int k = nst + __popc(m & lt);
                 sm.x[k] = xj;
-                if constexpr (kExtra) sm.e[k] = stage_e(q);
+                sm.q[base + k] = q;
                 sm.c[k] = (unsigned char)((q >= b1) + (q >= b2) + (q >= b3) + (q >= b4));
             }
             nst += __popc(m);
-            if (nst > CH - 32) process();
+            if (nst > CH - 32) test_chunk();
         }
     }
-    if (nst > 0) process();
+    if (nst > 0) test_chunk();
+    if (base > 0) evaluate();
 }
 
 // Scene of sorted particle p (0 for a single scene).
