@@ -424,7 +424,8 @@ int pbf_server_submit(pbf_server* server, long long scene_id, float dt, int nste
 int pbf_server_wait(pbf_server* server, long long request_id, double timeout_s, int* state_out);
 /* A rigid body of a served coupled scene: the state World's semi-implicit
  * Euler integrates (src/dynamics/integrator.cpp), which the server runs on
- * the device for free bodies (served scenes model no rigid contacts).
+ * the device, for free bodies or, with contact shapes
+ * (pbf_server_open_coupled_scene_contacts), through World's contact pipeline.
  * inv_mass 0 marks a static body; inv_inertia is RigidBody::inv_inertia,
  * row-major. */
 typedef struct pbf_rigid_body {
@@ -435,6 +436,30 @@ typedef struct pbf_rigid_body {
     float inv_mass;
     float inv_inertia[9];
 } pbf_rigid_body;
+
+/* A collision shape of a served coupled scene's rigid contacts
+ * (CollisionShape, include/novaphy/collision/shape.h: make_sphere,
+ * make_plane, ModelBuilder::add_ground_plane).  Spheres and planes. */
+#define PBF_SHAPE_SPHERE 0
+#define PBF_SHAPE_PLANE 1
+typedef struct pbf_rigid_shape {
+    int type;           /* PBF_SHAPE_* */
+    int body;           /* sphere: its body (-1: fixed in the world); plane: -1 */
+    float radius;       /* sphere */
+    float local_pos[3]; /* sphere: centre in the body frame (local_transform.position) */
+    float normal[3];    /* plane: unit normal (make_plane normalises it) */
+    float offset;       /* plane: normal . x = offset */
+    float friction;
+    float restitution;
+} pbf_rigid_shape;
+
+/* The contact solve's SolverSettings (include/novaphy/sim/world.h). */
+typedef struct pbf_contact_settings {
+    int velocity_iterations; /* 30 */
+    float baumgarte;         /* 0.3 */
+    float slop;              /* 0.005 */
+    int warm_starting;       /* 1 */
+} pbf_contact_settings;
 
 /* Opens a coupled scene: the fluid of pbf_server_open_scene plus nb Akinci
  * boundary particles (pbf_scene_set_boundary layout; psi from
@@ -451,6 +476,22 @@ int pbf_server_open_coupled_scene(pbf_server* server, const pbf_settings* settin
                                   const int* body, const float* psi, int nbodies,
                                   const pbf_rigid_body* bodies, long long* scene_id,
                                   int* state_out);
+
+/* pbf_server_open_coupled_scene whose bodies also collide: after each step's
+ * coupling the server runs World's rigid pipeline on the device
+ * (src/sim/world.cpp:30-182 with sleep off: symplectic Euler, shape boxes,
+ * broad phase, sphere-sphere and sphere-plane contacts, the warm-started
+ * sequential-impulse solve of src/dynamics/free_body_solver.cpp, position
+ * update) with the float operations of the host World, so the bodies follow
+ * FluidWorld::step bit for bit.  Up to 16 shapes and 16 bodies; a shape
+ * other than a sphere or a plane, or one naming a missing body, is
+ * PBF_ERR_INVALID_ARG. */
+int pbf_server_open_coupled_scene_contacts(
+    pbf_server* server, const pbf_settings* settings, int n, const float* x3, const float* v3,
+    float mass, const float* gravity3, int nb, const float* local3, const int* body,
+    const float* psi, int nbodies, const pbf_rigid_body* bodies, int nshapes,
+    const pbf_rigid_shape* shapes, const pbf_contact_settings* contact_settings,
+    long long* scene_id, int* state_out);
 
 /* The bodies of a coupled scene after its completed steps (waits until the
  * scene has no pending request). */

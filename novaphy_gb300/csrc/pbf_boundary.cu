@@ -6,6 +6,7 @@
 #include "pbf_boundary.cuh"
 #include "pbf_kernels.cuh"
 #include "rigid_step.hpp"
+#include "rigid_world.cuh"
 
 namespace pbf {
 namespace bnd {
@@ -247,6 +248,30 @@ __global__ void k_rigid_step(pbf_rigid_body* __restrict__ bodies, int nbodies,
     }
 }
 
+// World's rigid pipeline for one scene's bodies and shapes (rigid_world.cuh),
+// in shared memory by one thread; then the new poses of the first nforce
+// bodies into body_pos/body_quat, as k_rigid_step.
+__global__ void __launch_bounds__(32)
+k_rigid_world(pbf_rigid_body* __restrict__ bodies, int nbodies,
+              const pbf_rigid_shape* __restrict__ shapes, int nshapes, pbf_contact_settings set,
+              const float* __restrict__ force3, const float* __restrict__ torque3, int nforce,
+              float gx, float gy, float gz, float dt, float4* __restrict__ body_pos,
+              float4* __restrict__ body_quat) {
+    __shared__ rw::World W;
+    __shared__ pbf_rigid_body B[rw::kMaxShapes];
+    __shared__ pbf_rigid_shape S[rw::kMaxShapes];
+    if (threadIdx.x != 0 || nbodies > rw::kMaxShapes || nshapes > rw::kMaxShapes) return;
+    for (int k = 0; k < nbodies; ++k) B[k] = bodies[k];
+    for (int k = 0; k < nshapes; ++k) S[k] = shapes[k];
+    const float g[3] = {gx, gy, gz};
+    if (rw::world_step(W, B, nbodies, S, nshapes, set, force3, torque3, nforce, g, dt)) return;
+    for (int k = 0; k < nbodies; ++k) bodies[k] = B[k];
+    for (int k = 0; k < nforce && k < nbodies; ++k) {
+        body_pos[k] = make_float4(B[k].pos[0], B[k].pos[1], B[k].pos[2], 0.0f);
+        body_quat[k] = make_float4(B[k].quat[0], B[k].quat[1], B[k].quat[2], B[k].quat[3]);
+    }
+}
+
 __global__ void __launch_bounds__(kBlock)
 k_volumes(const float4* __restrict__ world, int nb, const QuerySet Q, const PointIndex I,
           float* __restrict__ psi, const StepConsts C) {
@@ -342,6 +367,17 @@ cudaError_t body_reduce(const float4* Fb, const float4* bworld, const int* list_
     else
         k_body_reduce<<<grid_of(nbodies, 32), 32, 0, st>>>(Fb, bworld, list_off, list, body_pos,
                                                            nbodies, force3, torque3);
+    return cudaGetLastError();
+}
+
+cudaError_t rigid_world(pbf_rigid_body* bodies, int nbodies, const pbf_rigid_shape* shapes,
+                        int nshapes, const pbf_contact_settings& set, const float* force3,
+                        const float* torque3, int nforce, float gx, float gy, float gz, float dt,
+                        float4* body_pos, float4* body_quat, cudaStream_t st) {
+    using namespace bnd;
+    if (nbodies <= 0) return cudaSuccess;
+    k_rigid_world<<<1, 32, 0, st>>>(bodies, nbodies, shapes, nshapes, set, force3, torque3, nforce,
+                                    gx, gy, gz, dt, body_pos, body_quat);
     return cudaGetLastError();
 }
 

@@ -85,6 +85,14 @@ cudaError_t rigid_step(pbf_rigid_body* bodies, int nbodies, const float* force3,
                        const float* torque3, int nforce, float gx, float gy, float gz, float dt,
                        float4* body_pos, float4* body_quat, cudaStream_t st);
 
+// World's rigid pipeline with sphere and plane contacts (rigid_world.cuh)
+// for one scene's bodies, in place of rigid_step; the same outputs.
+// Shapes must have been validated (types, bodies, at most 16 of each).
+cudaError_t rigid_world(pbf_rigid_body* bodies, int nbodies, const pbf_rigid_shape* shapes,
+                        int nshapes, const pbf_contact_settings& set, const float* force3,
+                        const float* torque3, int nforce, float gx, float gy, float gz, float dt,
+                        float4* body_pos, float4* body_quat, cudaStream_t st);
+
 // psi_b = 1 / sum_b' poly6 (0 when the sum <= 1e-10), boundary.cpp:152-176.
 cudaError_t boundary_volumes(const float4* world, int nb, const QuerySet& Q, const PointIndex& I,
                              float* psi, const StepConsts& C, cudaStream_t st);

@@ -622,7 +622,7 @@ int pbf_scene_destroy(pbf_scene* s) {
         DeviceGuard dg(s->device);
         if (s->stream) cudaStreamSynchronize(s->stream);
         for (void* m : {s->bnd.mem, s->bnd.body_mem, s->bnd.sort_mem, s->bnd.fq_mem,
-                        static_cast<void*>(s->bnd.rb)})
+                        static_cast<void*>(s->bnd.rb), static_cast<void*>(s->bnd.shapes)})
             if (m) cudaFree(m);
         if (s->bnd.idx.off) cudaFree(s->bnd.idx.off);
         if (s->couple_graph) cudaGraphExecDestroy(s->couple_graph);
@@ -1427,6 +1427,42 @@ int scene_set_rigid(pbf_scene* s, int nbodies, const pbf_rigid_body* bodies) {
     return PBF_OK;
 }
 
+int scene_set_contacts(pbf_scene* s, int nshapes, const pbf_rigid_shape* shapes,
+                       const pbf_contact_settings* cs) {
+    if (!s || nshapes < 0 || (nshapes > 0 && !shapes))
+        return fail(PBF_ERR_INVALID_ARG, "bad shape arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    if (nshapes > 16 || b.nrb > 16)
+        return fail(PBF_ERR_INVALID_ARG, "rigid contacts take at most 16 shapes and 16 bodies");
+    for (int k = 0; k < nshapes; ++k) {
+        const pbf_rigid_shape& sh = shapes[k];
+        if (sh.type == PBF_SHAPE_SPHERE) {
+            if (sh.body >= b.nrb || sh.body < -1)
+                return fail(PBF_ERR_INVALID_ARG, "a contact shape names a missing body");
+        } else if (sh.type == PBF_SHAPE_PLANE) {
+            if (sh.body != -1) return fail(PBF_ERR_INVALID_ARG, "a plane belongs to the world");
+        } else {
+            return fail(PBF_ERR_INVALID_ARG, "contact shapes are spheres and planes");
+        }
+    }
+    if (cs && cs->velocity_iterations < 0)
+        return fail(PBF_ERR_INVALID_ARG, "velocity_iterations must be >= 0");
+    ++s->buf_gen;
+    if (b.shapes) cudaFree(b.shapes);
+    b.shapes = nullptr;
+    b.nshapes = 0;
+    if (cs) b.cset = *cs;
+    if (nshapes == 0) return PBF_OK;
+    PBF_CUDA(cudaMalloc(&b.shapes, (size_t)nshapes * sizeof(pbf_rigid_shape)));
+    PBF_CUDA(cudaMemcpyAsync(b.shapes, shapes, (size_t)nshapes * sizeof(pbf_rigid_shape),
+                             cudaMemcpyHostToDevice, s->stream));
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
+    b.nshapes = nshapes;
+    return PBF_OK;
+}
+
 int scene_read_rigid(pbf_scene* s, pbf_rigid_body* out) {
     std::lock_guard<std::mutex> lk(s->mu);
     DeviceGuard dg(s->device);
@@ -1474,6 +1510,12 @@ int scene_couple_rigid_locked(pbf_scene* s, float dt, const float g[3]) {
             if (rc) return rc;
         }
         const int nforce = couple ? b.nbodies : 0;
+        if (b.nshapes > 0) {
+            const cudaError_t e = rigid_world(b.rb, b.nrb, b.shapes, b.nshapes, b.cset, b.force3,
+                                              b.torque3, nforce, g[0], g[1], g[2], dt, b.body_pos,
+                                              b.body_quat, s->stream);
+            return e == cudaSuccess ? PBF_OK : cuda_fail(e, "rigid contacts");
+        }
         const cudaError_t e = rigid_step(b.rb, b.nrb, b.force3, b.torque3, nforce, g[0], g[1], g[2],
                                          dt, b.body_pos, b.body_quat, s->stream);
         return e == cudaSuccess ? PBF_OK : cuda_fail(e, "rigid step");

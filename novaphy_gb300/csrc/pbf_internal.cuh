@@ -165,6 +165,10 @@ struct pbf_scene {
         // (served coupled scenes), else null.
         pbf_rigid_body* rb = nullptr;
         int nrb = 0;
+        // Contact shapes of those bodies (device copy), when they collide.
+        pbf_rigid_shape* shapes = nullptr;
+        int nshapes = 0;
+        pbf_contact_settings cset{30, 0.3f, 0.005f, 1};
     } bnd;
 };
 
@@ -197,6 +201,10 @@ size_t scene_device_bytes(const pbf_scene* s);
 uint32_t grid_slots_for(const pbf_settings& st, const float* x3, int n);
 // Device copy of the scene's rigid bodies, which then step on the device.
 int scene_set_rigid(pbf_scene* s, int nbodies, const pbf_rigid_body* bodies);
+// Contact shapes of the device rigid bodies: with nshapes > 0 the rigid step
+// runs World's contact pipeline (rigid_world.cuh).  Validates the shapes.
+int scene_set_contacts(pbf_scene* s, int nshapes, const pbf_rigid_shape* shapes,
+                       const pbf_contact_settings* cs);
 // The device copy of the rigid bodies, after the scene's queued work.
 int scene_read_rigid(pbf_scene* s, pbf_rigid_body* out);
 // FluidWorld's post-step on the scene's stream, without waiting: the coupling

@@ -437,14 +437,18 @@ __device__ __forceinline__ T ld_step(const T* p) {
 //  1. listing, chunk by chunk: each lane loads one candidate per round of 32
 //     (coalesced); a candidate farther from the bounding box of the warp's
 //     positions than the kernel support adds an exact zero to every lane and
-//     is dropped, the rest are staged in shared memory in order, up to CH per
-//     chunk, and their positions appended to the warp's survivor list.  Each
-//     lane then tests the chunk's candidates in order and sets a bit in its
-//     own mask over the survivor list for each one in its support (and in its
-//     own 27 cells);
+//     is dropped, the rest are staged in shared memory in order (x, y and z
+//     in separate arrays), up to CH per chunk, and their positions appended
+//     to the warp's survivor list.  Each lane then tests the chunk's
+//     candidates two at a time (paired f32x2 operations) and sets a bit in
+//     its own mask over the survivor list for each one that may be in its
+//     support and lies in its own 27 cells.  The test is conservative: it
+//     fuses the squares and sums (a few ulps from the exact r^2) and compares
+//     against the support radius widened by 1e-6, so it keeps every
+//     in-support candidate, and every term re-tests the exact r^2 itself;
 //  2. evaluation, once the list holds up to CAP survivors or the walk ends:
 //     each lane evaluates the terms of its set bits in order, loading each
-//     candidate by its position.
+//     candidate by its position one term ahead.
 //
 // Every lane thus adds exactly the nonzero terms of the one-thread walk, in
 // the same order, so the sums are bit-identical.  The terms (two IEEE
@@ -454,24 +458,23 @@ __device__ __forceinline__ T ld_step(const T* p) {
 // The list spans the whole walk rather than one chunk because the candidate
 // order is spatially coherent: a chunk covers a few rows, which lie in the
 // support of some lanes and not of others, so evaluating chunk by chunk
-// left about half the lanes of each term step idle (482 term steps per warp
-// for 242 terms per lane on the seeded 1M dam break, against 253 over the
-// whole walk).  Only single scenes of at least kBigScene particles walk
-// cooperatively (see CoopBlock).
+// leaves many lanes of each term step idle.  Only single scenes of at least
+// kBigScene particles walk cooperatively (see CoopBlock).
 
 // Candidates staged per chunk, and survivors listed before an evaluation:
-// shared memory is CH * 17 + CAP * 8 bytes per warp (9.3 KB), six blocks of
-// four warps per SM.  The seeded 1M dam break lists about 700 survivors per
-// warp, so nearly every warp evaluates once, at the end of its walk.
+// shared memory is CH * 13 + CAP * 8 bytes per warp (6.8 KB), eight blocks
+// of four warps per SM.
 constexpr int coop_chunk(int) { return 64; }
-constexpr int kCoopCap = 1024;
+constexpr int kCoopCap = 768;
 
 template <int CH, bool kExtra>
 struct CoopSmem {
     static constexpr int kCap = CH > 1 ? kCoopCap : 1;
-    float4 x[CH];                     // staged x* of the chunk (w: lambda or unused)
-    unsigned char c[CH];              // cell of the candidate among [xmin - 1, xmax + 1]
-    uint32_t q[kCap];                 // candidate position of each listed survivor
+    alignas(16) float sx[CH];          // staged x* of the chunk, by component; slots past
+    alignas(16) float sy[CH];          // the last staged one up to a multiple of 32
+    alignas(16) float sz[CH];          // hold +inf (never in support)
+    unsigned char c[CH];               // cell of the candidate among [xmin - 1, xmax + 1]
+    uint32_t q[kCap];                  // candidate position of each listed survivor
     uint32_t mask[(kCap + 31) / 32][32];  // mask[w][lane] bit b: survivor 32 w + b is a term of the lane
 };
 
@@ -522,7 +525,7 @@ __device__ __forceinline__ bool coop_row(bool active, const int4 cell, const Gri
 // The cooperative walk (see above) of a warp for which coop_row held.  xi is
 // the lane's x*, ci its cell x; `cut` the support test r_sq < cut of the
 // pass.  extra(q) returns the per-candidate extras of candidate q (kExtra);
-// body(xj, ej) adds one in-support term.
+// body(xj, ej) adds the term of one candidate, re-testing r_sq < cut.
 template <int CH, bool kExtra, bool kPersist, class Extra, class Body>
 __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRow& R, int ci,
                                           const float4 xi, const float4* xin, float cut,
@@ -542,59 +545,95 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
         hy = fmaxf(hy, __shfl_xor_sync(full, hy, o));
         hz = fmaxf(hz, __shfl_xor_sync(full, hz, o));
     }
-    // A candidate in some lane's support is within sqrt(cut) of the box; the
-    // margin covers the rounding of both distance computations.
+    // A candidate in some lane's support is within sqrt(cut) of the box, and
+    // within the widened radius of the lane's fused r^2; the margins cover
+    // the rounding of both distance computations.
     const float lim = cut * 1.001f;
+    const float lim2 = cut * 1.000001f;
     const bool all_member = R.W == 3;  // one cell: every staged candidate is in it
     const int myc = ci - R.xmin + 1;   // the lane's cell among the row's cells
     const uint32_t lt = lanemask_lt();
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 px = make_float2(xi.x, xi.x), py = make_float2(xi.y, xi.y),
+                 pz = make_float2(xi.z, xi.z);
     int nst = 0;   // staged in the current chunk
     int base = 0;  // survivors listed so far (a multiple of 32)
     int cnt = 0;   // the lane's listed terms
 
-    // Phase 2: every lane evaluates its listed terms in list order.
+    // Phase 2: every lane evaluates its listed terms in list order, loading
+    // the next term's candidate before adding the current one.
     auto evaluate = [&]() {
         const int most = (int)__reduce_max_sync(full, (unsigned)cnt);
         int w = 0;
         uint32_t bits = sm.mask[0][lane];
+        auto next_q = [&]() {
+            while (bits == 0) bits = sm.mask[++w][lane];
+            const int k = 32 * w + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            return sm.q[k];
+        };
+        float4 xn = make_float4(0.0f, 0.0f, 0.0f, 0.0f), en = xn;
+        if (cnt > 0) {
+            const uint32_t q = next_q();
+            xn = ld_step<kPersist>(xin + q);
+            if constexpr (kExtra) en = extra(q);
+        }
         for (int t = 0; t < most; ++t) {
-            if (t < cnt) {
-                while (bits == 0) bits = sm.mask[++w][lane];
-                const int k = 32 * w + __ffs(bits) - 1;
-                bits &= bits - 1u;
-                const uint32_t q = sm.q[k];
-                if constexpr (kExtra) body(ld_step<kPersist>(xin + q), extra(q));
-                else body(ld_step<kPersist>(xin + q), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+            const float4 xj = xn, ej = en;
+            if (t + 1 < cnt) {
+                const uint32_t q = next_q();
+                xn = ld_step<kPersist>(xin + q);
+                if constexpr (kExtra) en = extra(q);
             }
+            if (t < cnt) body(xj, ej);
         }
         __syncwarp();
         cnt = 0;
         base = 0;
     };
 
-    // Phase 1b: the lane's support tests over the staged chunk, one mask word
-    // per 32 candidates.
+    // Phase 1b: the lane's support tests over the staged chunk, two
+    // candidates per paired operation, one mask word per 32 candidates.
     auto test_chunk = [&]() {
-        __syncwarp();
         const int words = (nst + 31) >> 5;
+        // Pad the last word with candidates that are never in support.
+        for (int k = nst + lane; k < (words << 5); k += 32) {
+            sm.sx[k] = __int_as_float(0x7f800000);
+            sm.sy[k] = 0.0f;
+            sm.sz[k] = 0.0f;
+            sm.c[k] = 0;
+        }
+        __syncwarp();
         for (int wd = 0; wd < words; ++wd) {
             const int k0 = wd << 5;
-            const int kn = min(32, nst - k0);
-            uint32_t bits = 0u;
-            if (all_member) {
-#pragma unroll 4
-                for (int b = 0; b < kn; ++b) {
-                    float rx, ry, rz;
-                    if (rel_sq(xi, sm.x[k0 + b], rx, ry, rz) < cut) bits |= 1u << b;
-                }
-            } else {
-#pragma unroll 4
-                for (int b = 0; b < kn; ++b) {
-                    float rx, ry, rz;
-                    const bool in = rel_sq(xi, sm.x[k0 + b], rx, ry, rz) < cut;
-                    if (in && (unsigned)((int)sm.c[k0 + b] - myc + 1) <= 2u) bits |= 1u << b;
+            uint32_t allowed = full;
+            if (!all_member) {
+                // Candidates of the word in each of the row's cells (at most
+                // 5), then those in the lane's three.
+                const int cc = sm.c[k0 + lane];
+                allowed = 0u;
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const uint32_t mc = __ballot_sync(full, cc == v);
+                    if ((unsigned)(v - myc + 1) <= 2u) allowed |= mc;
                 }
             }
+            uint32_t bits = 0u;
+#pragma unroll
+            for (int b = 0; b < 32; b += 2) {
+                const float2 X = *reinterpret_cast<const float2*>(&sm.sx[k0 + b]);
+                const float2 Y = *reinterpret_cast<const float2*>(&sm.sy[k0 + b]);
+                const float2 Z = *reinterpret_cast<const float2*>(&sm.sz[k0 + b]);
+                const float2 dx = __ffma2_rn(X, m1, px);
+                const float2 dy = __ffma2_rn(Y, m1, py);
+                const float2 dz = __ffma2_rn(Z, m1, pz);
+                float2 r2 = __fmul2_rn(dx, dx);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dz, dz, r2);
+                if (r2.x < lim2) bits |= 1u << b;
+                if (r2.y < lim2) bits |= 2u << b;
+            }
+            bits &= allowed;
             sm.mask[(base >> 5) + wd][lane] = bits;
             cnt += __popc(bits);
         }
@@ -634,15 +673,23 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
             const uint32_t m = __ballot_sync(full, pass);
             if (pass) {
                 const int k = nst + __popc(m & lt);
-                sm.x[k] = xj;
+                sm.sx[k] = xj.x;
+                sm.sy[k] = xj.y;
+                sm.sz[k] = xj.z;
                 sm.q[base + k] = q;
                 sm.c[k] = (unsigned char)((q >= b1) + (q >= b2) + (q >= b3) + (q >= b4));
             }
             nst += __popc(m);
-            if (nst > CH - 32) test_chunk();
+            if (nst > CH - 32) {
+                __syncwarp();
+                test_chunk();
+            }
         }
     }
-    if (nst > 0) test_chunk();
+    if (nst > 0) {
+        __syncwarp();
+        test_chunk();
+    }
     if (base > 0) evaluate();
 }
 

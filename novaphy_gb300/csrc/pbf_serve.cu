@@ -87,6 +87,8 @@ struct SceneRec {
     std::vector<float> local, psi;  // until the device copy is made
     std::vector<int> body;
     std::vector<pbf_rigid_body> bodies;  // until the device copy is made
+    std::vector<pbf_rigid_shape> shapes; // contact shapes of the bodies (none: free bodies)
+    pbf_contact_settings cset{30, 0.3f, 0.005f, 1};
 };
 
 struct ReqRec {
@@ -559,6 +561,8 @@ int materialize(pbf_server* sv, SceneRec& rec) {
             rc = pbf_scene_set_bodies(s, nbodies, pos.data(), quat.data(), dyn.data());
         }
         if (!rc) rc = scene_set_rigid(s, nbodies, rec.bodies.data());
+        if (!rc && !rec.shapes.empty())
+            rc = scene_set_contacts(s, (int)rec.shapes.size(), rec.shapes.data(), &rec.cset);
         if (rc) {
             pbf_scene_destroy(s);
             return rc;
@@ -720,6 +724,9 @@ struct CoupledArgs {
     const float* psi = nullptr;
     int nbodies = 0;
     const pbf_rigid_body* bodies = nullptr;
+    int nshapes = 0;
+    const pbf_rigid_shape* shapes = nullptr;
+    const pbf_contact_settings* cset = nullptr;
 };
 
 int open_impl(pbf_server* sv, const pbf_settings* st, int n, const float* x3, const float* v3,
@@ -740,6 +747,20 @@ int open_impl(pbf_server* sv, const pbf_settings* st, int n, const float* x3, co
         for (int i = 0; i < cp->nb; ++i)
             if (cp->body[i] >= cp->nbodies)
                 return fail(PBF_ERR_INVALID_ARG, "a boundary particle names a missing body");
+        if (cp->nshapes < 0 || (cp->nshapes > 0 && !cp->shapes))
+            return fail(PBF_ERR_INVALID_ARG, "bad contact shapes");
+        if (cp->nshapes > 16 || (cp->nshapes > 0 && cp->nbodies > 16))
+            return fail(PBF_ERR_INVALID_ARG, "rigid contacts take at most 16 shapes and 16 bodies");
+        for (int k = 0; k < cp->nshapes; ++k) {
+            const pbf_rigid_shape& sh = cp->shapes[k];
+            const bool sphere = sh.type == PBF_SHAPE_SPHERE && sh.body >= -1 && sh.body < cp->nbodies;
+            const bool plane = sh.type == PBF_SHAPE_PLANE && sh.body == -1;
+            if (!sphere && !plane)
+                return fail(PBF_ERR_INVALID_ARG,
+                            "contact shapes are spheres on existing bodies and world planes");
+        }
+        if (cp->cset && cp->cset->velocity_iterations < 0)
+            return fail(PBF_ERR_INVALID_ARG, "velocity_iterations must be >= 0");
         // The coupling runs on the scene's own step scratch and offsets.
         charge += work_bytes(n > 0 ? n : 1) + sort_scratch_bytes(n > 0 ? n : 1) +
                   (size_t)slots * kGridBytesPerSlot + (size_t)cp->nb * kBoundaryBytes;
@@ -769,6 +790,8 @@ int open_impl(pbf_server* sv, const pbf_settings* st, int n, const float* x3, co
         rec.body.assign(cp->body, cp->body + cp->nb);
         rec.psi.assign(cp->psi, cp->psi + cp->nb);
         rec.bodies.assign(cp->bodies, cp->bodies + cp->nbodies);
+        if (cp->nshapes > 0) rec.shapes.assign(cp->shapes, cp->shapes + cp->nshapes);
+        if (cp->cset) rec.cset = *cp->cset;
     }
     sv->admit_queue.push_back(id);
     admit_waiting(sv, lk);
@@ -801,6 +824,24 @@ int pbf_server_open_coupled_scene(pbf_server* sv, const pbf_settings* st, int n,
     cp.psi = psi;
     cp.nbodies = nbodies;
     cp.bodies = bodies;
+    return open_impl(sv, st, n, x3, v3, mass, g3, &cp, id_out, state_out);
+}
+
+int pbf_server_open_coupled_scene_contacts(
+    pbf_server* sv, const pbf_settings* st, int n, const float* x3, const float* v3, float mass,
+    const float* g3, int nb, const float* local3, const int* body, const float* psi, int nbodies,
+    const pbf_rigid_body* bodies, int nshapes, const pbf_rigid_shape* shapes,
+    const pbf_contact_settings* cset, long long* id_out, int* state_out) {
+    CoupledArgs cp;
+    cp.nb = nb;
+    cp.local3 = local3;
+    cp.body = body;
+    cp.psi = psi;
+    cp.nbodies = nbodies;
+    cp.bodies = bodies;
+    cp.nshapes = nshapes;
+    cp.shapes = shapes;
+    cp.cset = cset;
     return open_impl(sv, st, n, x3, v3, mass, g3, &cp, id_out, state_out);
 }
 
