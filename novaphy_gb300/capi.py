@@ -147,6 +147,11 @@ def load() -> C.CDLL:
         "pbf_server_open_coupled_scene": ([vp, vp, C.c_int, vp, vp, C.c_float, vp, C.c_int, vp, vp,
                                            vp, C.c_int, vp, vp, vp], C.c_int),
         "pbf_server_read_bodies": ([vp, C.c_longlong, vp], C.c_int),
+        "pbf_server_open_coupled_scene_contacts": (
+            [vp, vp, C.c_int, vp, vp, C.c_float, vp, C.c_int, vp, vp, vp, C.c_int, vp, C.c_int, vp,
+             vp, vp, vp], C.c_int),
+        "pbf_host_alloc": ([C.c_size_t, C.POINTER(vp)], C.c_int),
+        "pbf_host_free": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -524,6 +529,40 @@ class RigidBody(C.Structure):
     ]
 
 
+SHAPE_SPHERE = 0
+SHAPE_PLANE = 1
+
+
+class RigidShape(C.Structure):
+    """pbf_rigid_shape: a sphere on a body or a world plane of a served scene's contacts."""
+
+    _fields_ = [
+        ("type", C.c_int),
+        ("body", C.c_int),
+        ("radius", C.c_float),
+        ("local_pos", C.c_float * 3),
+        ("normal", C.c_float * 3),
+        ("offset", C.c_float),
+        ("friction", C.c_float),
+        ("restitution", C.c_float),
+    ]
+
+
+class ContactSettings(C.Structure):
+    """pbf_contact_settings: the contact solve's SolverSettings."""
+
+    _fields_ = [
+        ("velocity_iterations", C.c_int),
+        ("baumgarte", C.c_float),
+        ("slop", C.c_float),
+        ("warm_starting", C.c_int),
+    ]
+
+    @classmethod
+    def make(cls, velocity_iterations=30, baumgarte=0.3, slop=0.005, warm_starting=True):
+        return cls(velocity_iterations, baumgarte, slop, 1 if warm_starting else 0)
+
+
 class ServerConfig(C.Structure):
     """pbf_server_config."""
 
@@ -602,9 +641,12 @@ class Server:
         return sid.value, st.value
 
     def open_coupled_scene(self, settings: Settings, x, v, mass, gravity, local, body, psi,
-                           bodies):
+                           bodies, shapes=None, contact_settings=None):
         """A FluidWorld-like scene: boundary particles (local, body, psi) owned by
-        `bodies` (a sequence of RigidBody) that the server advances after each step."""
+        `bodies` (a sequence of RigidBody) that the server advances after each step:
+        as free bodies, or, with `shapes` (a sequence of RigidShape, spheres and
+        planes), through World's contact pipeline with `contact_settings`
+        (ContactSettings, default SolverSettings())."""
         x = _f32(x, (-1, 3))
         vv = _f32(v, x.shape) if v is not None else None
         g = _f32(gravity, (3,))
@@ -613,6 +655,15 @@ class Server:
         psi = _f32(psi)
         arr = (RigidBody * max(len(bodies), 1))(*bodies)
         sid, st = C.c_longlong(0), C.c_int(0)
+        if shapes:
+            sarr = (RigidShape * len(shapes))(*shapes)
+            cs = contact_settings if contact_settings is not None else ContactSettings.make()
+            check(self._L.pbf_server_open_coupled_scene_contacts(
+                self._h, C.byref(settings), len(x), _ptr(x),
+                _ptr(vv) if vv is not None else None, mass, _ptr(g), len(local), _ptr(local),
+                _ptr(body), _ptr(psi), len(bodies), arr, len(shapes), sarr, C.byref(cs),
+                C.byref(sid), C.byref(st)))
+            return sid.value, st.value
         check(self._L.pbf_server_open_coupled_scene(
             self._h, C.byref(settings), len(x), _ptr(x), _ptr(vv) if vv is not None else None,
             mass, _ptr(g), len(local), _ptr(local), _ptr(body), _ptr(psi), len(bodies), arr,

@@ -349,3 +349,137 @@ def test_deep_queue_runs_several_steps_per_launch():
     assert 0.0 < st["step_ms_p50"] <= st["step_ms_p99"]
     assert same(served(srv, sid, w.n), alone(w, [w.dt] * 16))
     srv.close()
+
+
+def served_shapes_of(model):
+    """capi.RigidShape for each of a model's sphere and plane shapes, in model order."""
+    import novaphy_gb300 as nv
+
+    out = []
+    for sh in model.shapes:
+        s = capi.RigidShape()
+        s.body = sh.body_index
+        s.friction = sh.friction
+        s.restitution = sh.restitution
+        if sh.type == nv.ShapeType.Sphere:
+            s.type = capi.SHAPE_SPHERE
+            s.radius = sh.sphere_radius
+            s.local_pos[:] = [float(c) for c in sh.local_transform.position]
+        else:
+            assert sh.type == nv.ShapeType.Plane
+            s.type = capi.SHAPE_PLANE
+            s.normal[:] = [float(c) for c in sh.plane_normal]
+            s.offset = sh.plane_offset
+        out.append(s)
+    return out
+
+
+def test_served_scene_with_contacts_equals_fluid_world():
+    """A served coupled scene whose bodies collide follows FluidWorld.step bit
+    for bit: a sphere resting on the ground plane, a second sphere pressed
+    against it, fluid falling on both, with contacts at work every step (the
+    host World's contact count says so).  The server runs World's rigid
+    pipeline on the device for it (pbf_server_open_coupled_scene_contacts);
+    a scene of free bodies shares the batch."""
+    import novaphy_gb300 as nv
+
+    mb = nv.ModelBuilder()
+    mb.add_ground_plane(y=0.0)
+    a = mb.add_body(nv.RigidBody.from_sphere(2.0, 0.1),
+                    nv.Transform.from_translation(np.array([0.5, 0.098, 0.5], np.float32)))
+    mb.add_shape(nv.CollisionShape.make_sphere(0.1, a))
+    b = mb.add_body(nv.RigidBody.from_sphere(1.0, 0.08),
+                    nv.Transform.from_translation(np.array([0.67, 0.085, 0.52], np.float32)))
+    mb.add_shape(nv.CollisionShape.make_sphere(0.08, b))
+    model = mb.build()
+    pbf = nv.PBFSettings()
+    pbf.kernel_radius = 0.2
+    pbf.solver_iterations = 2
+    blk = nv.FluidBlockDef()
+    blk.lower = np.array([0.35, 0.25, 0.35], np.float32)
+    blk.upper = np.array([0.75, 0.5, 0.7], np.float32)
+    blk.particle_spacing = 0.05
+    fw = nv.FluidWorld(model, [blk], nv.SolverSettings(), pbf, boundary_extent=1.0)
+    x0 = fw.fluid_state.positions_array.copy()
+    v0 = fw.fluid_state.velocities_array.copy()
+    bps = fw.boundary_particles
+    local = np.stack([bp.local_position for bp in bps]).astype(np.float32)
+    body = np.array([bp.body_index for bp in bps], np.int32)
+    psi = np.array([bp.volume for bp in bps], np.float32)
+    bodies = []
+    for k, rb in enumerate(model.bodies):
+        tr = model.initial_transforms[k]
+        q = np.asarray(tr.rotation, np.float32)  # x, y, z, w
+        rbc = capi.RigidBody()
+        rbc.pos[:] = [float(c) for c in tr.position]
+        rbc.quat[:] = [float(q[3]), float(q[0]), float(q[1]), float(q[2])]
+        rbc.inv_mass = rb.inv_mass()
+        rbc.inv_inertia[:] = rb.inv_inertia()
+        bodies.append(rbc)
+    st = capi.Settings()
+    for name, _ in capi.Settings._fields_:
+        val = getattr(fw.pbf_settings, name)
+        if name in ("domain_lower", "domain_upper"):
+            getattr(st, name)[:] = [float(c) for c in val]
+        else:
+            setattr(st, name, val)
+    mass = fw.pbf_settings.particle_mass(0.05)
+    g = [0.0, -9.81, 0.0]
+    dt = float(np.float32(1 / 60))
+    nsteps = 6
+
+    other = small_scenes(k=1, seed=29)[0]
+    srv = capi.Server(capi.server_config(min_step_particles=0))
+    oid, _ = srv.open_scene(settings_of(other), other.x, other.v, other.mass, other.gravity)
+    sid, state = srv.open_coupled_scene(st, x0, v0, mass, g, local, body, psi, bodies,
+                                        shapes=served_shapes_of(model))
+    assert state == capi.SCENE_RESIDENT
+    qo = srv.submit(oid, other.dt, nsteps)
+    qs = srv.submit(sid, dt, nsteps)
+    assert srv.wait(qs) == capi.REQ_DONE and srv.wait(qo) == capi.REQ_DONE
+    kinds = set()
+    for _ in range(nsteps):
+        fw.step(dt)
+        cs = fw.contacts
+        assert len(cs) >= 2, "the sphere rests on the plane and touches the other sphere"
+        kinds |= {(c.body_a, c.body_b) for c in cs}
+    assert (-1, 0) in kinds and (0, 1) in kinds
+    fs = fw.fluid_state
+    for got, want in ((srv.read(sid, capi.FIELD_POSITIONS, len(x0)), fs.positions_array),
+                      (srv.read(sid, capi.FIELD_VELOCITIES, len(x0)), fs.velocities_array),
+                      (srv.read(sid, capi.FIELD_DENSITIES, len(x0)), fs.densities_array)):
+        assert np.array_equal(got.view(np.uint32), np.asarray(want, np.float32).view(np.uint32))
+    out = srv.read_bodies(sid, len(bodies))
+    for k, rb in enumerate(out):
+        tr = fw.state.transforms[k]
+        q = np.asarray(tr.rotation, np.float32)
+        assert np.array_equal(np.array(rb.pos, np.float32), np.asarray(tr.position, np.float32)), k
+        assert np.array_equal(np.array(rb.quat, np.float32), q[[3, 0, 1, 2]]), k
+        assert np.array_equal(np.array(rb.lin_vel, np.float32),
+                              np.asarray(fw.state.linear_velocities[k], np.float32)), k
+        assert np.array_equal(np.array(rb.ang_vel, np.float32),
+                              np.asarray(fw.state.angular_velocities[k], np.float32)), k
+    # The sphere on the plane stays on it (the contact holds it up).
+    assert out[0].pos[1] > 0.09
+    srv.close()
+
+
+def test_served_contacts_reject_unsupported_shapes():
+    w = small_scenes(k=1, seed=30)[0]
+    rb = capi.RigidBody()
+    rb.quat[:] = [1.0, 0.0, 0.0, 0.0]
+    rb.inv_mass = 1.0
+    rb.inv_inertia[:] = [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    bad = capi.RigidShape()
+    bad.type = 7
+    bad.body = 0
+    missing = capi.RigidShape()
+    missing.type = capi.SHAPE_SPHERE
+    missing.body = 3
+    srv = capi.Server()
+    for sh in (bad, missing):
+        with pytest.raises(capi.PbfError):
+            srv.open_coupled_scene(settings_of(w), w.x, w.v, w.mass, w.gravity,
+                                   np.zeros((1, 3), np.float32), np.zeros(1, np.int32),
+                                   np.ones(1, np.float32), [rb], shapes=[sh])
+    srv.close()
