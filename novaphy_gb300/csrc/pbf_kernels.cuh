@@ -462,8 +462,9 @@ __device__ __forceinline__ T ld_step(const T* p) {
 // kBigScene particles walk cooperatively (see CoopBlock).
 
 // Candidates staged per chunk, and survivors listed before an evaluation:
-// shared memory is CH * 13 + CAP * 8 bytes per warp (6.8 KB), eight blocks
-// of four warps per SM.
+// shared memory is CH * 17 + CAP * 8 bytes per warp (7.2 KB), eight blocks
+// of four warps per SM.  (128-candidate chunks pad less but fit seven
+// blocks per SM, and measured slower.)
 constexpr int coop_chunk(int) { return 64; }
 constexpr int kCoopCap = 768;
 
@@ -473,6 +474,7 @@ struct CoopSmem {
     alignas(16) float sx[CH];          // staged x* of the chunk, by component; slots past
     alignas(16) float sy[CH];          // the last staged one up to a multiple of 32
     alignas(16) float sz[CH];          // hold +inf (never in support)
+    alignas(16) float sw[CH];          // staged x*.w (lambda in the delta pass)
     unsigned char c[CH];               // cell of the candidate among [xmin - 1, xmax + 1]
     uint32_t q[kCap];                  // candidate position of each listed survivor
     uint32_t mask[(kCap + 31) / 32][32];  // mask[w][lane] bit b: survivor 32 w + b is a term of the lane
@@ -526,7 +528,12 @@ __device__ __forceinline__ bool coop_row(bool active, const int4 cell, const Gri
 // the lane's x*, ci its cell x; `cut` the support test r_sq < cut of the
 // pass.  extra(q) returns the per-candidate extras of candidate q (kExtra);
 // body(xj, ej) adds the term of one candidate, re-testing r_sq < cut.
-template <int CH, bool kExtra, bool kPersist, class Extra, class Body>
+// kLam (the delta pass): a candidate whose lambda sum with the lane,
+// xi.w + xj.w, is zero adds an exact zero to the lane's sum (no s_corr
+// either, which needs a negative sum), and the sum, started at +0, never is
+// -0, so such candidates are not listed; when every lane's lambda is zero,
+// candidates with zero lambda are not staged at all.
+template <int CH, bool kExtra, bool kPersist, bool kLam, class Extra, class Body>
 __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRow& R, int ci,
                                           const float4 xi, const float4* xin, float cut,
                                           const GridDesc& Gd, const uint32_t* __restrict__ off,
@@ -555,7 +562,9 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
     const uint32_t lt = lanemask_lt();
     const float2 m1 = make_float2(-1.0f, -1.0f);
     const float2 px = make_float2(xi.x, xi.x), py = make_float2(xi.y, xi.y),
-                 pz = make_float2(xi.z, xi.z);
+                 pz = make_float2(xi.z, xi.z), pw = make_float2(xi.w, xi.w);
+    // Only candidates with a nonzero lambda can add to a lane whose own is zero.
+    const bool lam_filter = kLam && !__any_sync(full, xi.w != 0.0f);
     int nst = 0;   // staged in the current chunk
     int base = 0;  // survivors listed so far (a multiple of 32)
     int cnt = 0;   // the lane's listed terms
@@ -601,6 +610,7 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
             sm.sx[k] = __int_as_float(0x7f800000);
             sm.sy[k] = 0.0f;
             sm.sz[k] = 0.0f;
+            sm.sw[k] = 0.0f;
             sm.c[k] = 0;
         }
         __syncwarp();
@@ -630,8 +640,15 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
                 float2 r2 = __fmul2_rn(dx, dx);
                 r2 = __ffma2_rn(dy, dy, r2);
                 r2 = __ffma2_rn(dz, dz, r2);
-                if (r2.x < lim2) bits |= 1u << b;
-                if (r2.y < lim2) bits |= 2u << b;
+                if constexpr (kLam) {
+                    const float2 W = *reinterpret_cast<const float2*>(&sm.sw[k0 + b]);
+                    const float2 ls = __fadd2_rn(pw, W);
+                    if (r2.x < lim2 && ls.x != 0.0f) bits |= 1u << b;
+                    if (r2.y < lim2 && ls.y != 0.0f) bits |= 2u << b;
+                } else {
+                    if (r2.x < lim2) bits |= 1u << b;
+                    if (r2.y < lim2) bits |= 2u << b;
+                }
             }
             bits &= allowed;
             sm.mask[(base >> 5) + wd][lane] = bits;
@@ -669,6 +686,7 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
                 const float ey = fmaxf(0.0f, fmaxf(ly - xj.y, xj.y - hy));
                 const float ez = fmaxf(0.0f, fmaxf(lz - xj.z, xj.z - hz));
                 pass = ex * ex + (ey * ey + ez * ez) < lim;
+                if (lam_filter) pass = pass && xj.w != 0.0f;
             }
             const uint32_t m = __ballot_sync(full, pass);
             if (pass) {
@@ -676,6 +694,7 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
                 sm.sx[k] = xj.x;
                 sm.sy[k] = xj.y;
                 sm.sz[k] = xj.z;
+                sm.sw[k] = xj.w;
                 sm.q[base + k] = q;
                 sm.c[k] = (unsigned char)((q >= b1) + (q >= b2) + (q >= b3) + (q >= b4));
             }
@@ -736,7 +755,7 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     };
     if constexpr (kCoop) {
         if (coop) {
-            coop_walk<CH, false, kPersist>(
+            coop_walk<CH, false, kPersist, false>(
                 sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, [](uint32_t) { return float4{}; },
                 [&](const float4& xj, const float4&) { term(xj); });
         }
@@ -804,7 +823,9 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     auto term = [&](const float4& xj) {
         float rx, ry, rz, lambda_sum;
         const float r_sq = rel_sq<true>(xi, xj, rx, ry, rz, &lambda_sum);
-        if (r_sq < C.cut) {
+        // A zero lambda sum adds an exact zero (no s_corr either); the sum,
+        // started at +0, never becomes -0, so skipping it keeps every bit.
+        if (r_sq < C.cut && lambda_sum != 0.0f) {
             float s_corr = 0.0f;
             if (lambda_sum < -1e-10f && C.scorr_on) {
                 float ratio = poly6(r_sq, C) / C.w_dq;
@@ -822,7 +843,7 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     };
     if constexpr (kCoop) {
         if (coop) {
-            coop_walk<CH, false, kPersist>(
+            coop_walk<CH, false, kPersist, true>(
                 sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, [](uint32_t) { return float4{}; },
                 [&](const float4& xj, const float4&) { term(xj); });
         }
@@ -997,7 +1018,7 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
         };
         if constexpr (B::kOn) {
             if (coop)
-                coop_walk<coop_chunk(BS), true, false>(
+                coop_walk<coop_chunk(BS), true, false, false>(
                     sm[threadIdx.x >> 5], R, cell.x, xi, xin, C.h2, C.grid, G.off,
                     [&](uint32_t q) { return __ldg(sv + q); }, term);
         }
@@ -1058,7 +1079,7 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
     };
     if constexpr (B::kOn) {
         if (coop)
-            coop_walk<coop_chunk(BS), true, false>(sm[threadIdx.x >> 5], R, cell.x, xi, xin,
+            coop_walk<coop_chunk(BS), true, false, false>(sm[threadIdx.x >> 5], R, cell.x, xi, xin,
                                                    C.cut, C.grid, G.off,
                                                    [&](uint32_t q) { return __ldg(sv + q); }, term);
     }
@@ -1117,7 +1138,7 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     };
     if constexpr (B::kOn) {
         if (coop)
-            coop_walk<coop_chunk(BS), true, false>(
+            coop_walk<coop_chunk(BS), true, false, false>(
                 sm[threadIdx.x >> 5], R, cell.x, xi, xin, C.cut, C.grid, G.off,
                 [&](uint32_t q) {
                     return make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f);
