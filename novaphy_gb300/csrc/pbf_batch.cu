@@ -199,10 +199,12 @@ int ensure_slots(pbf_batch* b, uint32_t nslots) {
     b->off_cap = 0;
     const uint32_t c = nslots + nslots / 4 + 1;
     const size_t ob = align_up((size_t)(c + 1) * 4, 256);
-    PBF_CUDA(cudaMalloc(&b->off, ob + align_up(c, 256)));
+    const size_t ab = align_up(c + 1, 256);
+    PBF_CUDA(cudaMalloc(&b->off, ob + ab + (size_t)(c + 1) * 4));
     b->off_cap = c + 1;
     b->B.off = b->off;
     b->B.slot_alias = reinterpret_cast<unsigned char*>(b->off) + ob;
+    b->B.moved = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(b->off) + ob + ab);
     return PBF_OK;
 }
 
@@ -708,7 +710,9 @@ int batch_reserve(pbf_batch* b, int particles, int scenes) {
 size_t batch_bytes(const pbf_batch* b) {
     size_t t = 0;
     if (b->wmem) t += work_bytes(b->cap) + sort_scratch_bytes(b->cap) + extra_bytes(b->cap);
-    if (b->off) t += align_up((size_t)b->off_cap * 4, 256) + align_up(b->off_cap, 256);
+    if (b->off)
+        t += align_up((size_t)b->off_cap * 4, 256) + align_up(b->off_cap, 256) +
+             (size_t)b->off_cap * 4;
     t += b->tab_bytes + (size_t)b->bad_cap * 4;
     return t;
 }

@@ -138,8 +138,11 @@ void free_particles(pbf_scene* s) {
     s->sort = SortScratch{};
     s->B = StepBuffers{};
     s->B.off = s->off;
-    if (s->off) s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) +
-                                  align_up((size_t)s->off_cap * 4, 256);
+    if (s->off) {
+        s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) +
+                          align_up((size_t)s->off_cap * 4, 256);
+        s->B.moved = reinterpret_cast<uint32_t*>(s->B.slot_alias + align_up(s->off_cap, 256));
+    }
 }
 
 // (Re)allocates the resident state for `cap` particles; the step scratch
@@ -288,12 +291,15 @@ int ensure_offsets(pbf_scene* s, uint32_t nslots) {
     }
     if (s->off) cudaFree(s->off);
     s->off = nullptr;
-    // offsets (nslots + 1 words) followed by one alias byte per slot
+    // offsets (nslots + 1 words), one alias byte per slot, one moved word
+    // per slot
     const size_t ob = align_up((size_t)(nslots + 1) * 4, 256);
-    PBF_CUDA(cudaMalloc(&s->off, ob + align_up(nslots, 256)));
+    const size_t ab = align_up(nslots + 1, 256);
+    PBF_CUDA(cudaMalloc(&s->off, ob + ab + (size_t)(nslots + 1) * 4));
     s->off_cap = nslots + 1;
     s->B.off = s->off;
     s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) + ob;
+    s->B.moved = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(s->off) + ob + ab);
     return PBF_OK;
 }
 
@@ -813,7 +819,9 @@ size_t scene_device_bytes(const pbf_scene* s) {
              align_up((size_t)c * 12, 256);
     }
     if (s->wmem) b += work_bytes(s->work_cap) + sort_scratch_bytes(s->work_cap);
-    if (s->off) b += align_up((size_t)s->off_cap * 4, 256) + align_up(s->off_cap, 256);
+    if (s->off)
+        b += align_up((size_t)s->off_cap * 4, 256) + align_up(s->off_cap, 256) +
+             (size_t)s->off_cap * 4;
     return b;
 }
 

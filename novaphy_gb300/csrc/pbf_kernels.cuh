@@ -403,6 +403,7 @@ struct Grid {
     const uint32_t* __restrict__ bend;
     const uint32_t* __restrict__ btab;
     const uint32_t* __restrict__ spid;  // scene of each sorted particle (batches)
+    uint32_t* moved;                     // per slot, see StepBuffers::moved
 };
 
 __device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
@@ -717,6 +718,28 @@ __device__ __forceinline__ uint32_t scene_at(const Grid& G, uint32_t p) {
     return G.spid ? __ldg(G.spid + p) : 0u;
 }
 
+// Whether a particle of a slot among the 27 around a clean particle's cell
+// moved in the delta pass of Jacobi iteration it - 1 (moved stamp == it).
+// When none did, the particle's candidates all sit where they sat for the
+// previous density pass, so its rho and lambda would come out bit for bit
+// the same.
+template <bool kPersist>
+__device__ __forceinline__ bool neighbourhood_moved(const int4 cell, const GridDesc& Gd,
+                                                    const uint32_t* moved, int it) {
+    for (int dz = -1; dz <= 1; ++dz) {
+        const uint32_t wz = (uint32_t)wrap(cell.z + dz, Gd.oz, Gd.gz);
+        for (int dy = -1; dy <= 1; ++dy) {
+            const uint32_t row = Gd.base + (uint32_t)Gd.gx * ((uint32_t)wrap(cell.y + dy, Gd.oy, Gd.gy) +
+                                                              (uint32_t)Gd.gy * wz);
+            for (int dx = -1; dx <= 1; ++dx) {
+                const uint32_t s = row + (uint32_t)wrap(cell.x + dx, Gd.ox, Gd.gx);
+                if (ld_step<kPersist>(moved + s) == (uint32_t)it) return true;
+            }
+        }
+    }
+    return false;
+}
+
 // compute_density + compute_lambda (pbf_solver.cpp:129-179) in one candidate
 // pass for sorted particle p.  Reads x* from xin, writes (x*, lambda) to xout
 // and rho to srho.  Scenes whose `iters` are done by iteration `it` are left
@@ -730,8 +753,15 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     constexpr bool kCoop = CoopBlock<P, 32, false, U>::kOn;
     const uint32_t pa = active ? p : 0u;
     const StepConsts& C = prm.at(G.spid, pa);
-    const bool live = active && it < C.iters;
+    bool live = active && it < C.iters;
     const int4 cell = cell_at(G, pa);
+    if (live && it > 0 && G.moved && cell.w == 0 &&
+        !neighbourhood_moved<kPersist>(cell, C.grid, G.moved, it)) {
+        // Nothing around moved since the last density pass: keep its rho
+        // (srho) and lambda (x*.w, which the delta pass carried through).
+        xout[p] = xin[p];
+        live = false;
+    }
     CoopRow R;
     bool coop = false;
     if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R);
@@ -855,6 +885,10 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     const float py = xi.y + dy * C.inv_rho0;
     const float pz = xi.z + dz * C.inv_rho0;
     xout[p] = make_float4(px, py, pz, xi.w);
+    if (G.moved && (__float_as_uint(px) != __float_as_uint(xi.x) ||
+                    __float_as_uint(py) != __float_as_uint(xi.y) ||
+                    __float_as_uint(pz) != __float_as_uint(xi.z)))
+        G.moved[slot_of(cell.x, cell.y, cell.z, C.grid)] = (uint32_t)it + 1u;
     if (it == C.iters - 1) sv[p] = update_velocity(px, py, pz, sx[p], srho[p], C);
 }
 
@@ -1216,7 +1250,7 @@ k_debug_neighbors(const float4* __restrict__ xin, const float4* __restrict__ sx,
 inline int grid_of(int n, int b) { return (n + b - 1) / b; }
 
 inline Grid grid_view(const StepBuffers& B, const uint32_t* spid = nullptr) {
-    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid};
+    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved};
 }
 
 // predict, sort by cell and by reference key, cell offsets, gather, reference
@@ -1231,6 +1265,7 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     const OneScene one{Cs, StateRef{B.x, B.v, B.rho, B.lam, 0u, nullptr}};
     const SceneIds none{nullptr, nullptr};
     cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)C.grid.nslots, st);
+    if (e == cudaSuccess && B.moved) e = cudaMemsetAsync(B.moved, 0, (size_t)C.grid.nslots * 4, st);
     if (e != cudaSuccess) return e;
     if (pm) pm->mark(-1, 0, st);
     k_predict_key<<<nb, kBlock, 0, st>>>(B.keys, B.rkeys, n, none, one);
@@ -1432,6 +1467,7 @@ inline cudaError_t enqueue_batch_step(const StepBuffers& B, const BatchDesc& D, 
     const SceneTable tab{D.tab, D.refs};
     const SceneIds ids{D.pid, D.spid};
     cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)D.nslots, st);
+    if (e == cudaSuccess && B.moved) e = cudaMemsetAsync(B.moved, 0, (size_t)D.nslots * 4, st);
     if (e != cudaSuccess) return e;
     if (pm) pm->mark(-1, 0, st);
     k_scene_ids<<<grid_of(n, 256), 256, 0, st>>>(D.firsts, D.nscenes, D.pid, n);

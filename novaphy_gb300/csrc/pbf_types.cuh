@@ -86,6 +86,9 @@ struct StepBuffers {
     uint32_t* btab;      // 27 bucket starts per dirty owner row
     int* sown;           // 0 = clean, else owner row + 1
     unsigned char* slot_alias;  // slot holds a particle from outside the grid box
+    // Per slot: 1 + the Jacobi iteration whose delta pass last moved a
+    // particle of the slot (0: none in this step).
+    uint32_t* moved;
     uint32_t* err;  // device status word
 };
 
