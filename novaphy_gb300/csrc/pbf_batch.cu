@@ -200,11 +200,12 @@ int ensure_slots(pbf_batch* b, uint32_t nslots) {
     const uint32_t c = nslots + nslots / 4 + 1;
     const size_t ob = align_up((size_t)(c + 1) * 4, 256);
     const size_t ab = align_up(c + 1, 256);
-    PBF_CUDA(cudaMalloc(&b->off, ob + ab + (size_t)(c + 1) * 4));
+    PBF_CUDA(cudaMalloc(&b->off, ob + ab + (size_t)(c + 1) * 8));
     b->off_cap = c + 1;
     b->B.off = b->off;
     b->B.slot_alias = reinterpret_cast<unsigned char*>(b->off) + ob;
     b->B.moved = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(b->off) + ob + ab);
+    b->B.lamnz = b->B.moved + (c + 1);
     return PBF_OK;
 }
 
@@ -712,7 +713,7 @@ size_t batch_bytes(const pbf_batch* b) {
     if (b->wmem) t += work_bytes(b->cap) + sort_scratch_bytes(b->cap) + extra_bytes(b->cap);
     if (b->off)
         t += align_up((size_t)b->off_cap * 4, 256) + align_up(b->off_cap, 256) +
-             (size_t)b->off_cap * 4;
+             (size_t)b->off_cap * 8;
     t += b->tab_bytes + (size_t)b->bad_cap * 4;
     return t;
 }

@@ -142,6 +142,7 @@ void free_particles(pbf_scene* s) {
         s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) +
                           align_up((size_t)s->off_cap * 4, 256);
         s->B.moved = reinterpret_cast<uint32_t*>(s->B.slot_alias + align_up(s->off_cap, 256));
+        s->B.lamnz = s->B.moved + s->off_cap;
     }
 }
 
@@ -291,15 +292,16 @@ int ensure_offsets(pbf_scene* s, uint32_t nslots) {
     }
     if (s->off) cudaFree(s->off);
     s->off = nullptr;
-    // offsets (nslots + 1 words), one alias byte per slot, one moved word
-    // per slot
+    // offsets (nslots + 1 words), one alias byte per slot, a moved word and
+    // a lambda word per slot
     const size_t ob = align_up((size_t)(nslots + 1) * 4, 256);
     const size_t ab = align_up(nslots + 1, 256);
-    PBF_CUDA(cudaMalloc(&s->off, ob + ab + (size_t)(nslots + 1) * 4));
+    PBF_CUDA(cudaMalloc(&s->off, ob + ab + (size_t)(nslots + 1) * 8));
     s->off_cap = nslots + 1;
     s->B.off = s->off;
     s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) + ob;
     s->B.moved = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(s->off) + ob + ab);
+    s->B.lamnz = s->B.moved + (nslots + 1);
     return PBF_OK;
 }
 
@@ -821,7 +823,7 @@ size_t scene_device_bytes(const pbf_scene* s) {
     if (s->wmem) b += work_bytes(s->work_cap) + sort_scratch_bytes(s->work_cap);
     if (s->off)
         b += align_up((size_t)s->off_cap * 4, 256) + align_up(s->off_cap, 256) +
-             (size_t)s->off_cap * 4;
+             (size_t)s->off_cap * 8;
     return b;
 }
 

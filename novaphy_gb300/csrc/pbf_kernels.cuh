@@ -404,6 +404,7 @@ struct Grid {
     const uint32_t* __restrict__ btab;
     const uint32_t* __restrict__ spid;  // scene of each sorted particle (batches)
     uint32_t* moved;                     // per slot, see StepBuffers::moved
+    uint32_t* lamnz;                     // per slot, see StepBuffers::lamnz
 };
 
 __device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
@@ -463,11 +464,11 @@ __device__ __forceinline__ T ld_step(const T* p) {
 // kBigScene particles walk cooperatively (see CoopBlock).
 
 // Candidates staged per chunk, and survivors listed before an evaluation:
-// shared memory is CH * 17 + CAP * 8 bytes per warp (7.2 KB), eight blocks
-// of four warps per SM.  (128-candidate chunks pad less but fit seven
+// shared memory is CH * 17 + CAP * 8 bytes per warp (6.98 KB), eight blocks
+// of four warps per SM (each block also takes 1 KB of the SM's 228 KB).  (128-candidate chunks pad less but fit seven
 // blocks per SM, and measured slower.)
 constexpr int coop_chunk(int) { return 64; }
-constexpr int kCoopCap = 768;
+constexpr int kCoopCap = 736;
 
 template <int CH, bool kExtra>
 struct CoopSmem {
@@ -480,6 +481,12 @@ struct CoopSmem {
     uint32_t q[kCap];                  // candidate position of each listed survivor
     uint32_t mask[(kCap + 31) / 32][32];  // mask[w][lane] bit b: survivor 32 w + b is a term of the lane
 };
+
+// Blocks per SM the neighbour-pass kernels are compiled for: eight for the
+// cooperative single-scene kernels (64 registers; their shared memory fits
+// eight blocks), the compiler's choice for the others.
+template <int U>
+constexpr int kPassMinBlocks = U == 8 ? 8 : 1;
 
 // Shared memory of a kernel's warps: real for the kernels of a single large
 // scene (those with the 8-way row loop, see kBigScene), one byte otherwise.
@@ -718,11 +725,12 @@ __device__ __forceinline__ uint32_t scene_at(const Grid& G, uint32_t p) {
     return G.spid ? __ldg(G.spid + p) : 0u;
 }
 
-// Whether a particle of a slot among the 27 around a clean particle's cell
-// moved in the delta pass of Jacobi iteration it - 1 (moved stamp == it).
-// When none did, the particle's candidates all sit where they sat for the
-// previous density pass, so its rho and lambda would come out bit for bit
-// the same.
+// Whether a slot among the 27 around a clean particle's cell holds the stamp
+// `it`: with the moved stamps and it, whether a candidate moved in the delta
+// pass of Jacobi iteration it - 1 (when none did, the candidates all sit
+// where they sat for the previous density pass, so the particle's rho and
+// lambda would come out bit for bit the same); with the lambda stamps and
+// it + 1, whether a candidate has a nonzero lambda in iteration it.
 template <bool kPersist>
 __device__ __forceinline__ bool neighbourhood_moved(const int4 cell, const GridDesc& Gd,
                                                     const uint32_t* moved, int it) {
@@ -759,7 +767,10 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
         !neighbourhood_moved<kPersist>(cell, C.grid, G.moved, it)) {
         // Nothing around moved since the last density pass: keep its rho
         // (srho) and lambda (x*.w, which the delta pass carried through).
-        xout[p] = xin[p];
+        const float4 keep = xin[p];
+        xout[p] = keep;
+        if (G.lamnz && keep.w != 0.0f)
+            G.lamnz[slot_of(cell.x, cell.y, cell.z, C.grid)] = (uint32_t)it + 1u;
         live = false;
     }
     CoopRow R;
@@ -796,12 +807,13 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     sum_grad_sq += sqn(gix, giy, giz);
     const float Ci = density * C.inv_rho0 - 1.0f;
     const float lam = (Ci < 0.0f) ? 0.0f : -Ci / (sum_grad_sq + C.eps);
+    if (G.lamnz && lam != 0.0f) G.lamnz[slot_of(cell.x, cell.y, cell.z, C.grid)] = (uint32_t)it + 1u;
     srho[p] = density;
     xout[p] = make_float4(xi.x, xi.y, xi.z, lam);
 }
 
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
 k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
                  int it, int n, const Grid G, const P prm) {
     using B = CoopBlock<P, BS, false, U>;
@@ -844,11 +856,23 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     const StepConsts& C = prm.at(G.spid, pa);
     const bool live = active && it < C.iters;
     const int4 cell = cell_at(G, pa);
+    float4 xi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    bool walk = live;
+    if (live) {
+        xi = xin[p];
+        // A clean particle with a zero lambda whose 27 cells hold no nonzero
+        // lambda in this iteration has only zero terms: no walk.
+        if (G.lamnz && cell.w == 0 && xi.w == 0.0f &&
+            !neighbourhood_moved<kPersist>(cell, C.grid, G.lamnz, it + 1))
+            walk = false;
+    }
+    // The warp walks cooperatively when every lane is live, even if only
+    // some need the walk: the others have only zero terms, which the walk's
+    // lambda test leaves out, so they list nothing.
     CoopRow R;
     bool coop = false;
     if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R);
     if (!live) return;
-    const float4 xi = xin[p];
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
     auto term = [&](const float4& xj) {
         float rx, ry, rz, lambda_sum;
@@ -872,13 +896,13 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
         }
     };
     if constexpr (kCoop) {
-        if (coop) {
+        if (coop && __any_sync(0xffffffffu, walk)) {
             coop_walk<CH, false, kPersist, true>(
                 sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, [](uint32_t) { return float4{}; },
                 [&](const float4& xj, const float4&) { term(xj); });
         }
     }
-    if (!coop)
+    if (walk && !coop)
         for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
                               [&](uint32_t q) { term(ld_step<kPersist>(xin + q)); });
     const float px = xi.x + dx * C.inv_rho0;
@@ -893,7 +917,7 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
 }
 
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
 k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
         const float* __restrict__ srho, float4* __restrict__ sv, int it, int n, const Grid G,
         const P prm) {
@@ -1020,7 +1044,7 @@ __device__ __forceinline__ void commit(uint32_t p, float px, float py, float pz,
 // apply_xsph_viscosity (pbf_solver.cpp:225-250) + commit, no vorticity.
 // With skip_vort set, scenes with vorticity are left to the vorticity pair.
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
 k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, const float4* __restrict__ sx,
               const float* __restrict__ srho, int n, int skip_vort, const Grid G, const P prm) {
     using B = CoopBlock<P, BS, true, U>;
@@ -1075,7 +1099,7 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
 //   omega_i = sum_j (m/rho_j') spiky_grad(x*_i - x*_j) x (v_j - v_i),
 // the SPH curl (Macklin & Mueller 2013, section 5, with its volume factor).
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
 k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, float4* __restrict__ sv2,
              float4* __restrict__ som, int n, const Grid G, const P prm) {
     using B = CoopBlock<P, BS, true, U>;
@@ -1138,7 +1162,7 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
 //   eta_i = sum_j (m/rho_j') (|omega_j| - |omega_i|) spiky_grad(x*_i - x*_j),
 //   N = eta / |eta|,  v += dt * eps * (N x omega_i).
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
 k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv,
                    const float4* __restrict__ sv2, const float4* __restrict__ som,
                    const float4* __restrict__ sx, const float* __restrict__ srho, int n,
@@ -1250,7 +1274,7 @@ k_debug_neighbors(const float4* __restrict__ xin, const float4* __restrict__ sx,
 inline int grid_of(int n, int b) { return (n + b - 1) / b; }
 
 inline Grid grid_view(const StepBuffers& B, const uint32_t* spid = nullptr) {
-    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved};
+    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved, B.lamnz};
 }
 
 // predict, sort by cell and by reference key, cell offsets, gather, reference
@@ -1266,6 +1290,7 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     const SceneIds none{nullptr, nullptr};
     cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)C.grid.nslots, st);
     if (e == cudaSuccess && B.moved) e = cudaMemsetAsync(B.moved, 0, (size_t)C.grid.nslots * 4, st);
+    if (e == cudaSuccess && B.lamnz) e = cudaMemsetAsync(B.lamnz, 0, (size_t)C.grid.nslots * 4, st);
     if (e != cudaSuccess) return e;
     if (pm) pm->mark(-1, 0, st);
     k_predict_key<<<nb, kBlock, 0, st>>>(B.keys, B.rkeys, n, none, one);
@@ -1468,6 +1493,7 @@ inline cudaError_t enqueue_batch_step(const StepBuffers& B, const BatchDesc& D, 
     const SceneIds ids{D.pid, D.spid};
     cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)D.nslots, st);
     if (e == cudaSuccess && B.moved) e = cudaMemsetAsync(B.moved, 0, (size_t)D.nslots * 4, st);
+    if (e == cudaSuccess && B.lamnz) e = cudaMemsetAsync(B.lamnz, 0, (size_t)D.nslots * 4, st);
     if (e != cudaSuccess) return e;
     if (pm) pm->mark(-1, 0, st);
     k_scene_ids<<<grid_of(n, 256), 256, 0, st>>>(D.firsts, D.nscenes, D.pid, n);

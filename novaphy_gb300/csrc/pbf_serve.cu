@@ -52,7 +52,7 @@ using namespace pbf::capi;
 
 namespace {
 
-constexpr size_t kGridBytesPerSlot = 9;  // offset word, alias byte, moved word
+constexpr size_t kGridBytesPerSlot = 13;  // offset word, alias byte, moved and lambda words
 // Records of finished requests kept for pbf_server_wait; older ones are
 // dropped, so a long-running server holds bounded host memory.
 constexpr size_t kFinishedKept = (size_t)1 << 16;

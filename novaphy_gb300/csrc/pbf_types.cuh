@@ -89,6 +89,9 @@ struct StepBuffers {
     // Per slot: 1 + the Jacobi iteration whose delta pass last moved a
     // particle of the slot (0: none in this step).
     uint32_t* moved;
+    // Per slot: 1 + the Jacobi iteration whose density pass last left a
+    // particle of the slot with a nonzero lambda (0: none in this step).
+    uint32_t* lamnz;
     uint32_t* err;  // device status word
 };
 
