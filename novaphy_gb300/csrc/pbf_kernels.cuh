@@ -734,18 +734,26 @@ __device__ __forceinline__ uint32_t scene_at(const Grid& G, uint32_t p) {
 template <bool kPersist>
 __device__ __forceinline__ bool neighbourhood_moved(const int4 cell, const GridDesc& Gd,
                                                     const uint32_t* moved, int it) {
-    for (int dz = -1; dz <= 1; ++dz) {
-        const uint32_t wz = (uint32_t)wrap(cell.z + dz, Gd.oz, Gd.gz);
-        for (int dy = -1; dy <= 1; ++dy) {
-            const uint32_t row = Gd.base + (uint32_t)Gd.gx * ((uint32_t)wrap(cell.y + dy, Gd.oy, Gd.gy) +
-                                                              (uint32_t)Gd.gy * wz);
-            for (int dx = -1; dx <= 1; ++dx) {
-                const uint32_t s = row + (uint32_t)wrap(cell.x + dx, Gd.ox, Gd.gx);
-                if (ld_step<kPersist>(moved + s) == (uint32_t)it) return true;
-            }
-        }
+    // The 27 slots from 3 wrapped coordinates per axis; the loads are
+    // independent, so they overlap.
+    uint32_t wx[3], wy[3], wz[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        wx[d] = (uint32_t)wrap(cell.x + d - 1, Gd.ox, Gd.gx);
+        wy[d] = (uint32_t)wrap(cell.y + d - 1, Gd.oy, Gd.gy);
+        wz[d] = (uint32_t)wrap(cell.z + d - 1, Gd.oz, Gd.gz);
     }
-    return false;
+    bool any = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const uint32_t row = Gd.base + (uint32_t)Gd.gx * (wy[b] + (uint32_t)Gd.gy * wz[c]);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                any |= ld_step<kPersist>(moved + row + wx[a]) == (uint32_t)it;
+        }
+    return any;
 }
 
 // compute_density + compute_lambda (pbf_solver.cpp:129-179) in one candidate
