@@ -27,13 +27,13 @@ namespace pbf {
 namespace PBF_NS {
 
 constexpr int kBlock = 128;
-// A single scene of at least this many particles runs the two constraint
-// passes with the row loop unrolled by 8 (fewer loop instructions per
-// candidate: +3 % on a 1M-particle step).  Smaller scenes and batches keep the
-// 4-way loop: many small scenes stepped side by side on their own streams
-// run several kernels per SM at once, and there the larger code of the 8-way
-// loop measured up to 40 % slower.
-constexpr int kBigScene = 1 << 18;
+// A single scene of at least this many particles runs its neighbour passes
+// with the warp-cooperative walk (and its one-thread fallback with the row
+// loop unrolled by 8).  Smaller scenes and batches keep one thread per
+// particle and the 4-way loop: many small scenes stepped side by side on their
+// own streams run several kernels per SM at once, and there the larger code
+// and shared memory measured up to 40 % slower.
+constexpr int kBigScene = 1 << 17;
 constexpr uint32_t kNoBucket = 0xffffffffu;
 constexpr uint32_t kImpureBit = 0x80000000u;
 
