@@ -61,6 +61,15 @@ typedef struct pbf_settings {
                              bucket merging (neighbor_search.cpp:89-97),
                              including double-visited buckets; 0: plain
                              27-cell neighbourhood */
+    int boundary_two_way; /* 0 (default): the reference's coupling, in which
+                             the boundary pushes the bodies and never the fluid
+                             (fluid_world.cpp:68-79); 1: the Akinci boundary
+                             also enters the fluid's density constraint (its
+                             density, gradient and position correction) in
+                             every Jacobi iteration of pbf_scene_step_coupled,
+                             so the fluid is held off the bodies.  No
+                             counterpart in the reference; single coupled
+                             scenes only (batches and servers refuse it). */
 } pbf_settings;
 
 /* Field selectors for pbf_scene_read / pbf_scene_write. */

@@ -57,6 +57,7 @@ class Settings(C.Structure):
         ("domain_upper", C.c_float * 3),
         ("exact_arithmetic", C.c_int),
         ("hash_compat", C.c_int),
+        ("boundary_two_way", C.c_int),
     ]
 
 
@@ -180,7 +181,7 @@ def default_settings(**kw) -> Settings:
     for k, v in kw.items():
         if k in ("domain_lower", "domain_upper"):
             getattr(s, k)[:] = [float(t) for t in v]
-        elif k in ("use_domain_bounds", "exact_arithmetic", "hash_compat"):
+        elif k in ("use_domain_bounds", "exact_arithmetic", "hash_compat", "boundary_two_way"):
             setattr(s, k, int(bool(v)))
         else:
             setattr(s, k, v)

@@ -43,6 +43,7 @@ static int device_index() {
     }
     s.exact_arithmetic = exact_arithmetic ? 1 : 0;
     s.hash_compat = hash_compat ? 1 : 0;
+    s.boundary_two_way = boundary_two_way ? 1 : 0;
     return s;
 }
 
@@ -795,7 +796,8 @@ void FluidWorld::step(float dt) {
                                                dyn.data()));
             float* fp = needed ? &f[0].x : nullptr;
             float* tp = needed ? &t[0].x : nullptr;
-            if (!monitor_.enabled) {
+            if (!monitor_.enabled || pbf_.boundary_two_way) {
+                // (A two-way step runs only as the whole coupled step.)
                 Scope p(monitor_, "fluid.pbf.total");
                 check_pbf(pbf_scene_step_coupled(scene_, dt, fp, tp));
             } else {

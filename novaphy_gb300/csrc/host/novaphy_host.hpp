@@ -146,6 +146,7 @@ struct PBFSettings {
     Vec3 domain_upper{10.0f, 10.0f, 10.0f};
     bool exact_arithmetic = true;
     bool hash_compat = true;
+    bool boundary_two_way = false;  // no counterpart in the reference (pbf_settings)
     float particle_mass(float spacing) const { return rest_density * spacing * spacing * spacing; }
     ::pbf_settings to_c() const;
 };

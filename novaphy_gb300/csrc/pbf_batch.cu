@@ -662,6 +662,11 @@ int check_args(pbf_batch* b, int nscenes, pbf_scene* const* scenes, const float*
     if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
     if (nscenes < 0) return fail(PBF_ERR_INVALID_ARG, "nscenes must be >= 0");
     if (nscenes > 0 && (!scenes || !dt)) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+    for (int k = 0; k < nscenes; ++k)
+        if (scenes[k] && scenes[k]->settings.boundary_two_way && scenes[k]->bnd.nb > 0)
+            return fail(PBF_ERR_INVALID_ARG,
+                        "boundary_two_way steps run through pbf_scene_step_coupled; a batch "
+                        "steps the fluid without its boundary");
     return PBF_OK;
 }
 

@@ -43,6 +43,16 @@ k_ix_gather(const uint32_t* __restrict__ sidx, const float4* __restrict__ pos,
 }
 
 __global__ void __launch_bounds__(kBlock)
+k_predict_points(const float4* __restrict__ x, const float4* __restrict__ v, int n,
+                 float4* __restrict__ out, const StepConsts C) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float px, py, pz;
+    predict(x[i], v[i], C, px, py, pz);
+    out[i] = make_float4(px, py, pz, 0.0f);
+}
+
+__global__ void __launch_bounds__(kBlock)
 k_qcells(const float4* __restrict__ qpos, int nq, int4* __restrict__ qcell, const StepConsts C) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
@@ -306,6 +316,14 @@ cudaError_t index_build(PointIndex& I, const float4* pos, const float* attr, int
                                        I.slot_alias, C);
     k_buckets<<<grid_of(n, 256), 256, 0, st>>>(I.rsorted, I.ridx, I.pos_of, I.scell, nullptr, I.kpos,
                                                I.bend, n);
+    return cudaGetLastError();
+}
+
+cudaError_t predict_points(const float4* x, const float4* v, int n, float4* out,
+                           const StepConsts& C, cudaStream_t st) {
+    using namespace bnd;
+    if (n <= 0) return cudaSuccess;
+    k_predict_points<<<grid_of(n, kBlock), kBlock, 0, st>>>(x, v, n, out, C);
     return cudaGetLastError();
 }
 

@@ -46,6 +46,11 @@ struct QuerySet {
 cudaError_t index_build(PointIndex& I, const float4* pos, const float* attr, int n,
                         const StepConsts& C, SortScratch& sort, cudaStream_t st);
 
+// x* = x + (v + g dt) dt of n particles (w = 0): the positions whose cells
+// a step sorts by (the predict of k_predict_key, the same operations).
+cudaError_t predict_points(const float4* x, const float4* v, int n, float4* out,
+                           const StepConsts& C, cudaStream_t st);
+
 // Classifies query points qpos[0..nq) against `I`.
 cudaError_t index_classify(const QuerySet& Q, const float4* qpos, int nq, const PointIndex& I,
                            const StepConsts& C, cudaStream_t st);

@@ -378,6 +378,7 @@ int scene_consts(const pbf_scene* s, float dt, StepConsts& C) {
         C.hi[d] = st.domain_upper[d] - pr;
     }
     C.hash_compat = st.hash_compat ? 1 : 0;
+    C.two_way = st.boundary_two_way ? 1 : 0;
     C.iters = st.solver_iterations;
     C.seg_begin = 0;
     C.seg_end = (uint32_t)s->n;
@@ -572,6 +573,7 @@ int pbf_default_settings(pbf_settings* out) {
     d.domain_upper[2] = 10.0f;
     d.exact_arithmetic = 1;
     d.hash_compat = 1;
+    d.boundary_two_way = 0;
     *out = d;
     return PBF_OK;
 }
@@ -630,7 +632,8 @@ int pbf_scene_destroy(pbf_scene* s) {
         DeviceGuard dg(s->device);
         if (s->stream) cudaStreamSynchronize(s->stream);
         for (void* m : {s->bnd.mem, s->bnd.body_mem, s->bnd.sort_mem, s->bnd.fq_mem,
-                        static_cast<void*>(s->bnd.rb), static_cast<void*>(s->bnd.shapes)})
+                        s->bnd.tw_mem, static_cast<void*>(s->bnd.rb),
+                        static_cast<void*>(s->bnd.shapes)})
             if (m) cudaFree(m);
         if (s->bnd.idx.off) cudaFree(s->bnd.idx.off);
         if (s->couple_graph) cudaGraphExecDestroy(s->couple_graph);
@@ -1309,7 +1312,8 @@ namespace {
 // (fluid_world.cpp:57-81 after the PBF step).  C are the constants of the step
 // that produced the current state.  Needs b.nb > 0.
 int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
-                     const float* torque_in, cudaEvent_t* marks = nullptr) {
+                     const float* torque_in, cudaEvent_t* marks = nullptr,
+                     bool density_has_boundary = false) {
     auto& b = s->bnd;
     const int nbodies = b.nbodies;
     cudaStream_t st = s->stream;
@@ -1329,8 +1333,12 @@ int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
     if (rc) return rc;
     e = index_build(b.idx, b.world, nullptr, b.nb, C, b.sort, st);
     QuerySet fq{b.fq_cell, s->B.sown, s->B.btab};
-    if (e == cudaSuccess) e = index_classify(fq, s->B.x, s->n, b.idx, C, st);
-    if (e == cudaSuccess) e = boundary_density(s->B.x, s->n, fq, b.idx, s->B.rho, C, st);
+    // A two-way step's densities already hold the boundary's share (from
+    // its last Jacobi iteration).
+    if (!density_has_boundary) {
+        if (e == cudaSuccess) e = index_classify(fq, s->B.x, s->n, b.idx, C, st);
+        if (e == cudaSuccess) e = boundary_density(s->B.x, s->n, fq, b.idx, s->B.rho, C, st);
+    }
     if (e == cudaSuccess) e = mark(2);
     if (e != cudaSuccess) return cuda_fail(e, "boundary density");
     // 3. coupling forces from a fresh fluid grid on the final positions
@@ -1377,7 +1385,7 @@ int enqueue_coupling(pbf_scene* s, const StepConsts& C, const float* force_in,
 // With phase_ms (3 entries), also the device time of the boundary positions,
 // the boundary density and the coupling forces.
 int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* torque3,
-                      float* phase_ms = nullptr) {
+                      float* phase_ms = nullptr, bool density_has_boundary = false) {
     auto& b = s->bnd;
     if (phase_ms)
         for (int k = 0; k < 3; ++k) phase_ms[k] = 0.0f;
@@ -1394,7 +1402,8 @@ int couple_after_step(pbf_scene* s, const StepConsts& C, float* force3, float* t
         destroy();
         return cuda_fail(cudaGetLastError(), "cudaEventCreate");
     }
-    int rc = enqueue_coupling(s, C, force3, torque3, phase_ms ? ev : nullptr);
+    int rc = enqueue_coupling(s, C, force3, torque3, phase_ms ? ev : nullptr,
+                              density_has_boundary);
     if (!rc && b.nbodies > 0) {
         const size_t bytes = (size_t)b.nbodies * 12;
         cudaError_t e = cudaMemcpyAsync(force3, b.force3, bytes, cudaMemcpyDeviceToHost, s->stream);
@@ -1567,6 +1576,56 @@ int scene_couple_rigid_locked(pbf_scene* s, float dt, const float g[3]) {
 
 namespace {
 
+// Buffers of a two-way step: predicted positions, their cells, owner words
+// and bucket rows, per fluid particle.
+int ensure_two_way(pbf_scene* s) {
+    auto& b = s->bnd;
+    if (b.tw_mem && b.tw_cap >= s->n) return PBF_OK;
+    if (b.tw_mem) cudaFree(b.tw_mem);
+    b.tw_mem = nullptr;
+    const size_t c = (size_t)(s->n > 0 ? s->n : 1);
+    const size_t pb = align_up(c * 16, 256), cb = align_up(c * 16, 256), ob = align_up(c * 4, 256);
+    PBF_CUDA(cudaMalloc(&b.tw_mem, pb + cb + ob + c * 27 * 4));
+    unsigned char* m = static_cast<unsigned char*>(b.tw_mem);
+    b.tw_pred = reinterpret_cast<float4*>(m);
+    b.tw_cell = reinterpret_cast<int4*>(m + pb);
+    b.tw_own = reinterpret_cast<int*>(m + pb + cb);
+    b.tw_btab = reinterpret_cast<uint32_t*>(m + pb + cb + ob);
+    b.tw_cap = (int)c;
+    return PBF_OK;
+}
+
+// One PBF step with the Akinci boundary inside the density constraint
+// (pbf_settings.boundary_two_way): the boundary's world positions at the
+// step-start poses, the reference-bucket index over them, every fluid
+// particle's predicted cell classified against it, then the step.
+int two_way_step(pbf_scene* s, const StepConsts& C) {
+    auto& b = s->bnd;
+    int rc = ensure_boundary_grid(s, C.grid.nslots);
+    if (!rc) rc = ensure_two_way(s);
+    if (rc) return rc;
+    cudaStream_t st = s->stream;
+    cudaError_t e = boundary_xform(b.local, b.body, b.nb, b.body_pos, b.body_quat, b.nbodies,
+                                   b.world, st);
+    if (e == cudaSuccess) e = index_build(b.idx, b.world, nullptr, b.nb, C, b.sort, st);
+    if (e == cudaSuccess) e = predict_points(s->B.x, s->B.v, s->n, b.tw_pred, C, st);
+    QuerySet q{b.tw_cell, b.tw_own, b.tw_btab};
+    if (e == cudaSuccess) e = index_classify(q, b.tw_pred, s->n, b.idx, C, st);
+    if (e != cudaSuccess) return cuda_fail(e, "two-way boundary");
+    BoundaryGrid bg;
+    bg.spos = b.idx.spos;
+    bg.off = b.idx.off;
+    bg.kpos = b.idx.kpos;
+    bg.bend = b.idx.bend;
+    bg.own = b.tw_own;
+    bg.btab = b.tw_btab;
+    const int iters = s->settings.solver_iterations;
+    e = s->settings.exact_arithmetic
+            ? exact_enqueue_step(s->B, C, iters, s->sort, st, nullptr, &bg)
+            : fast_enqueue_step(s->B, C, iters, s->sort, st, nullptr, &bg);
+    return e == cudaSuccess ? PBF_OK : cuda_fail(e, "two-way step");
+}
+
 int check_coupling_args(pbf_scene* s, float* force3, float* torque3) {
     auto& b = s->bnd;
     if (b.nb > 0 && b.nbodies < b.needed_bodies)
@@ -1590,6 +1649,11 @@ int pbf_scene_step_coupled(pbf_scene* s, float dt, float* force3, float* torque3
     StepConsts C;
     rc = make_consts(s, dt, C);
     if (rc) return rc;
+    if (C.two_way && s->bnd.nb > 0) {
+        rc = two_way_step(s, C);
+        if (rc) return rc;
+        return couple_after_step(s, C, force3, torque3, nullptr, true);
+    }
     rc = run_steps(s, dt, 1);
     if (rc) return rc;
     return couple_after_step(s, C, force3, torque3);

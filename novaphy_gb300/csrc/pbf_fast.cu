@@ -8,8 +8,9 @@
 namespace pbf {
 
 cudaError_t fast_enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
-                               SortScratch& sort, cudaStream_t st, PhaseMarks* pm) {
-    return fast::enqueue_step(B, C, iters, sort, st, pm);
+                               SortScratch& sort, cudaStream_t st, PhaseMarks* pm,
+                               const BoundaryGrid* bg) {
+    return fast::enqueue_step(B, C, iters, sort, st, pm, bg);
 }
 
 cudaError_t fast_enqueue_batch(const StepBuffers& B, const BatchDesc& D, SortScratch& sort,

@@ -145,6 +145,14 @@ struct pbf_scene {
         void* sort_mem = nullptr;
         void* fq_mem = nullptr;    // fluid-query cells (per fluid particle)
         int fq_cap = 0;
+        // Two-way coupled steps: predicted fluid positions and their
+        // classification against the boundary index (per fluid particle).
+        void* tw_mem = nullptr;
+        int tw_cap = 0;
+        float4* tw_pred = nullptr;
+        int4* tw_cell = nullptr;
+        int* tw_own = nullptr;
+        uint32_t* tw_btab = nullptr;
         float4* local = nullptr;   // w = psi
         int* body = nullptr;
         float4* world = nullptr;   // w = psi

@@ -405,7 +405,14 @@ struct Grid {
     const uint32_t* __restrict__ spid;  // scene of each sorted particle (batches)
     uint32_t* moved;                     // per slot, see StepBuffers::moved
     uint32_t* lamnz;                     // per slot, see StepBuffers::lamnz
+    BoundaryGrid bg;                     // two-way coupled steps only
 };
+
+// The cell of sorted particle p against the boundary index (two-way steps).
+__device__ __forceinline__ int4 boundary_cell(const Grid& G, uint32_t p, const int4 cell) {
+    const uint32_t i = __float_as_uint(__ldg(&G.bg.sx[p].w));
+    return make_int4(cell.x, cell.y, cell.z, __ldg(G.bg.own + i));
+}
 
 __device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
     int4 c = G.scell[p];
@@ -812,6 +819,26 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     if (!coop)
         for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
                               [&](uint32_t q) { term(ld_step<kPersist>(xin + q)); });
+    if (G.bg.spos) {
+        // Two-way coupling (no counterpart in the reference): after the fluid
+        // terms, the boundary's Akinci density rho0 psi_b W and its gradient
+        // psi_b grad W (= (rho0 psi_b / rho0) grad W) in the boundary index's
+        // bucket order.  The boundary does not move, so it adds nothing to
+        // the sum of the neighbours' squared gradients.
+        for_each_candidate<4>(boundary_cell(G, p, cell), G.bg.off, G.bg.kpos, G.bg.bend,
+                              G.bg.btab, C, [&](uint32_t q) {
+                                  const float4 b = __ldg(G.bg.spos + q);
+                                  const float rx = xi.x - b.x, ry = xi.y - b.y, rz = xi.z - b.z;
+                                  const float r_sq = sqn(rx, ry, rz);
+                                  if (r_sq < C.cut) {
+                                      density += C.rho0 * b.w * poly6(r_sq, C);
+                                      const float c = spiky_coeff(r_sq, C);
+                                      gix += b.w * (c * rx);
+                                      giy += b.w * (c * ry);
+                                      giz += b.w * (c * rz);
+                                  }
+                              });
+    }
     sum_grad_sq += sqn(gix, giy, giz);
     const float Ci = density * C.inv_rho0 - 1.0f;
     const float lam = (Ci < 0.0f) ? 0.0f : -Ci / (sum_grad_sq + C.eps);
@@ -913,6 +940,24 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     if (walk && !coop)
         for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
                               [&](uint32_t q) { term(ld_step<kPersist>(xin + q)); });
+    if (G.bg.spos && xi.w != 0.0f) {
+        // Two-way coupling: the boundary's share of the position correction,
+        // lambda_i (rho0 psi_b) grad W, after the fluid terms (zero when
+        // lambda_i is).
+        for_each_candidate<4>(boundary_cell(G, p, cell), G.bg.off, G.bg.kpos, G.bg.bend,
+                              G.bg.btab, C, [&](uint32_t q) {
+                                  const float4 b = __ldg(G.bg.spos + q);
+                                  const float rx = xi.x - b.x, ry = xi.y - b.y, rz = xi.z - b.z;
+                                  const float r_sq = sqn(rx, ry, rz);
+                                  if (r_sq < C.cut) {
+                                      const float c = spiky_coeff(r_sq, C);
+                                      const float a = xi.w * (C.rho0 * b.w);
+                                      dx += a * (c * rx);
+                                      dy += a * (c * ry);
+                                      dz += a * (c * rz);
+                                  }
+                              });
+    }
     const float px = xi.x + dx * C.inv_rho0;
     const float py = xi.y + dy * C.inv_rho0;
     const float pz = xi.z + dz * C.inv_rho0;
@@ -1281,8 +1326,9 @@ k_debug_neighbors(const float4* __restrict__ xin, const float4* __restrict__ sx,
 
 inline int grid_of(int n, int b) { return (n + b - 1) / b; }
 
-inline Grid grid_view(const StepBuffers& B, const uint32_t* spid = nullptr) {
-    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved, B.lamnz};
+inline Grid grid_view(const StepBuffers& B, const uint32_t* spid = nullptr,
+                      const BoundaryGrid& bg = BoundaryGrid{}) {
+    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved, B.lamnz, bg};
 }
 
 // predict, sort by cell and by reference key, cell offsets, gather, reference
@@ -1439,14 +1485,18 @@ inline cudaError_t enqueue_passes(const StepBuffers& B, const Grid& G, int n, in
 }
 
 inline cudaError_t enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
-                                SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr) {
+                                SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr,
+                                const BoundaryGrid* bg = nullptr) {
     const int n = C.n;
     if (n <= 0) return cudaSuccess;
     cudaError_t e = enqueue_prefix(B, C, sort, st, pm);
     if (e != cudaSuccess) return e;
     StepConsts Ci = C;
     Ci.iters = iters;
-    return enqueue_passes(B, grid_view(B), n, iters, iters <= 0, C.vort_on != 0, C.vort_on == 0,
+    BoundaryGrid bgs = bg ? *bg : BoundaryGrid{};
+    if (bg) bgs.sx = B.sx;
+    return enqueue_passes(B, grid_view(B, nullptr, bgs), n, iters, iters <= 0, C.vort_on != 0,
+                          C.vort_on == 0,
                           C.xsph_on != 0, OneScene{Ci, StateRef{B.x, B.v, B.rho, B.lam, 0u, nullptr}}, st,
                           pm);
 }

@@ -6,10 +6,13 @@
 
 namespace pbf {
 
+// bg: the Akinci boundary of a two-way coupled step, else null.
 cudaError_t exact_enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
-                               SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr);
+                               SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr,
+                               const BoundaryGrid* bg = nullptr);
 cudaError_t fast_enqueue_step(const StepBuffers& B, const StepConsts& C, int iters,
-                              SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr);
+                              SortScratch& sort, cudaStream_t st, PhaseMarks* pm = nullptr,
+                              const BoundaryGrid* bg = nullptr);
 
 // One step of a batch of scenes (B holds the batch's scratch; the scenes'
 // state is reached through D.refs).

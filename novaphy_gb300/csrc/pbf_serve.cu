@@ -738,6 +738,10 @@ int open_impl(pbf_server* sv, const pbf_settings* st, int n, const float* x3, co
     if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n must be >= 0");
     rc = check_settings(st);
     if (rc) return rc;
+    if (st->boundary_two_way)
+        return fail(PBF_ERR_INVALID_ARG,
+                    "boundary_two_way is not served: served coupled scenes use the reference's "
+                    "one-way coupling");
     const uint32_t slots = grid_slots_for(*st, x3, n);
     size_t charge = charge_of(n, slots);
     if (cp) {

@@ -51,10 +51,26 @@ struct StepConsts {
     int clamp;
     float lo[3], hi[3];  // domain_lower + pr, domain_upper - pr (pbf_solver.cpp:105-107)
     int hash_compat;
+    int two_way;         // the boundary enters the constraint (coupled steps)
     int iters;           // Jacobi iterations of this scene
     uint32_t seg_begin;  // this scene's range in the key-sorted order of a batch
     uint32_t seg_end;
     GridDesc grid;
+};
+
+// The Akinci boundary of a two-way coupled step (pbf_settings.boundary_two_way):
+// the reference-bucket index over the boundary's world positions (spos.w =
+// psi), each fluid particle's classification against it (own, btab; indexed
+// by particle), and the sorted x (sx.w = particle index bits) that maps a
+// sorted position to its particle.  All null when the step has none.
+struct BoundaryGrid {
+    const float4* spos = nullptr;
+    const uint32_t* off = nullptr;
+    const uint32_t* kpos = nullptr;
+    const uint32_t* bend = nullptr;
+    const int* own = nullptr;
+    const uint32_t* btab = nullptr;
+    const float4* sx = nullptr;
 };
 
 // Device buffers of one step.  Arrays named s* are in sorted (cell) order.
