@@ -617,18 +617,24 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
     };
 
     // Phase 1b: the lane's support tests over the staged chunk, two
-    // candidates per paired operation, one mask word per 32 candidates.
-    auto test_chunk = [&]() {
-        const int words = (nst + 31) >> 5;
-        // Pad the last word with candidates that are never in support.
-        for (int k = nst + lane; k < (words << 5); k += 32) {
-            sm.sx[k] = __int_as_float(0x7f800000);
-            sm.sy[k] = 0.0f;
-            sm.sz[k] = 0.0f;
-            sm.sw[k] = 0.0f;
-            sm.c[k] = 0;
+    // candidates per paired operation, one mask word per 32 candidates.  Only
+    // whole words are tested until the walk ends: the last partial word's
+    // candidates move to the front of the stage (their list positions stay
+    // where they are, at base + k) and wait for the next chunk, so a tested
+    // word is padded only at the very end of the walk.
+    auto test_chunk = [&](bool last) {
+        const int words = last ? (nst + 31) >> 5 : nst >> 5;
+        if (last) {
+            // Pad the last word with candidates that are never in support.
+            for (int k = nst + lane; k < (words << 5); k += 32) {
+                sm.sx[k] = __int_as_float(0x7f800000);
+                sm.sy[k] = 0.0f;
+                sm.sz[k] = 0.0f;
+                sm.sw[k] = 0.0f;
+                sm.c[k] = 0;
+            }
+            __syncwarp();
         }
-        __syncwarp();
         for (int wd = 0; wd < words; ++wd) {
             const int k0 = wd << 5;
             uint32_t allowed = full;
@@ -669,10 +675,33 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
             sm.mask[(base >> 5) + wd][lane] = bits;
             cnt += __popc(bits);
         }
-        base += words << 5;
-        nst = 0;
+        // The untested rest (fewer than 32) moves to the front of the stage.
+        const int rest = last ? 0 : nst - (words << 5);
+        float kx = 0.0f, ky = 0.0f, kz = 0.0f, kw = 0.0f;
+        unsigned char kc = 0;
+        uint32_t kq = 0u;
+        if (lane < rest) {
+            const int k = (words << 5) + lane;
+            kx = sm.sx[k];
+            ky = sm.sy[k];
+            kz = sm.sz[k];
+            kw = sm.sw[k];
+            kc = sm.c[k];
+            kq = sm.q[base + k];
+        }
         __syncwarp();
+        base += words << 5;
         if (base > CAP - CH) evaluate();
+        if (lane < rest) {
+            sm.sx[lane] = kx;
+            sm.sy[lane] = ky;
+            sm.sz[lane] = kz;
+            sm.sw[lane] = kw;
+            sm.c[lane] = kc;
+            sm.q[base + lane] = kq;
+        }
+        nst = rest;
+        __syncwarp();
     };
 
     for (int rr = 0; rr < 9; ++rr) {
@@ -714,15 +743,15 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
                 sm.c[k] = (unsigned char)((q >= b1) + (q >= b2) + (q >= b3) + (q >= b4));
             }
             nst += __popc(m);
-            if (nst > CH - 32) {
+            if (nst >= 32) {
                 __syncwarp();
-                test_chunk();
+                test_chunk(false);
             }
         }
     }
     if (nst > 0) {
         __syncwarp();
-        test_chunk();
+        test_chunk(true);
     }
     if (base > 0) evaluate();
 }
