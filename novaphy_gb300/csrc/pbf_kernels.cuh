@@ -498,7 +498,9 @@ constexpr int kPassMinBlocks = U == 8 ? 8 : 1;
 // Shared memory of a kernel's warps: real for the kernels of a single large
 // scene (those with the 8-way row loop, see kBigScene), one byte otherwise.
 // Small scenes and batches keep the one-thread walk: the shared memory costs
-// them occupancy, and many small scenes side by side measured slower with it.
+// them occupancy (a batch of 1,024 small scenes ran at 94 M particle-steps/s
+// with the cooperative walk against 108 M without), and many small scenes
+// side by side on their own streams measured slower with it too.
 template <class P, int BS, bool kExtra, int U>
 struct CoopBlock {
     static constexpr bool kOn = std::is_same<P, OneScene>::value && U == 8;
@@ -520,11 +522,13 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 
 // Warp-collective (every lane of the warp must call it): whether the warp
 // walks cooperatively, and its row.  `cell` is the lane's step-start cell
-// with w = its owner row (0 = clean).
+// with w = its owner row (0 = clean); `sid` its scene (0 for a single scene):
+// the lanes must share one scene, whose grid is Gd.
 __device__ __forceinline__ bool coop_row(bool active, const int4 cell, const GridDesc& Gd,
-                                         CoopRow& R) {
+                                         CoopRow& R, uint32_t sid) {
     const unsigned full = 0xffffffffu;
     if (!__all_sync(full, active)) return false;
+    if (!__all_sync(full, sid == __shfl_sync(full, sid, 0))) return false;
     const int cy0 = __shfl_sync(full, cell.y, 0);
     const int cz0 = __shfl_sync(full, cell.z, 0);
     if (!__all_sync(full, cell.w == 0 && cell.y == cy0 && cell.z == cz0)) return false;
@@ -819,7 +823,7 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     }
     CoopRow R;
     bool coop = false;
-    if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R);
+    if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R, scene_at(G, pa));
     if (!live) return;
     const float4 xi = xin[p];
     float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
@@ -935,7 +939,7 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     // lambda test leaves out, so they list nothing.
     CoopRow R;
     bool coop = false;
-    if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R);
+    if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R, scene_at(G, pa));
     if (!live) return;
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
     auto term = [&](const float4& xj) {
@@ -1139,7 +1143,7 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
     const int4 cell = cell_at(G, pa);
     CoopRow R;
     bool coop = false;
-    if constexpr (B::kOn) coop = coop_row(live && C.xsph_on, cell, C.grid, R);
+    if constexpr (B::kOn) coop = coop_row(live && C.xsph_on, cell, C.grid, R, scene_at(G, pa));
     if (!live) return;
     const float4 xi = xin[p];
     const float4 vi = sv[p];
@@ -1194,7 +1198,7 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
     const int4 cell = cell_at(G, pa);
     CoopRow R;
     bool coop = false;
-    if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R);
+    if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R, scene_at(G, pa));
     if (!live) return;
     const float4 xi = xin[p];
     const float4 vi = sv[p];
@@ -1259,7 +1263,7 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     const int4 cell = cell_at(G, pa);
     CoopRow R;
     bool coop = false;
-    if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R);
+    if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R, scene_at(G, pa));
     if (!live) return;
     const float4 xi = xin[p];
     const float4 wi = som[p];
