@@ -489,11 +489,10 @@ struct CoopSmem {
     uint32_t mask[(kCap + 31) / 32][32];  // mask[w][lane] bit b: survivor 32 w + b is a term of the lane
 };
 
-// Blocks per SM the neighbour-pass kernels are compiled for: eight for the
-// cooperative single-scene kernels (64 registers; their shared memory fits
-// eight blocks), the compiler's choice for the others.
-template <int U>
-constexpr int kPassMinBlocks = U == 8 ? 8 : 1;
+// Blocks per SM the neighbour-pass kernels are compiled for: 32 warps per SM
+// (64 registers a thread), which their shared memory also fits.
+template <int BS>
+constexpr int kPassMinBlocks = 1024 / BS;
 
 // Shared memory of a kernel's warps: real for the kernels of a single large
 // scene (those with the 8-way row loop, see kBigScene), one byte otherwise.
@@ -881,7 +880,7 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
 }
 
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<BS>)
 k_density_lambda(const float4* __restrict__ xin, float4* __restrict__ xout, float* __restrict__ srho,
                  int it, int n, const Grid G, const P prm) {
     using B = CoopBlock<P, BS, false, U>;
@@ -1003,7 +1002,7 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
 }
 
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<BS>)
 k_delta(const float4* __restrict__ xin, float4* __restrict__ xout, const float4* __restrict__ sx,
         const float* __restrict__ srho, float4* __restrict__ sv, int it, int n, const Grid G,
         const P prm) {
@@ -1130,7 +1129,7 @@ __device__ __forceinline__ void commit(uint32_t p, float px, float py, float pz,
 // apply_xsph_viscosity (pbf_solver.cpp:225-250) + commit, no vorticity.
 // With skip_vort set, scenes with vorticity are left to the vorticity pair.
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<BS>)
 k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, const float4* __restrict__ sx,
               const float* __restrict__ srho, int n, int skip_vort, const Grid G, const P prm) {
     using B = CoopBlock<P, BS, true, U>;
@@ -1185,7 +1184,7 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
 //   omega_i = sum_j (m/rho_j') spiky_grad(x*_i - x*_j) x (v_j - v_i),
 // the SPH curl (Macklin & Mueller 2013, section 5, with its volume factor).
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<BS>)
 k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, float4* __restrict__ sv2,
              float4* __restrict__ som, int n, const Grid G, const P prm) {
     using B = CoopBlock<P, BS, true, U>;
@@ -1248,7 +1247,7 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
 //   eta_i = sum_j (m/rho_j') (|omega_j| - |omega_i|) spiky_grad(x*_i - x*_j),
 //   N = eta / |eta|,  v += dt * eps * (N x omega_i).
 template <int BS, class P, int U = 4>
-__global__ void __launch_bounds__(BS, kPassMinBlocks<U>)
+__global__ void __launch_bounds__(BS, kPassMinBlocks<BS>)
 k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv,
                    const float4* __restrict__ sv2, const float4* __restrict__ som,
                    const float4* __restrict__ sx, const float* __restrict__ srho, int n,
