@@ -357,39 +357,45 @@ k_classify(const int4* __restrict__ qcell, int nq, const int4* __restrict__ scel
     const uint32_t sc = (active && qsid) ? qsid[p] : 0xffffffffu;
     const unsigned long long kxy =
         ((unsigned long long)(unsigned)cell.x << 32) | (unsigned long long)(unsigned)cell.y;
-    const uint32_t same = __match_any_sync(0xffffffffu, kxy) &
-                          __match_any_sync(0xffffffffu, (unsigned)cell.z) &
-                          __match_any_sync(0xffffffffu, sc) & __ballot_sync(0xffffffffu, active);
+    const unsigned full = 0xffffffffu;
+    const uint32_t same = __match_any_sync(full, kxy) & __match_any_sync(full, (unsigned)cell.z) &
+                          __match_any_sync(full, sc) & __ballot_sync(full, active);
     const int leader = same ? __ffs(same) - 1 : lane;
-    int dirty = 0;
-    if (active && lane == leader && prm.at(qsid, p).hash_compat) {
-        const StepConsts& C = prm.at(qsid, p);
-        uint32_t tab[27];
-        int m = 0;
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx, ++m) {
-                    const int nx = cell.x + dx, ny = cell.y + dy, nz = cell.z + dz;
-                    const unsigned long long k = ref_hash(nx, ny, nz);
-                    const uint32_t lb = key_lower_bound(rsorted, C.seg_begin, C.seg_end, k);
-                    if (lb < C.seg_end && __ldg(rsorted + lb) == k) {
-                        tab[m] = lb;
-                        const uint32_t e = __ldg(bend + lb);
-                        const int4 c0 = scell[__ldg(kpos + lb)];
-                        if ((e & kImpureBit) || c0.x != nx || c0.y != ny || c0.z != nz) dirty = 1;
-                    } else {
-                        tab[m] = kNoBucket;
-                    }
-                    if (slot_alias[slot_of(nx, ny, nz, C.grid)]) dirty = 1;
+    // Each distinct cell of the warp in turn (its first lane is the owner of
+    // its bucket row); lanes 0..26 look up one neighbour bucket each, m =
+    // 9 (dz + 1) + 3 (dy + 1) + (dx + 1), so the 27 searches run side by side.
+    uint32_t todo = __ballot_sync(full, active && lane == leader);
+    int own = 0;
+    while (todo) {
+        const int L = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        const uint32_t lp = __shfl_sync(full, p, L);
+        const int cx = __shfl_sync(full, cell.x, L);
+        const int cy = __shfl_sync(full, cell.y, L);
+        const int cz = __shfl_sync(full, cell.z, L);
+        const uint32_t grp = __shfl_sync(full, same, L);
+        const StepConsts& C = prm.at(qsid, lp);
+        int dirty = 0;
+        if (C.hash_compat) {
+            uint32_t t = kNoBucket;
+            if (lane < 27) {
+                const int nx = cx + lane % 3 - 1, ny = cy + (lane / 3) % 3 - 1, nz = cz + lane / 9 - 1;
+                const unsigned long long k = ref_hash(nx, ny, nz);
+                const uint32_t lb = key_lower_bound(rsorted, C.seg_begin, C.seg_end, k);
+                if (lb < C.seg_end && __ldg(rsorted + lb) == k) {
+                    t = lb;
+                    const uint32_t e = __ldg(bend + lb);
+                    const int4 c0 = scell[__ldg(kpos + lb)];
+                    if ((e & kImpureBit) || c0.x != nx || c0.y != ny || c0.z != nz) dirty = 1;
                 }
-        if (dirty) {
-            uint32_t* row = btab + (size_t)p * 27u;
-            for (int k = 0; k < 27; ++k) row[k] = tab[k];
+                if (slot_alias[slot_of(nx, ny, nz, C.grid)]) dirty = 1;
+            }
+            dirty = __any_sync(full, dirty);
+            if (dirty && lane < 27) btab[(size_t)lp * 27u + (uint32_t)lane] = t;
         }
+        if ((grp >> lane) & 1u) own = dirty ? (int)(lp + 1u) : 0;
     }
-    const int d = __shfl_sync(0xffffffffu, dirty, leader);
-    const uint32_t owner = __shfl_sync(0xffffffffu, p, leader);
-    if (active) qown[p] = d ? (int)(owner + 1u) : 0;
+    if (active) qown[p] = own;
 }
 
 // ---------------------------------------------------------------------------
