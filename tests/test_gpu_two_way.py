@@ -114,3 +114,52 @@ def test_batches_and_servers_refuse_two_way(port):
         srv.open_scene(capi.default_settings(**dict(w.settings, boundary_two_way=1)), w.x, w.v,
                        w.mass, w.gravity)
     srv.close()
+
+
+@pytest.mark.parametrize("monitor", [False, True])
+def test_fluid_world_two_way(monitor):
+    """PBFSettings.boundary_two_way through FluidWorld: a block dropped on a
+    static box is held off it; with the performance monitor on, the world
+    still steps through the whole coupled step (the profiled phases cannot
+    split a two-way step) and gives the same bits."""
+    import novaphy_gb300 as nv
+
+    def world(two_way, mon):
+        mb = nv.ModelBuilder()
+        bi = mb.add_body(nv.RigidBody.make_static(),
+                         nv.Transform.from_translation(np.array([0.5, 0.5, 0.15], np.float32)))
+        mb.add_shape(nv.CollisionShape.make_box(np.array([0.2, 0.2, 0.1], np.float32), bi))
+        blk = nv.FluidBlockDef()
+        blk.lower = np.array([0.4125, 0.4125, 0.3625], np.float32)
+        blk.upper = np.array([0.5875, 0.5875, 0.5], np.float32)
+        blk.particle_spacing = R
+        st = nv.PBFSettings()
+        st.kernel_radius = 4 * R
+        st.use_domain_bounds = True
+        st.domain_lower = [0.0, 0.0, 0.0]
+        st.domain_upper = [1.0, 1.0, 1.0]
+        st.particle_radius = R / 2
+        st.boundary_two_way = two_way
+        w = nv.FluidWorld(mb.build(), [blk], nv.SolverSettings(), st, 1.0)
+        w.set_gravity([0.0, 0.0, -9.81])
+        w.performance_monitor.enabled = mon
+        return w
+
+    peaks, finals = {}, {}
+    for tw in (False, True):
+        w = world(tw, monitor)
+        counts = []
+        for k in range(90):
+            w.step(1.0 / 120.0)
+            if k % 15 == 14:
+                counts.append(int(inside_box(w.fluid_state.positions_array).sum()))
+        peaks[tw] = max(counts)
+        finals[tw] = w.fluid_arrays()["positions"].copy()
+    n = len(finals[True])
+    assert peaks[False] > n // 2, peaks
+    assert peaks[True] <= 0.08 * n, peaks
+    if monitor:
+        w = world(True, False)
+        for _ in range(90):
+            w.step(1.0 / 120.0)
+        assert np.array_equal(w.fluid_arrays()["positions"], finals[True])
