@@ -70,6 +70,12 @@ typedef struct pbf_settings {
                              so the fluid is held off the bodies.  No
                              counterpart in the reference; single coupled
                              scenes only (batches and servers refuse it). */
+    float boundary_friction; /* with boundary_two_way: XSPH-style friction of the
+                                fluid against the bodies' surface velocity,
+                                v_i += c sum_b psi_b (v_b - v_i) W_ib, before the
+                                fluid's own XSPH (0, the default, disables it;
+                                set the bodies' velocities with
+                                pbf_scene_set_body_velocities) */
 } pbf_settings;
 
 /* Field selectors for pbf_scene_read / pbf_scene_write. */
@@ -183,6 +189,13 @@ int pbf_scene_set_boundary(pbf_scene* scene, int nb, const float* local3, const 
  * fluid_world.cpp:141).  nbodies must cover every body the boundary names. */
 int pbf_scene_set_bodies(pbf_scene* scene, int nbodies, const float* pos3, const float* quat4,
                          const int* dynamic);
+
+/* Linear and angular velocities (world frame) of those bodies, for the
+ * boundary friction of two-way coupled steps (pbf_settings.boundary_friction):
+ * a boundary particle moves with v + w x (x_b - p) of its body, a world-owned
+ * one not at all.  Zero until set.  No counterpart in the reference. */
+int pbf_scene_set_body_velocities(pbf_scene* scene, int nbodies, const float* lin3,
+                                  const float* ang3);
 
 /* The fluid part of FluidWorld::step (fluid_world.cpp:57-81): boundary world
  * positions from the current body poses, one PBF step, boundary density added

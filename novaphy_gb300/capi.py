@@ -58,6 +58,7 @@ class Settings(C.Structure):
         ("exact_arithmetic", C.c_int),
         ("hash_compat", C.c_int),
         ("boundary_two_way", C.c_int),
+        ("boundary_friction", C.c_float),
     ]
 
 
@@ -116,6 +117,7 @@ def load() -> C.CDLL:
         "pbf_scene_replay_timed": ([vp, vp, C.c_float, C.c_int, f32p], C.c_int),
         "pbf_scene_set_boundary": ([vp, C.c_int, vp, vp, vp], C.c_int),
         "pbf_scene_set_bodies": ([vp, C.c_int, vp, vp, vp], C.c_int),
+        "pbf_scene_set_body_velocities": ([vp, C.c_int, vp, vp], C.c_int),
         "pbf_scene_step_coupled": ([vp, C.c_float, vp, vp], C.c_int),
         "pbf_scene_couple": ([vp, C.c_float, vp, vp], C.c_int),
         "pbf_scene_read_boundary": ([vp, vp], C.c_int),
@@ -282,6 +284,15 @@ class Scene:
         quat = _f32(quat, (-1, 4))
         dyn = np.ascontiguousarray(dynamic, np.int32)
         check(self._L.pbf_scene_set_bodies(self._h, len(pos), _ptr(pos), _ptr(quat), _ptr(dyn)))
+
+    def set_body_velocities(self, lin, ang):
+        """World-frame linear and angular body velocities for the boundary
+        friction of two-way steps (Settings.boundary_friction)."""
+        lin = _f32(lin, (-1, 3))
+        ang = _f32(ang, (-1, 3))
+        if len(ang) != len(lin):
+            raise ValueError("lin and ang must have one row per body")
+        check(self._L.pbf_scene_set_body_velocities(self._h, len(lin), _ptr(lin), _ptr(ang)))
 
     def step_coupled(self, dt, force, torque):
         """One coupled fluid step; returns (force, torque) accumulated onto the inputs."""

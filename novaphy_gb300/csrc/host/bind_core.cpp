@@ -469,6 +469,7 @@ PYBIND11_MODULE(_core, m) {
         .def_readwrite("exact_arithmetic", &PBFSettings::exact_arithmetic)
         .def_readwrite("hash_compat", &PBFSettings::hash_compat)
         .def_readwrite("boundary_two_way", &PBFSettings::boundary_two_way)
+        .def_readwrite("boundary_friction", &PBFSettings::boundary_friction)
         .def("particle_mass", &PBFSettings::particle_mass, py::arg("spacing"));
 
     py::class_<PBFSolver>(m, "PBFSolver")

@@ -44,6 +44,7 @@ static int device_index() {
     s.exact_arithmetic = exact_arithmetic ? 1 : 0;
     s.hash_compat = hash_compat ? 1 : 0;
     s.boundary_two_way = boundary_two_way ? 1 : 0;
+    s.boundary_friction = boundary_friction;
     return s;
 }
 
@@ -791,9 +792,24 @@ void FluidWorld::step(float dt) {
                 f[(size_t)k] = state_.forces[(size_t)k];
                 t[(size_t)k] = state_.torques[(size_t)k];
             }
-            if (!boundary_.empty() && needed > 0)
+            if (!boundary_.empty() && needed > 0) {
                 check_pbf(pbf_scene_set_bodies(scene_, needed, pos.data(), quat.data(),
                                                dyn.data()));
+                if (pbf_.boundary_two_way && pbf_.boundary_friction != 0.0f) {
+                    std::vector<float> lin(3 * (size_t)needed, 0.0f), ang(3 * (size_t)needed, 0.0f);
+                    for (int k = 0; k < needed && k < model_.num_bodies(); ++k) {
+                        const Vec3& l = state_.linear_velocities[(size_t)k];
+                        const Vec3& a = state_.angular_velocities[(size_t)k];
+                        lin[3 * k] = l.x;
+                        lin[3 * k + 1] = l.y;
+                        lin[3 * k + 2] = l.z;
+                        ang[3 * k] = a.x;
+                        ang[3 * k + 1] = a.y;
+                        ang[3 * k + 2] = a.z;
+                    }
+                    check_pbf(pbf_scene_set_body_velocities(scene_, needed, lin.data(), ang.data()));
+                }
+            }
             float* fp = needed ? &f[0].x : nullptr;
             float* tp = needed ? &t[0].x : nullptr;
             if (!monitor_.enabled || pbf_.boundary_two_way) {

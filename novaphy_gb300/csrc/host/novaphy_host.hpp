@@ -147,6 +147,7 @@ struct PBFSettings {
     bool exact_arithmetic = true;
     bool hash_compat = true;
     bool boundary_two_way = false;  // no counterpart in the reference (pbf_settings)
+    float boundary_friction = 0.0f;  // two-way only; no counterpart in the reference
     float particle_mass(float spacing) const { return rest_density * spacing * spacing * spacing; }
     ::pbf_settings to_c() const;
 };

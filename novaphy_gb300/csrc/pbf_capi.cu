@@ -379,6 +379,7 @@ int scene_consts(const pbf_scene* s, float dt, StepConsts& C) {
     }
     C.hash_compat = st.hash_compat ? 1 : 0;
     C.two_way = st.boundary_two_way ? 1 : 0;
+    C.bfric = st.boundary_two_way ? st.boundary_friction : 0.0f;
     C.iters = st.solver_iterations;
     C.seg_begin = 0;
     C.seg_end = (uint32_t)s->n;
@@ -574,6 +575,7 @@ int pbf_default_settings(pbf_settings* out) {
     d.exact_arithmetic = 1;
     d.hash_compat = 1;
     d.boundary_two_way = 0;
+    d.boundary_friction = 0.0f;
     *out = d;
     return PBF_OK;
 }
@@ -1254,12 +1256,14 @@ int pbf_scene_set_boundary(pbf_scene* s, int nb, const float* local3, const int*
     const size_t s16 = align_up((size_t)cap * 16, 256), s4 = align_up((size_t)(cap + 1) * 4, 256),
                  sl = align_up(std::max<size_t>(lst.size(), 1) * 4, 256),
                  s12 = align_up((size_t)cap * 12, 256);
-    const size_t need = 2 * s16 + 2 * s4 + sl + 2 * s12;
+    const size_t need = 4 * s16 + 2 * s4 + sl + 2 * s12;
     PBF_CUDA(cudaMalloc(&b.body_mem, need));
     char* p = reinterpret_cast<char*>(b.body_mem);
     auto take = [&](size_t n) { char* r = p; p += n; return r; };
     b.body_pos = reinterpret_cast<float4*>(take(s16));
     b.body_quat = reinterpret_cast<float4*>(take(s16));
+    b.body_lin = reinterpret_cast<float4*>(take(s16));
+    b.body_ang = reinterpret_cast<float4*>(take(s16));
     b.body_dyn = reinterpret_cast<int*>(take(s4));
     b.list_off = reinterpret_cast<int*>(take(s4));
     b.list = reinterpret_cast<int*>(take(sl));
@@ -1298,6 +1302,30 @@ int pbf_scene_set_bodies(pbf_scene* s, int nbodies, const float* pos3, const flo
     }
     PBF_CUDA(cudaStreamSynchronize(s->stream));
     b.nbodies = nbodies;
+    return PBF_OK;
+}
+
+int pbf_scene_set_body_velocities(pbf_scene* s, int nbodies, const float* lin3,
+                                  const float* ang3) {
+    if (!s || nbodies < 0 || (nbodies > 0 && (!lin3 || !ang3)))
+        return fail(PBF_ERR_INVALID_ARG, "bad body velocity arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    DeviceGuard dg(s->device);
+    auto& b = s->bnd;
+    if (!b.body_mem) return fail(PBF_ERR_INVALID_ARG, "set the boundary particles first");
+    if (nbodies < b.needed_bodies)
+        return fail(PBF_ERR_INVALID_ARG, "fewer bodies than the boundary particles reference");
+    nbodies = b.needed_bodies;
+    std::vector<float4> lv(nbodies), av(nbodies);
+    for (int k = 0; k < nbodies; ++k) {
+        lv[k] = make_float4(lin3[3 * k], lin3[3 * k + 1], lin3[3 * k + 2], 0.0f);
+        av[k] = make_float4(ang3[3 * k], ang3[3 * k + 1], ang3[3 * k + 2], 0.0f);
+    }
+    if (nbodies > 0) {
+        PBF_CUDA(cudaMemcpyAsync(b.body_lin, lv.data(), (size_t)nbodies * 16, cudaMemcpyHostToDevice, s->stream));
+        PBF_CUDA(cudaMemcpyAsync(b.body_ang, av.data(), (size_t)nbodies * 16, cudaMemcpyHostToDevice, s->stream));
+    }
+    PBF_CUDA(cudaStreamSynchronize(s->stream));
     return PBF_OK;
 }
 
@@ -1619,6 +1647,12 @@ int two_way_step(pbf_scene* s, const StepConsts& C) {
     bg.bend = b.idx.bend;
     bg.own = b.tw_own;
     bg.btab = b.tw_btab;
+    bg.sidx = b.idx.sidx;
+    bg.body = b.body;
+    bg.nbodies = b.nbodies;
+    bg.body_pos = b.body_pos;
+    bg.body_lin = b.body_lin;
+    bg.body_ang = b.body_ang;
     const int iters = s->settings.solver_iterations;
     e = s->settings.exact_arithmetic
             ? exact_enqueue_step(s->B, C, iters, s->sort, st, nullptr, &bg)

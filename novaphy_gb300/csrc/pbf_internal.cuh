@@ -162,6 +162,8 @@ struct pbf_scene {
         int4* fq_cell = nullptr;
         float4* body_pos = nullptr;
         float4* body_quat = nullptr;
+        float4* body_lin = nullptr;  // body velocities (two-way boundary friction)
+        float4* body_ang = nullptr;
         int* body_dyn = nullptr;
         int* list_off = nullptr;
         int* list = nullptr;

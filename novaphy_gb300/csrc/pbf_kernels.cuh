@@ -1132,6 +1132,46 @@ __device__ __forceinline__ void commit(uint32_t p, float px, float py, float pz,
     R.lam[l] = lam;
 }
 
+// Boundary friction of two-way steps (StepConsts::bfric), one thread per
+// cell-sorted particle after the velocity update and before XSPH:
+//   v_i += bfric * sum_b psi_b (v_b - v_i) W(x*_i - x_b),
+// an XSPH term against the surface velocity v_b = v_k + w_k x (x_b - p_k) of
+// boundary particle b's body k (zero for world-owned particles), over the
+// boundary buckets of the particle's cell.  Each thread reads and writes only
+// its own velocity.
+__global__ void __launch_bounds__(kBlock)
+k_boundary_friction(const float4* __restrict__ xin, float4* __restrict__ sv, int n, const Grid G,
+                    const StepConsts C) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)n) return;
+    const float4 xi = xin[p];
+    const float4 vi = sv[p];
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    for_each_candidate<4>(boundary_cell(G, p, cell_at(G, p)), G.bg.off, G.bg.kpos, G.bg.bend,
+                          G.bg.btab, C, [&](uint32_t q) {
+                              const float4 b = __ldg(G.bg.spos + q);
+                              const float rx = xi.x - b.x, ry = xi.y - b.y, rz = xi.z - b.z;
+                              const float r_sq = sqn(rx, ry, rz);
+                              if (r_sq >= C.h2) return;
+                              const int k = __ldg(G.bg.body + __ldg(G.bg.sidx + q));
+                              float ux = 0.0f, uy = 0.0f, uz = 0.0f;
+                              if (k >= 0 && k < G.bg.nbodies) {
+                                  const float4 c = __ldg(G.bg.body_pos + k);
+                                  const float4 l = __ldg(G.bg.body_lin + k);
+                                  const float4 a = __ldg(G.bg.body_ang + k);
+                                  const float dx = b.x - c.x, dy = b.y - c.y, dz = b.z - c.z;
+                                  ux = l.x + (a.y * dz - a.z * dy);
+                                  uy = l.y + (a.z * dx - a.x * dz);
+                                  uz = l.z + (a.x * dy - a.y * dx);
+                              }
+                              const float w = b.w * poly6(r_sq, C);
+                              fx += (ux - vi.x) * w;
+                              fy += (uy - vi.y) * w;
+                              fz += (uz - vi.z) * w;
+                          });
+    sv[p] = make_float4(vi.x + C.bfric * fx, vi.y + C.bfric * fy, vi.z + C.bfric * fz, vi.w);
+}
+
 // apply_xsph_viscosity (pbf_solver.cpp:225-250) + commit, no vorticity.
 // With skip_vort set, scenes with vorticity are left to the vorticity pair.
 template <int BS, class P, int U = 4>
@@ -1486,6 +1526,12 @@ inline cudaError_t enqueue_passes_bs(const StepBuffers& B, const Grid& G, int n,
     if (any_zero_iters) {
         k_velocity<BS><<<nb, BS, 0, st>>>(B.xa, B.sx, B.srho, B.sv, n, G, prm);
         if (pm) pm->mark(kPhaseDelta, 1, st);
+    }
+    if constexpr (std::is_same<P, OneScene>::value) {
+        if (G.bg.spos && prm.C.bfric != 0.0f) {
+            k_boundary_friction<<<nb, BS, 0, st>>>(B.xa, B.sv, n, G, prm.C);
+            if (pm) pm->mark(kPhaseXsph, 1, st);
+        }
     }
     if constexpr (std::is_same<P, OneScene>::value) {
         if (n >= kBigScene)

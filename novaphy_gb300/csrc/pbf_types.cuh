@@ -52,6 +52,7 @@ struct StepConsts {
     float lo[3], hi[3];  // domain_lower + pr, domain_upper - pr (pbf_solver.cpp:105-107)
     int hash_compat;
     int two_way;         // the boundary enters the constraint (coupled steps)
+    float bfric;         // boundary friction coefficient of two-way steps (0: none)
     int iters;           // Jacobi iterations of this scene
     uint32_t seg_begin;  // this scene's range in the key-sorted order of a batch
     uint32_t seg_end;
@@ -71,6 +72,14 @@ struct BoundaryGrid {
     const int* own = nullptr;
     const uint32_t* btab = nullptr;
     const float4* sx = nullptr;
+    // Boundary friction: the index's sorted-to-original map, each original
+    // boundary particle's body, and the bodies' poses and velocities.
+    const uint32_t* sidx = nullptr;
+    const int* body = nullptr;
+    int nbodies = 0;
+    const float4* body_pos = nullptr;
+    const float4* body_lin = nullptr;
+    const float4* body_ang = nullptr;
 };
 
 // Device buffers of one step.  Arrays named s* are in sorted (cell) order.

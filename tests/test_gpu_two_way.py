@@ -12,7 +12,10 @@ output to match; the tests pin what the extension must keep:
   coupling and falls through it with the reference's one-way coupling;
 * it is deterministic;
 * batches and the serving loop, which step the fluid without its boundary,
-  refuse it.
+  refuse it;
+* boundary friction (pbf_settings.boundary_friction): zero is a no-op; a
+  positive coefficient drags the fluid along a moving or spinning body's
+  surface and slows fluid sliding over still boundaries.
 """
 import numpy as np
 import pytest
@@ -163,3 +166,131 @@ def test_fluid_world_two_way(monitor):
         for _ in range(90):
             w.step(1.0 / 120.0)
         assert np.array_equal(w.fluid_arrays()["positions"], finals[True])
+
+
+# ---- boundary friction (pbf_settings.boundary_friction, two-way steps only) ----
+
+def mean_velocity(sc):
+    return sc.state()[1].mean(0)
+
+
+def test_zero_friction_is_a_no_op(port):
+    """boundary_friction = 0 launches nothing: body velocities do not matter."""
+    runs = []
+    for vel in (False, True):
+        w, sc = box_scene(port, 1, boundary_friction=0.0)
+        if vel:
+            sc.set_body_velocities([[1.0, 0.0, 0.0]], [[0.0, 0.0, 3.0]])
+        runs.append(run(sc, w, 20)[0])
+        sc.close()
+    for u, v in zip(*runs):
+        assert np.array_equal(u.view(np.uint32), v.view(np.uint32))
+
+
+def test_friction_drags_the_fluid_along_a_moving_surface(port):
+    """The box stays put but its surface moves at 0.5 m/s in x (a conveyor):
+    with friction the block resting on it picks up x momentum, short of the
+    surface's speed on average, without it next to none (splashing particles
+    move faster than the surface either way, so only means are compared)."""
+    mean = {}
+    for c in (0.0, 0.5):
+        w, sc = box_scene(port, 1, boundary_friction=c)
+        sc.set_body_velocities([[0.5, 0.0, 0.0]], [[0.0, 0.0, 0.0]])
+        run(sc, w, 40)
+        x, v = sc.state()[:2]
+        assert np.isfinite(v).all()
+        mean[c] = float(v[:, 0].mean())
+        sc.close()
+    assert abs(mean[0.0]) < 0.05, mean
+    assert 0.2 < mean[0.5] < 0.5, mean
+
+
+def test_friction_spins_the_fluid_on_a_spinning_body(port):
+    """A box spinning about z (w = 2 rad/s) drags the fluid on its top into
+    rotation: positive angular momentum about the box axis with friction,
+    none without."""
+    lz = {}
+    for c in (0.0, 0.5):
+        w, sc = box_scene(port, 1, boundary_friction=c)
+        sc.set_body_velocities([[0.0, 0.0, 0.0]], [[0.0, 0.0, 2.0]])
+        run(sc, w, 40)
+        x, v = sc.state()[:2]
+        d = x - BOX_POS[0]
+        lz[c] = float((d[:, 0] * v[:, 1] - d[:, 1] * v[:, 0]).mean())
+        sc.close()
+    assert abs(lz[0.0]) < 5e-3, lz
+    assert lz[0.5] > 0.015, lz
+
+
+def test_friction_against_world_owned_particles(port):
+    """World-owned boundary particles (body -1) have zero surface velocity:
+    a block sliding over them at 0.5 m/s is slowed by friction."""
+    mean = {}
+    for c in (0.0, 0.5):
+        w = workloads.dam_break((8, 8, 6), R, (1.0, 1.0, 1.0), dt=1.0 / 120.0, seed=0,
+                                vorticity=0.0)
+        w.x = (w.x + np.array([0.4, 0.4, 0.26], np.float32)).astype(np.float32)
+        w.v[:, 0] = 0.5
+        local = port.sample_box(HALF, (0, 0, 0), IDENT, np.float32(R)).astype(np.float32)
+        world = (local + BOX_POS[0]).astype(np.float32)
+        psi = port.boundary_volumes(world, np.float32(4 * R)).astype(np.float32)
+        st = dict(w.settings, boundary_two_way=1, boundary_friction=c, corr_k=0.001,
+                  corr_delta_q=0.3)
+        sc = capi.Scene(capi.default_settings(**st), w.x, w.v, mass=w.mass)
+        sc.set_gravity(w.gravity)
+        sc.set_boundary(world, np.full(len(world), -1, np.int32), psi)
+        f0 = np.zeros((0, 3), np.float32)
+        for _ in range(20):
+            sc.step_coupled(w.dt, f0, f0)
+        v = sc.state()[1]
+        assert np.isfinite(v).all()
+        mean[c] = float(v[:, 0].mean())
+        sc.close()
+    assert mean[0.5] < mean[0.0] - 0.02, mean
+
+
+def test_body_velocities_need_the_boundary_and_every_body(port):
+    w = workloads.dam_break((4, 4, 4), R, (1.0, 1.0, 1.0), seed=0, vorticity=0.0)
+    sc = capi.Scene(capi.default_settings(**w.settings), w.x, w.v, mass=w.mass)
+    with pytest.raises(capi.PbfError):
+        sc.set_body_velocities([[0.0, 0.0, 0.0]], [[0.0, 0.0, 0.0]])
+    local = np.zeros((2, 3), np.float32)
+    sc.set_boundary(local, np.array([0, 1], np.int32), np.ones(2, np.float32))
+    with pytest.raises(capi.PbfError):
+        sc.set_body_velocities([[0.0, 0.0, 0.0]], [[0.0, 0.0, 0.0]])
+    sc.set_body_velocities(np.zeros((2, 3)), np.zeros((2, 3)))
+    sc.close()
+
+
+def test_fluid_world_friction_against_a_static_box():
+    """PBFSettings.boundary_friction through FluidWorld: a block thrown over a
+    static box at 0.5 m/s in x is slowed by the box's surface."""
+    import novaphy_gb300 as nv
+
+    mean = {}
+    for c in (0.0, 0.5):
+        mb = nv.ModelBuilder()
+        bi = mb.add_body(nv.RigidBody.make_static(),
+                         nv.Transform.from_translation(np.array([0.5, 0.5, 0.15], np.float32)))
+        mb.add_shape(nv.CollisionShape.make_box(np.array([0.2, 0.2, 0.1], np.float32), bi))
+        blk = nv.FluidBlockDef()
+        blk.lower = np.array([0.4125, 0.4125, 0.2625], np.float32)
+        blk.upper = np.array([0.5875, 0.5875, 0.4], np.float32)
+        blk.particle_spacing = R
+        blk.initial_velocity = np.array([0.5, 0.0, 0.0], np.float32)
+        st = nv.PBFSettings()
+        st.kernel_radius = 4 * R
+        st.use_domain_bounds = True
+        st.domain_lower = [0.0, 0.0, 0.0]
+        st.domain_upper = [1.0, 1.0, 1.0]
+        st.particle_radius = R / 2
+        st.boundary_two_way = True
+        st.boundary_friction = c
+        w = nv.FluidWorld(mb.build(), [blk], nv.SolverSettings(), st, 1.0)
+        w.set_gravity([0.0, 0.0, -9.81])
+        for _ in range(20):
+            w.step(1.0 / 120.0)
+        v = w.fluid_arrays()["velocities"]
+        assert np.isfinite(v).all()
+        mean[c] = float(v[:, 0].mean())
+    assert mean[0.5] < mean[0.0] - 0.02, mean
