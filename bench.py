@@ -94,7 +94,7 @@ def profile_value(kernel: str, key: str = "traffic_bytes_per_launch"):
     return None
 
 
-def issue_roof(inst_per_launch, launch_ms, sm_mhz, sms=152):
+def issue_roof(inst_per_launch, launch_ms, sm_mhz, kernel, sms=152):
     """Third roof, the one that binds: warp instructions issued per cycle per SM
     (4 schedulers, one instruction each per cycle).  Instructions per launch
     come from the ncu capture of the same kernel on the same workload; the
@@ -104,7 +104,7 @@ def issue_roof(inst_per_launch, launch_ms, sm_mhz, sms=152):
     ipc = inst_per_launch / (launch_ms / 1e3 * sm_mhz * 1e6 * sms)
     return {"achieved": ipc, "peak": 4.0, "unit": "warp inst/cycle/SM", "frac": ipc / 4.0,
             "inst_per_launch": inst_per_launch,
-            "source": "smsp__inst_executed.sum of profiles/k_delta_dam_break_1m.md"}
+            "source": f"smsp__inst_executed.sum of profiles/{kernel}_dam_break_1m.md"}
 
 
 class ClockSampler:
@@ -910,7 +910,7 @@ def run_ours(args, ws, rank, local):
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                 "fp32": fp32_roof(value / ws, iters),
                 "issue": issue_roof(profile_value(kern, "warp_instructions_per_launch"), launch_ms,
-                                    clocks.get("sm_mhz") if clocks else None)}
+                                    clocks.get("sm_mhz") if clocks else None, kern)}
 
     progress("single scene: fast build")
     # The FMA build on the same batch.

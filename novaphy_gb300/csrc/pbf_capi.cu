@@ -143,6 +143,7 @@ void free_particles(pbf_scene* s) {
                           align_up((size_t)s->off_cap * 4, 256);
         s->B.moved = reinterpret_cast<uint32_t*>(s->B.slot_alias + align_up(s->off_cap, 256));
         s->B.lamnz = s->B.moved + s->off_cap;
+        s->B.dhist = s->B.lamnz + s->off_cap;
     }
 }
 
@@ -293,15 +294,17 @@ int ensure_offsets(pbf_scene* s, uint32_t nslots) {
     if (s->off) cudaFree(s->off);
     s->off = nullptr;
     // offsets (nslots + 1 words), one alias byte per slot, a moved word and
-    // a lambda word per slot
+    // a lambda word per slot, then the density pass's walk counts
     const size_t ob = align_up((size_t)(nslots + 1) * 4, 256);
     const size_t ab = align_up(nslots + 1, 256);
-    PBF_CUDA(cudaMalloc(&s->off, ob + ab + (size_t)(nslots + 1) * 8));
+    PBF_CUDA(cudaMalloc(&s->off, ob + ab + (size_t)(nslots + 1) * 8 + 4 * kWalkHist * 4));
     s->off_cap = nslots + 1;
     s->B.off = s->off;
     s->B.slot_alias = reinterpret_cast<unsigned char*>(s->off) + ob;
     s->B.moved = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(s->off) + ob + ab);
     s->B.lamnz = s->B.moved + (nslots + 1);
+    s->B.dhist = s->B.lamnz + (nslots + 1);
+    PBF_CUDA(cudaMemsetAsync(s->B.dhist, 0, 4 * kWalkHist * 4, s->stream));
     return PBF_OK;
 }
 

@@ -412,6 +412,7 @@ struct Grid {
     uint32_t* moved;                     // per slot, see StepBuffers::moved
     uint32_t* lamnz;                     // per slot, see StepBuffers::lamnz
     BoundaryGrid bg;                     // two-way coupled steps only
+    uint32_t* dhist;                     // see StepBuffers::dhist
 };
 
 // The cell of sorted particle p against the boundary index (two-way steps).
@@ -552,6 +553,8 @@ __device__ __forceinline__ bool coop_row(bool active, const int4 cell, const Gri
 // the lane's x*, ci its cell x; `cut` the support test r_sq < cut of the
 // pass.  extra(q) returns the per-candidate extras of candidate q (kExtra);
 // body(xj, ej) adds the term of one candidate, re-testing r_sq < cut.
+// Lanes with `want` false list no candidates and do not widen the warp's
+// box (at least one lane must want).
 // kLam (the delta pass): a candidate whose lambda sum with the lane,
 // xi.w + xj.w, is zero adds an exact zero to the lane's sum (no s_corr
 // either, which needs a negative sum), and the sum, started at +0, never is
@@ -561,12 +564,14 @@ template <int CH, bool kExtra, bool kPersist, bool kLam, class Extra, class Body
 __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRow& R, int ci,
                                           const float4 xi, const float4* xin, float cut,
                                           const GridDesc& Gd, const uint32_t* __restrict__ off,
-                                          Extra&& extra, Body&& body) {
+                                          Extra&& extra, Body&& body, bool want = true) {
     constexpr int CAP = CoopSmem<CH, kExtra>::kCap;
     static_assert(CH % 32 == 0 && CAP % 32 == 0 && CAP >= 2 * CH, "coop walk sizes");
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    float lx = xi.x, ly = xi.y, lz = xi.z, hx = xi.x, hy = xi.y, hz = xi.z;
+    const float inf = __int_as_float(0x7f800000);
+    float lx = want ? xi.x : inf, ly = want ? xi.y : inf, lz = want ? xi.z : inf;
+    float hx = want ? xi.x : -inf, hy = want ? xi.y : -inf, hz = want ? xi.z : -inf;
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         lx = fminf(lx, __shfl_xor_sync(full, lx, o));
@@ -681,6 +686,7 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
                 }
             }
             bits &= allowed;
+            if (!want) bits = 0u;
             sm.mask[(base >> 5) + wd][lane] = bits;
             cnt += __popc(bits);
         }
@@ -832,6 +838,8 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     if (!live) return;
     const float4 xi = xin[p];
     float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
+    float ci_first = 0.0f;  // C_i of a density-first walk (computed once)
+    bool have_ci = false;
     auto term = [&](const float4& xj) {
         float rx, ry, rz;
         const float r_sq = rel_sq(xi, xj, rx, ry, rz);
@@ -849,9 +857,61 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     };
     if constexpr (kCoop) {
         if (coop) {
-            coop_walk<CH, false, kPersist, false>(
-                sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, [](uint32_t) { return float4{}; },
-                [&](const float4& xj, const float4&) { term(xj); });
+            auto none = [](uint32_t) { return float4{}; };
+            // Density first: when C_i < 0 lambda_i is 0 whatever the gradient
+            // sums, so a warp can sum the densities alone (poly6 terms, no
+            // square root or division), then walk again, in the same
+            // candidate order, for the gradients of its lanes with
+            // C_i >= 0 only.  Each sum sees the same terms in the same order
+            // as the single walk: same bits.  It pays where most warps have
+            // no such lane; which way a warp goes follows the share of
+            // warps that needed gradients in the same iteration of the last
+            // step.
+            bool dfirst = false;
+            if (G.dhist && it < kWalkHist && !G.bg.spos) {
+                const uint32_t need = __ldg(G.dhist + it), ran = __ldg(G.dhist + kWalkHist + it);
+                dfirst = ran > 0 && 3u * need < ran;
+            }
+            if (!dfirst) {
+                coop_walk<CH, false, kPersist, false>(
+                    sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, none,
+                    [&](const float4& xj, const float4&) { term(xj); });
+            } else {
+                // grads false: densities only; true: gradients only.
+                bool grads = false, want = true;
+                for (;;) {
+                    coop_walk<CH, false, kPersist, false>(
+                        sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, none,
+                        [&](const float4& xj, const float4&) {
+                            float rx, ry, rz;
+                            const float r_sq = rel_sq(xi, xj, rx, ry, rz);
+                            if (r_sq < C.cut) {
+                                if (!grads) {
+                                    density += C.mass * poly6(r_sq, C);
+                                } else {
+                                    const float c = spiky_coeff(r_sq, C);
+                                    const float gx = C.mr * (c * rx);
+                                    const float gy = C.mr * (c * ry);
+                                    const float gz = C.mr * (c * rz);
+                                    sum_grad_sq += sqn(gx, gy, gz);
+                                    gix += gx;
+                                    giy += gy;
+                                    giz += gz;
+                                }
+                            }
+                        },
+                        want);
+                    if (grads) break;
+                    ci_first = density * C.inv_rho0 - 1.0f;
+                    have_ci = true;
+                    want = !(ci_first < 0.0f);
+                    if (!__any_sync(0xffffffffu, want)) break;
+                    grads = true;
+                }
+            }
+            if (G.dhist && it < kWalkHist && (threadIdx.x & 31) == 0) {
+                atomicAdd(G.dhist + 3 * kWalkHist + it, 1u);
+            }
         }
     }
     if (!coop)
@@ -878,8 +938,13 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
                               });
     }
     sum_grad_sq += sqn(gix, giy, giz);
-    const float Ci = density * C.inv_rho0 - 1.0f;
+    const float Ci = have_ci ? ci_first : density * C.inv_rho0 - 1.0f;
     const float lam = (Ci < 0.0f) ? 0.0f : -Ci / (sum_grad_sq + C.eps);
+    if constexpr (kCoop) {
+        if (coop && G.dhist && it < kWalkHist &&
+            __any_sync(0xffffffffu, !(Ci < 0.0f)) && (threadIdx.x & 31) == 0)
+            atomicAdd(G.dhist + 2 * kWalkHist + it, 1u);
+    }
     if (G.lamnz && lam != 0.0f) G.lamnz[slot_of(cell.x, cell.y, cell.z, C.grid)] = (uint32_t)it + 1u;
     srho[p] = density;
     xout[p] = make_float4(xi.x, xi.y, xi.z, lam);
@@ -1406,7 +1471,8 @@ inline int grid_of(int n, int b) { return (n + b - 1) / b; }
 
 inline Grid grid_view(const StepBuffers& B, const uint32_t* spid = nullptr,
                       const BoundaryGrid& bg = BoundaryGrid{}) {
-    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved, B.lamnz, bg};
+    return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved, B.lamnz, bg,
+                spid ? nullptr : B.dhist};
 }
 
 // predict, sort by cell and by reference key, cell offsets, gather, reference
@@ -1423,6 +1489,12 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     cudaError_t e = cudaMemsetAsync(B.slot_alias, 0, (size_t)C.grid.nslots, st);
     if (e == cudaSuccess && B.moved) e = cudaMemsetAsync(B.moved, 0, (size_t)C.grid.nslots * 4, st);
     if (e == cudaSuccess && B.lamnz) e = cudaMemsetAsync(B.lamnz, 0, (size_t)C.grid.nslots * 4, st);
+    if (e == cudaSuccess && B.dhist) {
+        // This step's density-pass counts become the previous step's.
+        e = cudaMemcpyAsync(B.dhist, B.dhist + 2 * kWalkHist, 2 * kWalkHist * 4,
+                            cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.dhist + 2 * kWalkHist, 0, 2 * kWalkHist * 4, st);
+    }
     if (e != cudaSuccess) return e;
     if (pm) pm->mark(-1, 0, st);
     k_predict_key<<<nb, kBlock, 0, st>>>(B.keys, B.rkeys, n, none, one);

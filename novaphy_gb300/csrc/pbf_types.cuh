@@ -117,8 +117,15 @@ struct StepBuffers {
     // Per slot: 1 + the Jacobi iteration whose density pass last left a
     // particle of the slot with a nonzero lambda (0: none in this step).
     uint32_t* lamnz;
+    // Per Jacobi iteration (kWalkHist of them): how many cooperative warps
+    // of the density pass had a lane with C_i >= 0, and how many ran, in
+    // the previous step ([0, 2 kWalkHist)) and in this one (the rest).
+    // Single scenes only (null in batches).
+    uint32_t* dhist;
     uint32_t* err;  // device status word
 };
+
+constexpr int kWalkHist = 16;
 
 // Phases of one step, named after the reference's PerformanceMonitor scopes
 // (pbf_solver.cpp:29-103).  Fused kernels report under the first scope they
