@@ -406,6 +406,43 @@ class Scene:
         return x, v, rho, lam
 
 
+class _HostBlock:
+    """Page-locked host memory from pbf_host_alloc, freed with its last view."""
+
+    def __init__(self, nbytes: int):
+        self.ptr = C.c_void_p()
+        check(load().pbf_host_alloc(nbytes, C.byref(self.ptr)))
+
+    def __del__(self):
+        if self.ptr and self.ptr.value:
+            load().pbf_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
+    """An uninitialised numpy array in page-locked host memory (pbf_host_alloc),
+    which the copies of pbf_solver_step_host and pbf_scene_read/write move by
+    DMA without an intermediate pageable bounce."""
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape))
+    blk = _HostBlock(max(count * dt.itemsize, 1))
+    buf = (C.c_byte * max(count * dt.itemsize, 1)).from_address(blk.ptr.value)
+    buf._owner = blk  # the numpy array keeps buf, and buf the block, alive
+    return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+
+
+def solver_step_host_inplace(scene: "Scene", x, v, rho, lam, dt, g, mass) -> None:
+    """pbf_solver_step_host on the caller's arrays, updated in place (float32,
+    C-contiguous; x and v n x 3)."""
+    for a in (x, v, rho, lam):
+        if a.dtype != np.float32 or not a.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous float32")
+    g = _f32(g, (3,))
+    check(scene._L.pbf_solver_step_host(scene.handle, len(x), _ptr(x), _ptr(v), _ptr(rho),
+                                        _ptr(lam), dt, g.ctypes.data_as(C.POINTER(C.c_float)),
+                                        mass))
+
+
 def _handles(objs):
     arr = (C.c_void_p * max(len(objs), 1))()
     for k, o in enumerate(objs):

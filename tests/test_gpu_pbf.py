@@ -300,3 +300,25 @@ def test_replay_timed_restores_each_step():
     b.step(w.dt, 1)
     for u, t in zip(a.state(), b.state()):
         assert np.array_equal(u, t)
+
+
+def test_solver_step_host_on_page_locked_arrays():
+    """pbf_solver_step_host on page-locked arrays (capi.pinned_empty, updated in
+    place) gives the bits of the same call on pageable arrays, for sizes that
+    are not a multiple of the block and across changes of n."""
+    for counts in ((20, 20, 20), (12, 11, 7), (13, 11, 7)):
+        w = workloads.dam_break(counts, 0.025, (1.0, 1.0, 1.0), seed=3)
+        drop = capi.Scene(settings_of(w), np.zeros((1, 3), np.float32), None, mass=w.mass)
+        z = np.zeros(w.n, np.float32)
+        want = drop.solver_step_host(w.x, w.v, z, z, w.dt, w.gravity, w.mass)
+        hx, hv = capi.pinned_empty((w.n, 3)), capi.pinned_empty((w.n, 3))
+        hr, hl = capi.pinned_empty((w.n,)), capi.pinned_empty((w.n,))
+        for _ in range(2):
+            hx[:] = w.x
+            hv[:] = w.v
+            hr[:] = 0
+            hl[:] = 0
+            capi.solver_step_host_inplace(drop, hx, hv, hr, hl, w.dt, w.gravity, w.mass)
+            for a, b in zip((hx, hv, hr, hl), want):
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        drop.close()
