@@ -314,9 +314,7 @@ cudaError_t index_build(PointIndex& I, const float4* pos, const float* attr, int
     k_offsets<<<grid_of((int)C.grid.nslots + 1, 256), 256, 0, st>>>(I.skeys, n, I.off, C.grid.nslots);
     k_ix_gather<<<nb, kBlock, 0, st>>>(I.sidx, pos, attr, n, I.spos, I.scell, I.pos_of,
                                        I.slot_alias, C);
-    k_buckets<<<grid_of(n, 256), 256, 0, st>>>(I.rsorted, I.ridx, I.pos_of, I.scell, nullptr, I.kpos,
-                                               I.bend, n);
-    return cudaGetLastError();
+    return enqueue_buckets(I.rsorted, I.ridx, I.pos_of, I.scell, nullptr, I.kpos, I.bend, n, st);
 }
 
 cudaError_t predict_points(const float4* x, const float4* v, int n, float4* out,

@@ -305,35 +305,95 @@ k_gather(const uint32_t* __restrict__ sidx, float4* __restrict__ sx, float4* __r
 // cell-sorted ones; at each bucket start, bend holds the bucket end with
 // kImpureBit set when the bucket mixes cells (hash collision).  With scene
 // ids (ksid, in key-sorted order) a bucket never crosses a scene boundary:
-// every scene has its own hash grid.
-__global__ void __launch_bounds__(256)
-k_buckets(const unsigned long long* __restrict__ rsorted, const uint32_t* __restrict__ ridx,
-          const uint32_t* __restrict__ pos_of, const int4* __restrict__ scell,
-          const uint32_t* __restrict__ ksid, uint32_t* __restrict__ kpos,
-          uint32_t* __restrict__ bend, int n) {
-    const int kp = blockIdx.x * blockDim.x + threadIdx.x;
-    if (kp >= n) return;
+// every scene has its own hash grid.  Two launches (enqueue_buckets): the
+// bucket starts find their ends, then members whose cell differs from the
+// previous member's mark their bucket impure.  Both searches gallop, so a
+// bucket of L members costs O(log L) per thread; a serial scan by the start
+// thread took milliseconds on buckets of tens of thousands of particles
+// (fluid piled into a corner cell by the domain clamp).
+struct BucketKeys {
+    const unsigned long long* __restrict__ rsorted;
+    const uint32_t* __restrict__ ksid;
+    int n;
+    __device__ __forceinline__ bool same(int m, unsigned long long k, uint32_t s0) const {
+        return rsorted[m] == k && (!ksid || ksid[m] == s0);
+    }
+    // First position after kp outside kp's bucket.
+    __device__ __forceinline__ int end_of(int kp) const {
+        const unsigned long long k = rsorted[kp];
+        const uint32_t s0 = ksid ? ksid[kp] : 0u;
+        int lo = kp, step = 1, hi = kp + 1;
+        while (hi < n && same(hi, k, s0)) {
+            lo = hi;
+            step <<= 1;
+            hi = (n - kp > step) ? kp + step : n;
+        }
+        while (hi - lo > 1) {
+            const int mid = lo + ((hi - lo) >> 1);
+            if (same(mid, k, s0)) lo = mid;
+            else hi = mid;
+        }
+        return hi;
+    }
+    // First position of kp's bucket.
+    __device__ __forceinline__ int start_of(int kp) const {
+        const unsigned long long k = rsorted[kp];
+        const uint32_t s0 = ksid ? ksid[kp] : 0u;
+        int hi = kp, step = 1, lo = kp - 1;
+        while (lo >= 0 && same(lo, k, s0)) {
+            hi = lo;
+            step <<= 1;
+            lo = (kp >= step) ? kp - step : -1;
+        }
+        while (hi - lo > 1) {
+            const int mid = lo + ((hi - lo) >> 1);
+            if (same(mid, k, s0)) hi = mid;
+            else lo = mid;
+        }
+        return hi;
+    }
+};
+
+__device__ __forceinline__ uint32_t cell_sorted_pos(const uint32_t* __restrict__ ridx,
+                                                    const uint32_t* __restrict__ pos_of, int kp,
+                                                    int n) {
     const uint32_t i0 = ridx[kp];
     uint32_t p0 = pos_of[i0 < (uint32_t)n ? i0 : 0];
-    if (p0 >= (uint32_t)n) p0 = 0;
-    kpos[kp] = p0;
-    const unsigned long long k = rsorted[kp];
-    const uint32_t s0 = ksid ? ksid[kp] : 0u;
-    if (kp > 0 && rsorted[kp - 1] == k && (!ksid || ksid[kp - 1] == s0)) return;
-    const int4 c0 = scell[p0];
-    bool pure = true;
-    int e = kp + 1;
-    while (e < n && rsorted[e] == k && (!ksid || ksid[e] == s0)) {
-        if (pure) {
-            const uint32_t ie = ridx[e];
-            uint32_t pe = pos_of[ie < (uint32_t)n ? ie : 0];
-            if (pe >= (uint32_t)n) pe = 0;
-            const int4 ce = scell[pe];
-            if (ce.x != c0.x || ce.y != c0.y || ce.z != c0.z) pure = false;
-        }
-        ++e;
-    }
-    bend[kp] = (uint32_t)e | (pure ? 0u : kImpureBit);
+    return p0 < (uint32_t)n ? p0 : 0u;
+}
+
+__global__ void __launch_bounds__(256)
+k_buckets(const BucketKeys K, const uint32_t* __restrict__ ridx, const uint32_t* __restrict__ pos_of,
+          uint32_t* __restrict__ kpos, uint32_t* __restrict__ bend) {
+    const int kp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kp >= K.n) return;
+    kpos[kp] = cell_sorted_pos(ridx, pos_of, kp, K.n);
+    if (kp > 0 && K.same(kp - 1, K.rsorted[kp], K.ksid ? K.ksid[kp] : 0u)) return;
+    bend[kp] = (uint32_t)K.end_of(kp);
+}
+
+__global__ void __launch_bounds__(256)
+k_bucket_mix(const BucketKeys K, const uint32_t* __restrict__ ridx,
+             const uint32_t* __restrict__ pos_of, const int4* __restrict__ scell,
+             uint32_t* __restrict__ bend) {
+    const int kp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kp == 0 || kp >= K.n) return;
+    if (!K.same(kp - 1, K.rsorted[kp], K.ksid ? K.ksid[kp] : 0u)) return;
+    const int4 c = scell[cell_sorted_pos(ridx, pos_of, kp, K.n)];
+    const int4 d = scell[cell_sorted_pos(ridx, pos_of, kp - 1, K.n)];
+    if (c.x != d.x || c.y != d.y || c.z != d.z) atomicOr(bend + K.start_of(kp), kImpureBit);
+}
+
+inline cudaError_t enqueue_buckets(const unsigned long long* rsorted, const uint32_t* ridx,
+                                   const uint32_t* pos_of, const int4* scell,
+                                   const uint32_t* ksid, uint32_t* kpos, uint32_t* bend, int n,
+                                   cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const BucketKeys K{rsorted, ksid, n};
+    const int nb = (n + 255) / 256;
+    k_buckets<<<nb, 256, 0, st>>>(K, ridx, pos_of, kpos, bend);
+    k_bucket_mix<<<nb, 256, 0, st>>>(K, ridx, pos_of, scell, bend);
+    return cudaGetLastError();
 }
 
 // Marks query points whose neighbourhood differs from the reference's
@@ -1512,15 +1572,15 @@ inline cudaError_t enqueue_prefix(const StepBuffers& B, const StepConsts& C, Sor
     k_gather<<<nb, kBlock, 0, st>>>(B.sidx, B.sx, B.xa, B.srho, B.scell, B.pos_of, B.slot_alias,
                                     B.err, n, none, one);
     if (C.hash_compat) {
-        k_buckets<<<grid_of(n, 256), 256, 0, st>>>(B.rsorted, B.ridx, B.pos_of, B.scell, nullptr,
-                                                   B.kpos, B.bend, n);
+        e = enqueue_buckets(B.rsorted, B.ridx, B.pos_of, B.scell, nullptr, B.kpos, B.bend, n, st);
+        if (e != cudaSuccess) return e;
         k_classify<<<nb, kBlock, 0, st>>>(B.scell, n, B.scell, B.rsorted, B.kpos, B.bend,
                                           B.slot_alias, B.btab, B.sown, nullptr, one);
     } else {
         e = cudaMemsetAsync(B.sown, 0, (size_t)n * 4, st);
         if (e != cudaSuccess) return e;
     }
-    if (pm) pm->mark(kPhaseNeighborQuery, C.hash_compat ? 3 : 1, st);
+    if (pm) pm->mark(kPhaseNeighborQuery, C.hash_compat ? 4 : 1, st);
     return cudaGetLastError();
 }
 
@@ -1728,11 +1788,11 @@ inline cudaError_t enqueue_batch_step(const StepBuffers& B, const BatchDesc& D, 
     if (pm) pm->mark(kPhaseGridBuild, 14 + (D.key_bits + 7) / 8 + (D.scene_bits + 7) / 8, st);
     k_gather<<<nb, kBlock, 0, st>>>(B.sidx, B.sx, B.xa, B.srho, B.scell, B.pos_of, B.slot_alias,
                                     B.err, n, ids, tab);
-    k_buckets<<<grid_of(n, 256), 256, 0, st>>>(B.rsorted, B.ridx, B.pos_of, B.scell, D.kpid, B.kpos,
-                                               B.bend, n);
+    e = enqueue_buckets(B.rsorted, B.ridx, B.pos_of, B.scell, D.kpid, B.kpos, B.bend, n, st);
+    if (e != cudaSuccess) return e;
     k_classify<<<nb, kBlock, 0, st>>>(B.scell, n, B.scell, B.rsorted, B.kpos, B.bend, B.slot_alias,
                                       B.btab, B.sown, D.spid, tab);
-    if (pm) pm->mark(kPhaseNeighborQuery, 3, st);
+    if (pm) pm->mark(kPhaseNeighborQuery, 4, st);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return enqueue_passes(B, grid_view(B, D.spid), n, D.max_iters, D.any_zero_iters, D.any_vort,
