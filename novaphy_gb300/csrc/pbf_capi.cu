@@ -831,7 +831,7 @@ size_t scene_device_bytes(const pbf_scene* s) {
     if (s->wmem) b += work_bytes(s->work_cap) + sort_scratch_bytes(s->work_cap);
     if (s->off)
         b += align_up((size_t)s->off_cap * 4, 256) + align_up(s->off_cap, 256) +
-             (size_t)s->off_cap * 8;
+             (size_t)s->off_cap * 8 + 4 * kWalkHist * 4;
     return b;
 }
 

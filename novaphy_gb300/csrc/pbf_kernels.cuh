@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <type_traits>
 
+#include "exact_repeat.h"
 #include "pbf_types.cuh"
 #include "radix_sort.cuh"
 
@@ -34,6 +35,10 @@ constexpr int kBlock = 128;
 // own streams run several kernels per SM at once, and there the larger code
 // and shared memory measured up to 40 % slower.
 constexpr int kBigScene = 1 << 17;
+// The fewest candidates a row of the cooperative walk must hold before the
+// walk looks for runs of identical candidates in it (rows of ordinary fluid
+// hold a few hundred).
+constexpr uint32_t kRunRow = 1024;
 constexpr uint32_t kNoBucket = 0xffffffffu;
 constexpr uint32_t kImpureBit = 0x80000000u;
 
@@ -93,6 +98,18 @@ __device__ __forceinline__ float spiky_coeff(float r_sq, const StepConsts& C) {
     return C.k_spiky * diff * diff / r_len;
 #endif
 }
+
+// Adding a term to a running sum once (One) or m times in a row (a run of
+// identical candidates in the cooperative walk): acc(s, t, m) is the float
+// that m single additions of t leave, bit for bit.
+struct One {};
+__device__ __forceinline__ float acc(float s, float t, One) { return s + t; }
+__device__ __forceinline__ bool bits_equal(const float4 a, const float4 b) {
+    return __float_as_uint(a.x) == __float_as_uint(b.x) && __float_as_uint(a.y) == __float_as_uint(b.y) &&
+           __float_as_uint(a.z) == __float_as_uint(b.z) && __float_as_uint(a.w) == __float_as_uint(b.w);
+}
+__device__ __forceinline__ float acc_n(float s, float t, uint32_t m) { return rep_add(s, t, m); }
+__device__ __forceinline__ float acc(float s, float t, uint32_t m) { return acc_n(s, t, m); }
 
 // ---------------------------------------------------------------------------
 // Grid helpers
@@ -612,19 +629,26 @@ __device__ __forceinline__ bool coop_row(bool active, const int4 cell, const Gri
 // The cooperative walk (see above) of a warp for which coop_row held.  xi is
 // the lane's x*, ci its cell x; `cut` the support test r_sq < cut of the
 // pass.  extra(q) returns the per-candidate extras of candidate q (kExtra);
-// body(xj, ej) adds the term of one candidate, re-testing r_sq < cut.
+// body(xj, ej) adds the term of one candidate, re-testing r_sq < cut;
+// rep(xj, ej, L) adds it L times in a row (exactly, see acc).
 // Lanes with `want` false list no candidates and do not widen the warp's
 // box (at least one lane must want).
+// kRuns: rows of at least kRunRow candidates collapse runs of identical
+// candidates (below).  The XSPH and vorticity passes compile it in; the
+// constraint passes do not (it cost their register allocation about 4 %
+// of their time on ordinary fluid).
 // kLam (the delta pass): a candidate whose lambda sum with the lane,
 // xi.w + xj.w, is zero adds an exact zero to the lane's sum (no s_corr
 // either, which needs a negative sum), and the sum, started at +0, never is
 // -0, so such candidates are not listed; when every lane's lambda is zero,
 // candidates with zero lambda are not staged at all.
-template <int CH, bool kExtra, bool kPersist, bool kLam, class Extra, class Body>
+template <int CH, bool kExtra, bool kPersist, bool kLam, bool kRuns, class Extra, class Body,
+          class Rep>
 __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRow& R, int ci,
                                           const float4 xi, const float4* xin, float cut,
                                           const GridDesc& Gd, const uint32_t* __restrict__ off,
-                                          Extra&& extra, Body&& body, bool want = true) {
+                                          Extra&& extra, Body&& body, Rep&& rep,
+                                          bool want = true) {
     constexpr int CAP = CoopSmem<CH, kExtra>::kCap;
     static_assert(CH % 32 == 0 && CAP % 32 == 0 && CAP >= 2 * CH, "coop walk sizes");
     const unsigned full = 0xffffffffu;
@@ -795,11 +819,11 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
             b3 = __ldg(off + row + 3);
             if (R.W > 4) b4 = __ldg(off + row + 4);
         }
-        for (uint32_t qb = q0; qb < q1; qb += 32) {
-            const uint32_t q = qb + (uint32_t)lane;
+        // Stages the candidates q of the lanes with `ok` that pass the box.
+        auto stage = [&](uint32_t q, bool ok) {
             bool pass = false;
             float4 xj = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (q < q1) {
+            if (ok) {
                 xj = ld_step<kPersist>(xin + q);
                 const float ex = fmaxf(0.0f, fmaxf(lx - xj.x, xj.x - hx));
                 const float ey = fmaxf(0.0f, fmaxf(ly - xj.y, xj.y - hy));
@@ -822,6 +846,74 @@ __device__ __forceinline__ void coop_walk(CoopSmem<CH, kExtra>& sm, const CoopRo
                 __syncwarp();
                 test_chunk(false);
             }
+        };
+        if (!kRuns || q1 - q0 < kRunRow) {
+            for (uint32_t qb = q0; qb < q1; qb += 32) stage(qb + (uint32_t)lane, qb + lane < q1);
+        } else {
+            // (kRuns) A row long enough to hold a run of identical
+            // candidates: the domain clamp piles fluid into a box corner, bit
+            // for bit, and such a cell holds tens of thousands.  Candidates with the same
+            // (xj, ej) in the same cell add the same term to a lane, so a
+            // run of whole 32-candidate chunks of them is not staged: the
+            // candidates before it are settled first, then each lane adds
+            // the run's term as many times as the run is long (rep, an exact
+            // repeated addition), then the walk goes on.  Shorter runs and
+            // run ends inside a chunk are staged as usual.
+            bool inrun = false;
+            float4 rx = make_float4(0.0f, 0.0f, 0.0f, 0.0f), re = rx;
+            uint32_t rn = 0;
+            int rc = 0;
+            auto apply = [&]() {
+                if (want && (all_member || (unsigned)(rc - myc + 1) <= 2u)) rep(rx, re, rn);
+                __syncwarp();
+                inrun = false;
+            };
+            for (uint32_t qb = q0; qb < q1; qb += 32) {
+                const uint32_t q = qb + (uint32_t)lane;
+                const bool ok = q < q1;
+                float4 xj = make_float4(0.0f, 0.0f, 0.0f, 0.0f), ej = xj;
+                if (ok) {
+                    xj = ld_step<kPersist>(xin + q);
+                    if constexpr (kExtra) ej = extra(q);
+                }
+                const int cq = (int)((q >= b1) + (q >= b2) + (q >= b3) + (q >= b4));
+                float4 ax = rx, ae = re;
+                int ac = rc;
+                if (!inrun) {
+                    ax = make_float4(__shfl_sync(full, xj.x, 0), __shfl_sync(full, xj.y, 0),
+                                     __shfl_sync(full, xj.z, 0), __shfl_sync(full, xj.w, 0));
+                    if constexpr (kExtra)
+                        ae = make_float4(__shfl_sync(full, ej.x, 0), __shfl_sync(full, ej.y, 0),
+                                         __shfl_sync(full, ej.z, 0), __shfl_sync(full, ej.w, 0));
+                    ac = __shfl_sync(full, cq, 0);
+                }
+                const bool same = ok && cq == ac && bits_equal(xj, ax) && (!kExtra || bits_equal(ej, ae));
+                const uint32_t sm_same = __ballot_sync(full, same);
+                if (inrun) {
+                    if (sm_same == full) {
+                        rn += 32;
+                        continue;
+                    }
+                    const int f = __ffs(~sm_same) - 1;  // the run ends before lane f
+                    rn += (uint32_t)f;
+                    apply();
+                    stage(q, ok && lane >= f);
+                } else if (sm_same == full) {
+                    if (nst > 0) {
+                        __syncwarp();
+                        test_chunk(true);
+                    }
+                    if (base > 0) evaluate();
+                    inrun = true;
+                    rx = ax;
+                    re = ae;
+                    rc = ac;
+                    rn = 32;
+                } else {
+                    stage(q, ok);
+                }
+            }
+            if (inrun) apply();
         }
     }
     if (nst > 0) {
@@ -900,21 +992,26 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     float density = 0.0f, sum_grad_sq = 0.0f, gix = 0.0f, giy = 0.0f, giz = 0.0f;
     float ci_first = 0.0f;  // C_i of a density-first walk (computed once)
     bool have_ci = false;
-    auto term = [&](const float4& xj) {
+    // The term of candidate xj, added L times (One: once); density-first
+    // walks add the density alone (grads false) or the gradient sums alone.
+    auto part = [&](const float4& xj, auto L, bool dens, bool grads) {
         float rx, ry, rz;
         const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
-            density += C.mass * poly6(r_sq, C);
-            const float c = spiky_coeff(r_sq, C);
-            const float gx = C.mr * (c * rx);
-            const float gy = C.mr * (c * ry);
-            const float gz = C.mr * (c * rz);
-            sum_grad_sq += sqn(gx, gy, gz);
-            gix += gx;
-            giy += gy;
-            giz += gz;
+            if (dens) density = acc(density, C.mass * poly6(r_sq, C), L);
+            if (grads) {
+                const float c = spiky_coeff(r_sq, C);
+                const float gx = C.mr * (c * rx);
+                const float gy = C.mr * (c * ry);
+                const float gz = C.mr * (c * rz);
+                sum_grad_sq = acc(sum_grad_sq, sqn(gx, gy, gz), L);
+                gix = acc(gix, gx, L);
+                giy = acc(giy, gy, L);
+                giz = acc(giz, gz, L);
+            }
         }
     };
+    auto term = [&](const float4& xj, auto L) { part(xj, L, true, true); };
     if constexpr (kCoop) {
         if (coop) {
             auto none = [](uint32_t) { return float4{}; };
@@ -932,15 +1029,16 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
                 const uint32_t need = __ldg(G.dhist + it), ran = __ldg(G.dhist + kWalkHist + it);
                 dfirst = ran > 0 && 3u * need < ran;
             }
+            auto once = [&](const float4& xj, const float4&) { term(xj, One{}); };
+            auto times = [&](const float4& xj, const float4&, uint32_t L) { term(xj, L); };
             if (!dfirst) {
-                coop_walk<CH, false, kPersist, false>(
-                    sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, none,
-                    [&](const float4& xj, const float4&) { term(xj); });
+                coop_walk<CH, false, kPersist, false, false>(sm, R, cell.x, xi, xin, C.cut, C.grid, G.off,
+                                                      none, once, times);
             } else {
-                // grads false: densities only; true: gradients only.
-                bool grads = false, want = true;
+                // Densities only, then gradients only for the lanes that want.
+                bool want = true, grads = false;
                 for (;;) {
-                    coop_walk<CH, false, kPersist, false>(
+                    coop_walk<CH, false, kPersist, false, false>(
                         sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, none,
                         [&](const float4& xj, const float4&) {
                             float rx, ry, rz;
@@ -960,6 +1058,9 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
                                 }
                             }
                         },
+                        [&](const float4& xj, const float4&, uint32_t L) {
+                            part(xj, L, !grads, grads);
+                        },
                         want);
                     if (grads) break;
                     ci_first = density * C.inv_rho0 - 1.0f;
@@ -976,7 +1077,7 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     }
     if (!coop)
         for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
-                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q)); });
+                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); });
     if (G.bg.spos) {
         // Two-way coupling (no counterpart in the reference): after the fluid
         // terms, the boundary's Akinci density rho0 psi_b W and its gradient
@@ -1072,7 +1173,7 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     if constexpr (kCoop) coop = coop_row(live, cell, C.grid, R, scene_at(G, pa));
     if (!live) return;
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-    auto term = [&](const float4& xj) {
+    auto term = [&](const float4& xj, auto L) {
         float rx, ry, rz, lambda_sum;
         const float r_sq = rel_sq<true>(xi, xj, rx, ry, rz, &lambda_sum);
         // A zero lambda sum adds an exact zero (no s_corr either); the sum,
@@ -1088,21 +1189,23 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
             }
             const float c = spiky_coeff(r_sq, C);
             const float a = (lambda_sum + s_corr) * C.mass;
-            dx += a * (c * rx);
-            dy += a * (c * ry);
-            dz += a * (c * rz);
+            dx = acc(dx, a * (c * rx), L);
+            dy = acc(dy, a * (c * ry), L);
+            dz = acc(dz, a * (c * rz), L);
         }
     };
     if constexpr (kCoop) {
         if (coop && __any_sync(0xffffffffu, walk)) {
-            coop_walk<CH, false, kPersist, true>(
-                sm, R, cell.x, xi, xin, C.cut, C.grid, G.off, [](uint32_t) { return float4{}; },
-                [&](const float4& xj, const float4&) { term(xj); });
+            coop_walk<CH, false, kPersist, true, false>(
+                sm, R, cell.x, xi, xin, C.cut, C.grid, G.off,
+                [](uint32_t) { return float4{}; },
+                [&](const float4& xj, const float4&) { term(xj, One{}); },
+                [&](const float4& xj, const float4&, uint32_t L) { term(xj, L); });
         }
     }
     if (walk && !coop)
         for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
-                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q)); });
+                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); });
     if (G.bg.spos && xi.w != 0.0f) {
         // Two-way coupling: the boundary's share of the position correction,
         // lambda_i (rho0 psi_b) grad W, after the fluid terms (zero when
@@ -1320,27 +1423,29 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
     float vx = vi.x, vy = vi.y, vz = vi.z;
     if (C.xsph_on) {
         float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-        auto term = [&](const float4& xj, const float4& vj) {
+        auto term = [&](const float4& xj, const float4& vj, auto L) {
             float rx, ry, rz;
             const float r_sq = rel_sq(xi, xj, rx, ry, rz);
             if (r_sq < C.h2) {
                 const float w = poly6(r_sq, C);
-                cx += vj.w * (vj.x - vi.x) * w;
-                cy += vj.w * (vj.y - vi.y) * w;
-                cz += vj.w * (vj.z - vi.z) * w;
+                cx = acc(cx, vj.w * (vj.x - vi.x) * w, L);
+                cy = acc(cy, vj.w * (vj.y - vi.y) * w, L);
+                cz = acc(cz, vj.w * (vj.z - vi.z) * w, L);
             }
         };
         if constexpr (B::kOn) {
             if (coop)
-                coop_walk<coop_chunk(BS), true, false, false>(
+                coop_walk<coop_chunk(BS), true, false, false, true>(
                     sm[threadIdx.x >> 5], R, cell.x, xi, xin, C.h2, C.grid, G.off,
-                    [&](uint32_t q) { return __ldg(sv + q); }, term);
+                    [&](uint32_t q) { return __ldg(sv + q); },
+                    [&](const float4& xj, const float4& vj) { term(xj, vj, One{}); },
+                    [&](const float4& xj, const float4& vj, uint32_t L) { term(xj, vj, L); });
         }
         if (!coop) {
             for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
                 const float4 xj = __ldg(xin + q);
                 float rx, ry, rz;
-                if (rel_sq(xi, xj, rx, ry, rz) < C.h2) term(xj, __ldg(sv + q));
+                if (rel_sq(xi, xj, rx, ry, rz) < C.h2) term(xj, __ldg(sv + q), One{});
             });
         }
         vx = vi.x + C.xsph_c * cx;
@@ -1373,7 +1478,7 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
     const float4 xi = xin[p];
     const float4 vi = sv[p];
     float cx = 0.0f, cy = 0.0f, cz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
-    auto term = [&](const float4& xj, const float4& vj) {
+    auto term = [&](const float4& xj, const float4& vj, auto L) {
         float rx, ry, rz;
         const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
@@ -1381,27 +1486,29 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
             const float uy = vj.y - vi.y;
             const float uz = vj.z - vi.z;
             const float w = poly6(r_sq, C);
-            cx += vj.w * ux * w;
-            cy += vj.w * uy * w;
-            cz += vj.w * uz * w;
+            cx = acc(cx, vj.w * ux * w, L);
+            cy = acc(cy, vj.w * uy * w, L);
+            cz = acc(cz, vj.w * uz * w, L);
             const float c = spiky_coeff(r_sq, C);
             const float gx = c * rx, gy = c * ry, gz = c * rz;
-            wx += vj.w * (gy * uz - gz * uy);
-            wy += vj.w * (gz * ux - gx * uz);
-            wz += vj.w * (gx * uy - gy * ux);
+            wx = acc(wx, vj.w * (gy * uz - gz * uy), L);
+            wy = acc(wy, vj.w * (gz * ux - gx * uz), L);
+            wz = acc(wz, vj.w * (gx * uy - gy * ux), L);
         }
     };
     if constexpr (B::kOn) {
         if (coop)
-            coop_walk<coop_chunk(BS), true, false, false>(sm[threadIdx.x >> 5], R, cell.x, xi, xin,
-                                                   C.cut, C.grid, G.off,
-                                                   [&](uint32_t q) { return __ldg(sv + q); }, term);
+            coop_walk<coop_chunk(BS), true, false, false, true>(
+                sm[threadIdx.x >> 5], R, cell.x, xi, xin, C.cut, C.grid, G.off,
+                [&](uint32_t q) { return __ldg(sv + q); },
+                [&](const float4& xj, const float4& vj) { term(xj, vj, One{}); },
+                [&](const float4& xj, const float4& vj, uint32_t L) { term(xj, vj, L); });
     }
     if (!coop) {
         for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
             const float4 xj = __ldg(xin + q);
             float rx, ry, rz;
-            if (rel_sq(xi, xj, rx, ry, rz) < C.cut) term(xj, __ldg(sv + q));
+            if (rel_sq(xi, xj, rx, ry, rz) < C.cut) term(xj, __ldg(sv + q), One{});
         });
     }
     float vx = vi.x, vy = vi.y, vz = vi.z;
@@ -1439,32 +1546,33 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     const float4 wi = som[p];
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     // e = (m / rho_j', |omega_j|) of the candidate.
-    auto term = [&](const float4& xj, const float4& e) {
+    auto term = [&](const float4& xj, const float4& e, auto L) {
         float rx, ry, rz;
         const float r_sq = rel_sq(xi, xj, rx, ry, rz);
         if (r_sq < C.cut) {
             const float c = spiky_coeff(r_sq, C);
             const float a = e.x * (e.y - wi.w);
-            ex += a * (c * rx);
-            ey += a * (c * ry);
-            ez += a * (c * rz);
+            ex = acc(ex, a * (c * rx), L);
+            ey = acc(ey, a * (c * ry), L);
+            ez = acc(ez, a * (c * rz), L);
         }
     };
     if constexpr (B::kOn) {
         if (coop)
-            coop_walk<coop_chunk(BS), true, false, false>(
+            coop_walk<coop_chunk(BS), true, false, false, true>(
                 sm[threadIdx.x >> 5], R, cell.x, xi, xin, C.cut, C.grid, G.off,
                 [&](uint32_t q) {
                     return make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f);
                 },
-                term);
+                [&](const float4& xj, const float4& e) { term(xj, e, One{}); },
+                [&](const float4& xj, const float4& e, uint32_t L) { term(xj, e, L); });
     }
     if (!coop) {
         for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
             const float4 xj = __ldg(xin + q);
             float rx, ry, rz;
             if (rel_sq(xi, xj, rx, ry, rz) < C.cut)
-                term(xj, make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f));
+                term(xj, make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f), One{});
         });
     }
     const float el = sqrtf(sqn(ex, ey, ez));

@@ -105,3 +105,37 @@ def test_density_first_walk_equals_single_walk(port_mt, exact):
         want = port_mt.steps(Settings.make(**w.settings), w.x, w.v, z, z, w.dt, w.gravity,
                              w.mass, 1)
         assert_equal(runs[2], want, "oracle")
+
+
+def clump_block(nclump, seed=9):
+    """The 64^3 lattice with nclump extra particles at one point, bit for bit
+    (x, v = 0), inside the block in cell (5, 5, 5): half of them inserted in
+    the index order between the lattice's z-layers 21 and 22 (so members of
+    that cell sit between the two halves in cell order) and half at the end."""
+    w = workloads.dam_break((64, 64, 64), 0.01, (4.0, 2.0, 2.0), dt=1.0 / 240.0, jitter=1e-5,
+                            seed=seed, vorticity=1e-4)
+    p = np.full((nclump, 3), 0.205, np.float32)
+    half = nclump // 2
+    cut = 64 * 64 * 22
+    w.x = np.concatenate([w.x[:cut], p[:half], w.x[cut:], p[half:]]).astype(np.float32)
+    w.v = np.zeros_like(w.x)
+    return w
+
+
+@pytest.mark.parametrize("nsteps", [1, 2])
+def test_runs_of_identical_particles(port_mt, nsteps):
+    """Particles with bit-identical state add identical terms one after another;
+    the XSPH and vorticity passes' cooperative walk adds such a run's term as
+    many times as it has particles in one exact repeated addition (rows of at
+    least 1,024 candidates).  Two runs of 1,500 in one cell, with members of
+    the lattice between them: the oracle's bits after one and two steps."""
+    w = clump_block(3000)
+    assert w.n >= 1 << 18
+    assert_equal(*run_both(port_mt, w, nsteps), ("runs", nsteps))
+
+
+def test_runs_with_default_scorr(port_mt):
+    """The same with PBFSettings' own s_corr."""
+    w = clump_block(2400, seed=10)
+    got, want = run_both(port_mt, w, 2, corr_k=0.001, corr_delta_q=0.3)
+    assert_equal(got, want, "runs default s_corr")
