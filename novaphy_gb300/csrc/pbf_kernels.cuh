@@ -101,15 +101,17 @@ __device__ __forceinline__ float spiky_coeff(float r_sq, const StepConsts& C) {
 
 // Adding a term to a running sum once (One) or m times in a row (a run of
 // identical candidates in the cooperative walk): acc(s, t, m) is the float
-// that m single additions of t leave, bit for bit.
+// that m single additions of t leave, bit for bit.  (rep_add is inlined: as
+// a call, the calling convention's saved registers cost the walk's hot
+// loops spills.)
 struct One {};
 __device__ __forceinline__ float acc(float s, float t, One) { return s + t; }
+__device__ __forceinline__ float acc(float s, float t, uint32_t m) { return rep_add(s, t, m); }
+
 __device__ __forceinline__ bool bits_equal(const float4 a, const float4 b) {
     return __float_as_uint(a.x) == __float_as_uint(b.x) && __float_as_uint(a.y) == __float_as_uint(b.y) &&
            __float_as_uint(a.z) == __float_as_uint(b.z) && __float_as_uint(a.w) == __float_as_uint(b.w);
 }
-__device__ __forceinline__ float acc_n(float s, float t, uint32_t m) { return rep_add(s, t, m); }
-__device__ __forceinline__ float acc(float s, float t, uint32_t m) { return acc_n(s, t, m); }
 
 // ---------------------------------------------------------------------------
 // Grid helpers
