@@ -7,12 +7,13 @@
 // t / u (for a tie, the choice that leaves |s| / u even).  D stays the same
 // for every later sum while the exact sums stay in the binade (and, for a
 // tie, while |s| / u stays even, which a tie's rounding makes it), so those
-// additions collapse into one multiplication, counted and applied in double
-// precision where every value involved is exact.  Each loop pass does one
-// real float addition (which also settles zeros, signs, infinities and NaN
-// exactly as the plain loop would) and then one such jump; the binade changes
-// a few dozen times at most.  Subnormal sums, the top binade and steps of
-// more than half of |s| are left to single additions.
+// additions collapse into one multiplication, counted in 64-bit integers in
+// units of u / 2^25, where every value involved is exact.  Each loop pass
+// does one real float addition (which also settles zeros, signs, infinities
+// and NaN exactly as the plain loop would) and then one such jump; the binade
+// changes a few dozen times at most.  Subnormal sums, the top binade, terms
+// of more than a quarter of |s| and runs of up to 16 are left to single
+// additions.
 //
 // Used for runs of identical terms: particles with bit-identical state (the
 // domain clamp piles fluid into a box corner) add identical terms to every
@@ -30,59 +31,58 @@
 
 namespace pbf {
 
-PBF_HD inline double rep_floor(double x) {
-    // floor of |x| < 2^52 without the math library (exact: the cast truncates).
-    const double t = (double)(long long)x;
-    return (t > x) ? t - 1.0 : t;
+PBF_HD inline uint32_t rep_bits(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, sizeof b);
+    return b;
 }
 
-PBF_HD inline double rep_pow2(int e) {
-    // 2^e for -1022 <= e <= 1023, from the bits.
-    const unsigned long long b = (unsigned long long)(e + 1023) << 52;
-    double d;
-    std::memcpy(&d, &b, sizeof d);
-    return d;
+PBF_HD inline float rep_float(uint32_t b) {
+    float x;
+    std::memcpy(&x, &b, sizeof x);
+    return x;
 }
 
 PBF_HD inline float rep_add(float s, float t, uint32_t m) {
-    while (m > 0) {
+    if (m <= 16u) {  // short runs: the additions themselves are cheaper
+        for (; m > 0u; --m) s = s + t;
+        return s;
+    }
+    while (m > 0u) {
         const float s1 = s + t;
         --m;
-        if (m == 0 || s1 != s1 || s1 == s) return s1;  // done, NaN, or absorbed
+        if (m == 0u || s1 != s1 || s1 == s) return s1;  // done, NaN, or absorbed
         s = s1;
-        uint32_t bits;
-        std::memcpy(&bits, &s, sizeof bits);
-        const int ex = (int)((bits >> 23) & 0xffu);  // biased exponent of |s|
-        if (ex < 1 || ex > 253) continue;  // |s| subnormal, or in the top binade
-        const double A = (double)(s < 0.0f ? -s : s);  // |s|
-        const double T = (s < 0.0f) ? -(double)t : (double)t;  // t as |s| sees it
-        if (!(T < A * 0.5 && T > -A * 0.5)) continue;  // large steps: a few single adds
-        const int e = ex - 127;
-        const double u = rep_pow2(e - 23), lo = rep_pow2(e), hi = rep_pow2(e + 1);
-        const double a = A / u;  // an integer below 2^24
-        const double x = a + T / u;
-        const double fl = rep_floor(x);
-        const double fr = x - fl;
-        double r;
-        if (fr > 0.5) r = fl + 1.0;
-        else if (fr < 0.5) r = fl;
-        else r = (rep_floor(fl * 0.5) * 2.0 == fl) ? fl : fl + 1.0;
-        const double D = r - a;
-        if (D == 0.0) return s;  // absorbed from here on
-        if (fr == 0.5 && rep_floor(D * 0.5) * 2.0 != D) continue;  // parity flips: step singly
-        // Additions j = 0, 1, ... whose exact sum A + j D u + T stays in [lo, hi).
-        double k;
-        if (D > 0.0) {
-            k = rep_floor((hi - A - T) / (D * u)) + 1.0;
-            while (k > 0.0 && !(A + (k - 1.0) * D * u + T < hi)) k -= 1.0;
-        } else {
-            k = rep_floor((A + T - lo) / (-D * u)) + 1.0;
-            while (k > 0.0 && !(A + (k - 1.0) * D * u + T >= lo)) k -= 1.0;
-        }
-        if (k <= 0.0) continue;
-        if (k > (double)m) k = (double)m;
-        const float An = (float)(A + k * D * u);
-        s = (s < 0.0f) ? -An : An;
+        const uint32_t sb = rep_bits(s), tb = rep_bits(t);
+        const int es = (int)((sb >> 23) & 0xffu), et = (int)((tb >> 23) & 0xffu);
+        // Single additions for subnormal or top-binade sums, subnormal or
+        // non-finite terms, and terms of more than a quarter of |s|.
+        if (es < 1 || es > 253 || et < 1 || et == 255) continue;
+        const int d = es - et;
+        if (d < 2) continue;
+        if (d > 24) return s;  // |t| < u / 2: absorbed from here on
+        // In units of u / 2^25 (u = 2^(es - 150), the spacing of the binade):
+        // |s| = S u exactly, and x = S + t' / u with t' = t as |s| sees it.
+        const int64_t S = (int64_t)((sb & 0x7fffffu) | 0x800000u);
+        const int64_t MT = (int64_t)((tb & 0x7fffffu) | 0x800000u);
+        const int64_t one = (int64_t)1 << 25, half = one >> 1;
+        const int64_t X = (S << 25) + (((sb ^ tb) >> 31) ? -(MT << (25 - d)) : (MT << (25 - d)));
+        const int64_t fl = X >> 25, fr = X & (one - 1);
+        const int64_t r = fr > half ? fl + 1 : (fr < half ? fl : ((fl & 1) ? fl + 1 : fl));
+        const int64_t D = r - S;  // the rounded step, in units of u
+        if (D == 0) return s;
+        if (fr == half && (D & 1)) continue;  // a tie flips the parity: step singly
+        // Additions j = 0, 1, ... whose exact sum stays in the binade [2^23, 2^24) u.
+        const int64_t LO = (int64_t)1 << 48, HI = (int64_t)1 << 49;
+        int64_t k;
+        if (D > 0) k = X < HI ? (HI - 1 - X) / (D << 25) + 1 : 0;
+        else k = X >= LO ? (X - LO) / ((-D) << 25) + 1 : 0;
+        if (k <= 0) continue;
+        if (k > (int64_t)m) k = (int64_t)m;
+        const int64_t A = S + k * D;  // |s| / u after the k additions, in [2^23, 2^24]
+        const uint32_t mag = A == ((int64_t)1 << 24) ? (uint32_t)(es + 1) << 23
+                                                     : ((uint32_t)es << 23) | (uint32_t)(A - 0x800000);
+        s = rep_float(mag | (sb & 0x80000000u));
         m -= (uint32_t)k;
     }
     return s;

@@ -181,11 +181,13 @@ int ensure_work(pbf_scene* s) {
     s->wmem = s->smem = nullptr;
     s->work_cap = 0;
     const int c = s->cap > 0 ? s->cap : 1;
-    const size_t wb = work_bytes(c);
+    // The step scratch batches share, then the scene's run ends.
+    const size_t wb = work_bytes(c) + align_up((size_t)c * 4, 256);
     int rc = pool_alloc(&s->wmem, wb, s->device, s->stream);
     if (rc) return rc;
     PBF_CUDA(cudaMemsetAsync(s->wmem, 0, wb, s->stream));
     bind_work(s->B, s->wmem, c);
+    s->B.segend = reinterpret_cast<uint32_t*>(static_cast<char*>(s->wmem) + work_bytes(c));
     const size_t sb = sort_scratch_bytes(c);
     rc = pool_alloc(&s->smem, sb, s->device, s->stream);
     if (rc) return rc;
@@ -828,7 +830,9 @@ size_t scene_device_bytes(const pbf_scene* s) {
         b += 2 * align_up((size_t)c * 16, 256) + 2 * align_up((size_t)c * 4, 256) +
              align_up((size_t)c * 12, 256);
     }
-    if (s->wmem) b += work_bytes(s->work_cap) + sort_scratch_bytes(s->work_cap);
+    if (s->wmem)
+        b += work_bytes(s->work_cap) + align_up((size_t)s->work_cap * 4, 256) +
+             sort_scratch_bytes(s->work_cap);
     if (s->off)
         b += align_up((size_t)s->off_cap * 4, 256) + align_up(s->off_cap, 256) +
              (size_t)s->off_cap * 8 + 4 * kWalkHist * 4;

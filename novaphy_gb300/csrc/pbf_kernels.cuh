@@ -41,6 +41,16 @@ constexpr int kBigScene = 1 << 17;
 constexpr uint32_t kRunRow = 1024;
 constexpr uint32_t kNoBucket = 0xffffffffu;
 constexpr uint32_t kImpureBit = 0x80000000u;
+// Flags in a particle's owner word (StepBuffers::sown) for runs of identical
+// particles (k_segments): the particle only copies the results of its run's
+// first particle (kCopyBit), or it is a run's first particle (kLeadBit).  The
+// owner row itself takes the low 30 bits.
+constexpr uint32_t kCopyBit = 0x40000000u;
+constexpr uint32_t kLeadBit = 0x80000000u;
+constexpr uint32_t kOwnerMask = 0x3fffffffu;
+// Set in a slot's alias byte (StepBuffers::slot_alias, bit 0: alias) when the
+// slot holds a run's first particle.
+constexpr unsigned char kRunSlot = 2;
 
 // ---------------------------------------------------------------------------
 // SPH kernels (include/novaphy/fluid/sph_kernel.h:24-46)
@@ -320,6 +330,80 @@ k_gather(const uint32_t* __restrict__ sidx, float4* __restrict__ sx, float4* __r
     if (!in_grid(cx, cy, cz, C.grid)) slot_alias[slot_of(cx, cy, cz, C.grid)] = 1;
 }
 
+// Runs of particles with bit-identical step state (x, x* and lambda and rho
+// as gathered) next to each other in cell order.  Everything a step computes
+// for a particle follows from that state and from its candidates, which are
+// those of its cell, so the particles of a run come out identical in every
+// pass: only the run's first particle computes, and writes its results for
+// the others too (their owner words get kCopyBit, the first one's segend the
+// run's end).  Such runs form where the domain clamp piles fluid into a box
+// corner, bit for bit: tens of thousands of particles, each of which would
+// otherwise sum over all the others.  One warp per 32 positions; a warp with
+// a run's first particle finds the run's end, 256 positions per round.
+struct StepState {
+    const float4* __restrict__ sx;
+    const float4* __restrict__ xa;
+    const float* __restrict__ srho;
+    int n;
+    __device__ __forceinline__ bool same(int a, int b) const {
+        const float4 x0 = sx[a], x1 = sx[b], y0 = xa[a], y1 = xa[b];
+        return __float_as_uint(x0.x) == __float_as_uint(x1.x) &&
+               __float_as_uint(x0.y) == __float_as_uint(x1.y) &&
+               __float_as_uint(x0.z) == __float_as_uint(x1.z) &&
+               __float_as_uint(y0.x) == __float_as_uint(y1.x) &&
+               __float_as_uint(y0.y) == __float_as_uint(y1.y) &&
+               __float_as_uint(y0.z) == __float_as_uint(y1.z) &&
+               __float_as_uint(y0.w) == __float_as_uint(y1.w) &&
+               __float_as_uint(srho[a]) == __float_as_uint(srho[b]);
+    }
+};
+
+__global__ void __launch_bounds__(256)
+k_segments(const StepState S, const int4* __restrict__ scell, const GridDesc Gd,
+           int* __restrict__ sown, unsigned char* __restrict__ slot_alias,
+           uint32_t* __restrict__ segend) {
+    const unsigned full = 0xffffffffu;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool in = p < S.n;
+    const bool prev = in && p > 0 && S.same(p, p - 1);
+    const bool next = in && p + 1 < S.n && S.same(p + 1, p);
+    if (prev) sown[p] = (int)((uint32_t)sown[p] | kCopyBit);
+    if (in && !prev && next) {
+        sown[p] = (int)((uint32_t)sown[p] | kLeadBit);
+        const int4 c = scell[p];
+        unsigned char* a = slot_alias + slot_of(c.x, c.y, c.z, Gd);
+        *a = (unsigned char)(*a | kRunSlot);
+    }
+    uint32_t end = 0u;
+    uint32_t firsts = __ballot_sync(full, in && !prev && next);
+    while (firsts) {
+        const int l = __ffs(firsts) - 1;
+        firsts &= firsts - 1u;
+        // Positions from the first one's successor on, 8 per lane per round,
+        // while each equals its predecessor.
+        int base = (p - lane) + l + 1;
+        int e = S.n;
+        for (;;) {
+            int fail = 8;
+#pragma unroll
+            for (int j = 7; j >= 0; --j) {
+                const int q = base + lane * 8 + j;
+                if (!(q < S.n && S.same(q, q - 1))) fail = j;
+            }
+            const uint32_t m = __ballot_sync(full, fail < 8);
+            if (m) {
+                const int fl = __ffs(m) - 1;
+                e = base + fl * 8 + __shfl_sync(full, fail, fl);
+                break;
+            }
+            base += 256;
+        }
+        if (lane == l) end = (uint32_t)e;
+    }
+    if (in) segend[p] = end;
+}
+
 // Reference buckets in key-sorted order: kpos maps key-sorted positions to
 // cell-sorted ones; at each bucket start, bend holds the bucket end with
 // kImpureBit set when the bucket mixes cells (hash collision).  With scene
@@ -492,7 +576,108 @@ struct Grid {
     uint32_t* lamnz;                     // per slot, see StepBuffers::lamnz
     BoundaryGrid bg;                     // two-way coupled steps only
     uint32_t* dhist;                     // see StepBuffers::dhist
+    const uint32_t* segend;              // see StepBuffers::segend (large single scenes)
+    const unsigned char* slot_alias;     // with kRunSlot where segend is set
 };
+
+// for_each_candidate over a single scene's step with runs of identical
+// particles (k_segments): in a cell range or a one-cell bucket of at least
+// kRunRow candidates, a run's first particle q calls fr(q, L) for the run's L
+// particles, which come next in the candidate order (the run lies in one
+// cell, in cell order), and the walk goes on after them.
+template <int U, bool kRuns, class F, class FR>
+__device__ __forceinline__ void for_each_candidate_runs(const int4 cell, const Grid& G,
+                                                        const StepConsts& C, F&& f, FR&& fr) {
+    if constexpr (!kRuns) {
+        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, f);
+        return;
+    }
+    if (!G.segend) {
+        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, f);
+        return;
+    }
+    const GridDesc& Gd = C.grid;
+    // Slots [s, s + k) of a cell range [q, q1): only ranges with a run's
+    // first particle read the run flags of their candidates.
+    auto range = [&](uint32_t q, uint32_t q1, uint32_t s, int k) {
+        bool any = false;
+        if (q1 - q >= kRunRow)
+            for (int d = 0; d < k; ++d) any |= (__ldg(G.slot_alias + s + d) & kRunSlot) != 0;
+        if (!any) {
+#pragma unroll U
+            for (; q < q1; ++q) f(q);
+            return;
+        }
+        while (q < q1) {
+            if ((uint32_t)__ldg(G.sown + q) & kLeadBit) {
+                const uint32_t e = __ldg(G.segend + q);
+                fr(q, e - q);
+                q = e;
+            } else {
+                f(q);
+                ++q;
+            }
+        }
+    };
+    if (cell.w == 0) {
+        for (int dz = -1; dz <= 1; ++dz) {
+            const uint32_t wz = (uint32_t)wrap(cell.z + dz, Gd.oz, Gd.gz);
+            for (int dy = -1; dy <= 1; ++dy) {
+                const uint32_t wy = (uint32_t)wrap(cell.y + dy, Gd.oy, Gd.gy);
+                const uint32_t row = Gd.base + (uint32_t)Gd.gx * (wy + (uint32_t)Gd.gy * wz);
+                const int wx = wrap(cell.x - 1, Gd.ox, Gd.gx);
+                if (wx + 2 < Gd.gx) {
+                    range(__ldg(G.off + row + wx), __ldg(G.off + row + wx + 3), row + wx, 3);
+                } else {
+                    for (int d = 0; d < 3; ++d) {
+                        const uint32_t s = row + (uint32_t)wrap(cell.x - 1 + d, Gd.ox, Gd.gx);
+                        range(__ldg(G.off + s), __ldg(G.off + s + 1), s, 1);
+                    }
+                }
+            }
+        }
+    } else {
+        const uint32_t* row = G.btab + (size_t)(uint32_t)(cell.w - 1) * 27u;
+        for (int k = 0; k < 27; ++k) {
+            const uint32_t b0 = __ldg(row + k);
+            if (b0 == kNoBucket) continue;
+            const uint32_t be = __ldg(G.bend + b0);
+            const uint32_t b1 = be & ~kImpureBit;
+            bool any = false;
+            if (!(be & kImpureBit) && b1 - b0 >= kRunRow) {
+                const int4 c = G.scell[__ldg(G.kpos + b0)];
+                any = (__ldg(G.slot_alias + slot_of(c.x, c.y, c.z, Gd)) & kRunSlot) != 0;
+            }
+            if (!any) {
+                for (uint32_t kq = b0; kq < b1; ++kq) f(__ldg(G.kpos + kq));
+                continue;
+            }
+            // One cell's members, in cell order: a run's particles follow its
+            // first one here too.
+            for (uint32_t kq = b0; kq < b1;) {
+                const uint32_t q = __ldg(G.kpos + kq);
+                if ((uint32_t)__ldg(G.sown + q) & kLeadBit) {
+                    const uint32_t L = __ldg(G.segend + q) - q;
+                    fr(q, L);
+                    kq += L;
+                } else {
+                    f(q);
+                    ++kq;
+                }
+            }
+        }
+    }
+}
+
+// The run flags of sorted particle p (kCopyBit, kLeadBit).
+__device__ __forceinline__ uint32_t run_flags(const Grid& G, uint32_t p) {
+    return (uint32_t)G.sown[p] & ~kOwnerMask;
+}
+
+// One past the last particle of the run p leads (p + 1 when it leads none).
+__device__ __forceinline__ uint32_t run_end(const Grid& G, uint32_t p, uint32_t flags) {
+    return (flags & kLeadBit) ? __ldg(G.segend + p) : p + 1;
+}
 
 // The cell of sorted particle p against the boundary index (two-way steps).
 __device__ __forceinline__ int4 boundary_cell(const Grid& G, uint32_t p, const int4 cell) {
@@ -502,7 +687,7 @@ __device__ __forceinline__ int4 boundary_cell(const Grid& G, uint32_t p, const i
 
 __device__ __forceinline__ int4 cell_at(const Grid& G, uint32_t p) {
     int4 c = G.scell[p];
-    c.w = G.sown[p];
+    c.w = (int)((uint32_t)G.sown[p] & kOwnerMask);
     return c;
 }
 
@@ -974,14 +1159,16 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     constexpr bool kCoop = CoopBlock<P, 32, false, U>::kOn;
     const uint32_t pa = active ? p : 0u;
     const StepConsts& C = prm.at(G.spid, pa);
-    bool live = active && it < C.iters;
     const int4 cell = cell_at(G, pa);
+    const uint32_t rf = run_flags(G, pa);
+    bool live = active && it < C.iters && !(rf & kCopyBit);
     if (live && it > 0 && G.moved && cell.w == 0 &&
         !neighbourhood_moved<kPersist>(cell, C.grid, G.moved, it)) {
         // Nothing around moved since the last density pass: keep its rho
         // (srho) and lambda (x*.w, which the delta pass carried through).
         const float4 keep = xin[p];
         xout[p] = keep;
+        for (uint32_t m = p + 1, e = run_end(G, p, rf); m < e; ++m) xout[m] = keep;
         if (G.lamnz && keep.w != 0.0f)
             G.lamnz[slot_of(cell.x, cell.y, cell.z, C.grid)] = (uint32_t)it + 1u;
         live = false;
@@ -1078,8 +1265,9 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
         }
     }
     if (!coop)
-        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
-                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); });
+        for_each_candidate_runs<U, std::is_same<P, OneScene>::value>(
+            cell, G, C, [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); },
+            [&](uint32_t q, uint32_t L) { term(ld_step<kPersist>(xin + q), L); });
     if (G.bg.spos) {
         // Two-way coupling (no counterpart in the reference): after the fluid
         // terms, the boundary's Akinci density rho0 psi_b W and its gradient
@@ -1111,6 +1299,10 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     if (G.lamnz && lam != 0.0f) G.lamnz[slot_of(cell.x, cell.y, cell.z, C.grid)] = (uint32_t)it + 1u;
     srho[p] = density;
     xout[p] = make_float4(xi.x, xi.y, xi.z, lam);
+    for (uint32_t m = p + 1, e = run_end(G, p, rf); m < e; ++m) {
+        srho[m] = density;
+        xout[m] = make_float4(xi.x, xi.y, xi.z, lam);
+    }
 }
 
 template <int BS, class P, int U = 4>
@@ -1155,8 +1347,9 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     constexpr bool kCoop = CoopBlock<P, 32, false, U>::kOn;
     const uint32_t pa = active ? p : 0u;
     const StepConsts& C = prm.at(G.spid, pa);
-    const bool live = active && it < C.iters;
     const int4 cell = cell_at(G, pa);
+    const uint32_t rf = run_flags(G, pa);
+    const bool live = active && it < C.iters && !(rf & kCopyBit);
     float4 xi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     bool walk = live;
     if (live) {
@@ -1206,8 +1399,9 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
         }
     }
     if (walk && !coop)
-        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C,
-                              [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); });
+        for_each_candidate_runs<U, std::is_same<P, OneScene>::value>(
+            cell, G, C, [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); },
+            [&](uint32_t q, uint32_t L) { term(ld_step<kPersist>(xin + q), L); });
     if (G.bg.spos && xi.w != 0.0f) {
         // Two-way coupling: the boundary's share of the position correction,
         // lambda_i (rho0 psi_b) grad W, after the fluid terms (zero when
@@ -1234,7 +1428,12 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
                     __float_as_uint(py) != __float_as_uint(xi.y) ||
                     __float_as_uint(pz) != __float_as_uint(xi.z)))
         G.moved[slot_of(cell.x, cell.y, cell.z, C.grid)] = (uint32_t)it + 1u;
-    if (it == C.iters - 1) sv[p] = update_velocity(px, py, pz, sx[p], srho[p], C);
+    float4 vu = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (it == C.iters - 1) sv[p] = vu = update_velocity(px, py, pz, sx[p], srho[p], C);
+    for (uint32_t m = p + 1, e = run_end(G, p, rf); m < e; ++m) {
+        xout[m] = make_float4(px, py, pz, xi.w);
+        if (it == C.iters - 1) sv[m] = vu;
+    }
 }
 
 template <int BS, class P, int U = 4>
@@ -1414,8 +1613,9 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
     const bool active = p < (uint32_t)n;
     const uint32_t pa = active ? p : 0u;
     const StepConsts& C = prm.at(G.spid, pa);
-    const bool live = active && !(skip_vort && C.vort_on);
     const int4 cell = cell_at(G, pa);
+    const uint32_t rf = run_flags(G, pa);
+    const bool live = active && !(skip_vort && C.vort_on) && !(rf & kCopyBit);
     CoopRow R;
     bool coop = false;
     if constexpr (B::kOn) coop = coop_row(live && C.xsph_on, cell, C.grid, R, scene_at(G, pa));
@@ -1444,17 +1644,21 @@ k_xsph_commit(const float4* __restrict__ xin, const float4* __restrict__ sv, con
                     [&](const float4& xj, const float4& vj, uint32_t L) { term(xj, vj, L); });
         }
         if (!coop) {
-            for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+            auto one = [&](uint32_t q, auto L) {
                 const float4 xj = __ldg(xin + q);
                 float rx, ry, rz;
-                if (rel_sq(xi, xj, rx, ry, rz) < C.h2) term(xj, __ldg(sv + q), One{});
-            });
+                if (rel_sq(xi, xj, rx, ry, rz) < C.h2) term(xj, __ldg(sv + q), L);
+            };
+            for_each_candidate_runs<U, false>(
+                cell, G, C, [&](uint32_t q) { one(q, One{}); },
+                [&](uint32_t q, uint32_t L) { one(q, L); });
         }
         vx = vi.x + C.xsph_c * cx;
         vy = vi.y + C.xsph_c * cy;
         vz = vi.z + C.xsph_c * cz;
     }
-    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, prm.state(G.spid, p), n, C);
+    for (uint32_t m = p, e = run_end(G, p, rf); m < e; ++m)
+        commit(m, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, prm.state(G.spid, m), n, C);
 }
 
 // XSPH correction + vorticity omega in one candidate pass (vorticity path).
@@ -1471,8 +1675,9 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
     const bool active = p < (uint32_t)n;
     const uint32_t pa = active ? p : 0u;
     const StepConsts& C = prm.at(G.spid, pa);
-    const bool live = active && C.vort_on;
     const int4 cell = cell_at(G, pa);
+    const uint32_t rf = run_flags(G, pa);
+    const bool live = active && C.vort_on && !(rf & kCopyBit);
     CoopRow R;
     bool coop = false;
     if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R, scene_at(G, pa));
@@ -1507,11 +1712,14 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
                 [&](const float4& xj, const float4& vj, uint32_t L) { term(xj, vj, L); });
     }
     if (!coop) {
-        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+        auto one = [&](uint32_t q, auto L) {
             const float4 xj = __ldg(xin + q);
             float rx, ry, rz;
-            if (rel_sq(xi, xj, rx, ry, rz) < C.cut) term(xj, __ldg(sv + q), One{});
-        });
+            if (rel_sq(xi, xj, rx, ry, rz) < C.cut) term(xj, __ldg(sv + q), L);
+        };
+        for_each_candidate_runs<U, false>(
+            cell, G, C, [&](uint32_t q) { one(q, One{}); },
+            [&](uint32_t q, uint32_t L) { one(q, L); });
     }
     float vx = vi.x, vy = vi.y, vz = vi.z;
     if (C.xsph_on) {
@@ -1519,8 +1727,11 @@ k_xsph_omega(const float4* __restrict__ xin, const float4* __restrict__ sv, floa
         vy = vi.y + C.xsph_c * cy;
         vz = vi.z + C.xsph_c * cz;
     }
-    sv2[p] = make_float4(vx, vy, vz, 0.0f);
-    som[p] = make_float4(wx, wy, wz, sqrtf(sqn(wx, wy, wz)));
+    const float4 o = make_float4(wx, wy, wz, sqrtf(sqn(wx, wy, wz)));
+    for (uint32_t m = p, e = run_end(G, p, rf); m < e; ++m) {
+        sv2[m] = make_float4(vx, vy, vz, 0.0f);
+        som[m] = o;
+    }
 }
 
 // Vorticity confinement (Macklin & Mueller 2013, section 5) + commit:
@@ -1538,8 +1749,9 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     const bool active = p < (uint32_t)n;
     const uint32_t pa = active ? p : 0u;
     const StepConsts& C = prm.at(G.spid, pa);
-    const bool live = active && C.vort_on;
     const int4 cell = cell_at(G, pa);
+    const uint32_t rf = run_flags(G, pa);
+    const bool live = active && C.vort_on && !(rf & kCopyBit);
     CoopRow R;
     bool coop = false;
     if constexpr (B::kOn) coop = coop_row(live, cell, C.grid, R, scene_at(G, pa));
@@ -1570,12 +1782,15 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
                 [&](const float4& xj, const float4& e, uint32_t L) { term(xj, e, L); });
     }
     if (!coop) {
-        for_each_candidate<U>(cell, G.off, G.kpos, G.bend, G.btab, C, [&](uint32_t q) {
+        auto one = [&](uint32_t q, auto L) {
             const float4 xj = __ldg(xin + q);
             float rx, ry, rz;
             if (rel_sq(xi, xj, rx, ry, rz) < C.cut)
-                term(xj, make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f), One{});
-        });
+                term(xj, make_float4(__ldg(sv + q).w, __ldg(som + q).w, 0.0f, 0.0f), L);
+        };
+        for_each_candidate_runs<U, false>(
+            cell, G, C, [&](uint32_t q) { one(q, One{}); },
+            [&](uint32_t q, uint32_t L) { one(q, L); });
     }
     const float el = sqrtf(sqn(ex, ey, ez));
     float nx = 0.0f, ny = 0.0f, nz = 0.0f;
@@ -1591,7 +1806,8 @@ k_vorticity_commit(const float4* __restrict__ xin, const float4* __restrict__ sv
     const float vx = vb.x + C.vort_scale * fx;
     const float vy = vb.y + C.vort_scale * fy;
     const float vz = vb.z + C.vort_scale * fz;
-    commit(p, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, prm.state(G.spid, p), n, C);
+    for (uint32_t m = p, e = run_end(G, p, rf); m < e; ++m)
+        commit(m, xi.x, xi.y, xi.z, vx, vy, vz, xi.w, sx, srho, prm.state(G.spid, m), n, C);
 }
 
 // ---------------------------------------------------------------------------
@@ -1642,7 +1858,7 @@ inline int grid_of(int n, int b) { return (n + b - 1) / b; }
 inline Grid grid_view(const StepBuffers& B, const uint32_t* spid = nullptr,
                       const BoundaryGrid& bg = BoundaryGrid{}) {
     return Grid{B.scell, B.sown, B.off, B.kpos, B.bend, B.btab, spid, B.moved, B.lamnz, bg,
-                spid ? nullptr : B.dhist};
+                spid ? nullptr : B.dhist, nullptr, B.slot_alias};
 }
 
 // predict, sort by cell and by reference key, cell offsets, gather, reference
@@ -1821,7 +2037,17 @@ inline cudaError_t enqueue_step(const StepBuffers& B, const StepConsts& C, int i
     Ci.iters = iters;
     BoundaryGrid bgs = bg ? *bg : BoundaryGrid{};
     if (bg) bgs.sx = B.sx;
-    return enqueue_passes(B, grid_view(B, nullptr, bgs), n, iters, iters <= 0, C.vort_on != 0,
+    Grid G = grid_view(B, nullptr, bgs);
+    if (B.segend && n >= kBigScene) {
+        // Runs of identical particles: from here on the owner words of the
+        // run's later particles carry kCopyBit, which only the passes below
+        // understand (they skip those particles).
+        k_segments<<<grid_of(n, 256), 256, 0, st>>>(StepState{B.sx, B.xa, B.srho, n}, B.scell,
+                                                    C.grid, B.sown, B.slot_alias, B.segend);
+        if (pm) pm->mark(kPhaseNeighborQuery, 1, st);
+        G.segend = B.segend;
+    }
+    return enqueue_passes(B, G, n, iters, iters <= 0, C.vort_on != 0,
                           C.vort_on == 0,
                           C.xsph_on != 0, OneScene{Ci, StateRef{B.x, B.v, B.rho, B.lam, 0u, nullptr}}, st,
                           pm);

@@ -122,6 +122,10 @@ struct StepBuffers {
     // the previous step ([0, 2 kWalkHist)) and in this one (the rest).
     // Single scenes only (null in batches).
     uint32_t* dhist;
+    // Per sorted position: for the first particle of a run of particles with
+    // bit-identical step state in cell order, one past the run's last; 0
+    // elsewhere (see k_segments).  Single scenes only (null in batches).
+    uint32_t* segend;
     uint32_t* err;  // device status word
 };
 

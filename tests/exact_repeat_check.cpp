@@ -41,6 +41,13 @@ int main(int argc, char** argv) {
         float s = (float)(t * (U(g) * 200 - 100));
         check(s, t, (uint32_t)(U(g) * 100000));
     }
+    for (int i = 0; i < 4000; ++i) {  // every exponent gap, both signs, long runs
+        const int d = 1 + (int)(U(g) * 27);
+        float s = (float)(std::ldexp(1.0 + U(g), (int)(U(g) * 80) - 40) * (U(g) < 0.5 ? -1 : 1));
+        float t = (float)(std::ldexp(std::fabs((double)s) * (1.0 + U(g)), -d) * (U(g) < 0.5 ? -1 : 1));
+        if (i % 5 == 0) t = (float)std::ldexp(std::floor(std::ldexp(std::fabs((double)t), 3)) + 0.5, -3);
+        check(s, t, 17 + (uint32_t)(U(g) * 200000));
+    }
     const float sp[] = {0.0f, -0.0f, 1.0f, -1.0f, 3.0e38f, -3.0e38f, INFINITY, -INFINITY, NAN, 1e-40f, -1e-44f, 1e-38f};
     for (float s : sp) for (float t : sp) for (uint32_t m : {0u, 1u, 2u, 3u, 17u, 1000u}) check(s, t, m);
     check(0.0f, 1e-3f, 54000); check(0.0f, 0.1f, 1u << 22); check(1.0f, 1e-8f, 100); check(16777215.0f, 0.5f, 10);
