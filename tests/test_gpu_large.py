@@ -124,9 +124,10 @@ def clump_block(nclump, seed=9):
 
 @pytest.mark.parametrize("nsteps", [1, 2])
 def test_runs_of_identical_particles(port_mt, nsteps):
-    """Particles with bit-identical state add identical terms one after another;
-    the XSPH and vorticity passes' cooperative walk adds such a run's term as
-    many times as it has particles in one exact repeated addition (rows of at
+    """Particles with bit-identical state next to each other in cell order
+    (runs) come out identical: the run's first particle computes and writes
+    its results for the others, and as candidates the run's particles add
+    their term in one exact repeated addition (cell ranges and rows of at
     least 1,024 candidates).  Two runs of 1,500 in one cell, with members of
     the lattice between them: the oracle's bits after one and two steps."""
     w = clump_block(3000)
