@@ -117,6 +117,13 @@ __device__ __forceinline__ float spiky_coeff(float r_sq, const StepConsts& C) {
 struct One {};
 __device__ __forceinline__ float acc(float s, float t, One) { return s + t; }
 __device__ __forceinline__ float acc(float s, float t, uint32_t m) { return rep_add(s, t, m); }
+// The same as a call (the constraint passes' one-thread walks, where the
+// inlined loop cost the density pass's hot loops registers).
+struct Many {
+    uint32_t n;
+};
+__device__ __noinline__ float rep_add_call(float s, float t, uint32_t m) { return rep_add(s, t, m); }
+__device__ __forceinline__ float acc(float s, float t, Many m) { return rep_add_call(s, t, m.n); }
 
 __device__ __forceinline__ bool bits_equal(const float4 a, const float4 b) {
     return __float_as_uint(a.x) == __float_as_uint(b.x) && __float_as_uint(a.y) == __float_as_uint(b.y) &&
@@ -1267,7 +1274,7 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
     if (!coop)
         for_each_candidate_runs<U, std::is_same<P, OneScene>::value>(
             cell, G, C, [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); },
-            [&](uint32_t q, uint32_t L) { term(ld_step<kPersist>(xin + q), L); });
+            [&](uint32_t q, uint32_t L) { term(ld_step<kPersist>(xin + q), Many{L}); });
     if (G.bg.spos) {
         // Two-way coupling (no counterpart in the reference): after the fluid
         // terms, the boundary's Akinci density rho0 psi_b W and its gradient
@@ -1401,7 +1408,7 @@ __device__ __forceinline__ void delta_at(uint32_t p, bool active, const float4* 
     if (walk && !coop)
         for_each_candidate_runs<U, std::is_same<P, OneScene>::value>(
             cell, G, C, [&](uint32_t q) { term(ld_step<kPersist>(xin + q), One{}); },
-            [&](uint32_t q, uint32_t L) { term(ld_step<kPersist>(xin + q), L); });
+            [&](uint32_t q, uint32_t L) { term(ld_step<kPersist>(xin + q), Many{L}); });
     if (G.bg.spos && xi.w != 0.0f) {
         // Two-way coupling: the boundary's share of the position correction,
         // lambda_i (rho0 psi_b) grad W, after the fluid terms (zero when
