@@ -1226,6 +1226,8 @@ __device__ __forceinline__ void density_lambda_at(uint32_t p, bool active, const
                 dfirst = ran > 0 && 3u * need < ran;
             }
             auto once = [&](const float4& xj, const float4&) { term(xj, One{}); };
+            // (The walk is compiled without runs here, kRuns false, so `times`
+            // is never called; it states what a run would add.)
             auto times = [&](const float4& xj, const float4&, uint32_t L) { term(xj, L); };
             if (!dfirst) {
                 coop_walk<CH, false, kPersist, false, false>(sm, R, cell.x, xi, xin, C.cut, C.grid, G.off,
