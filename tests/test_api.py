@@ -91,6 +91,10 @@ def test_settings_defaults_and_mass():
     npt.assert_allclose(s.kernel_radius, 0.1, atol=1e-6)
     assert s.solver_iterations == 4 and s.corr_n == 4 and not s.use_domain_bounds
     assert s.exact_arithmetic and s.hash_compat
+    # Extensions with no counterpart in the reference are off by default.
+    assert not s.boundary_two_way and s.boundary_friction == 0.0
+    s.boundary_friction = 0.25
+    npt.assert_allclose(s.boundary_friction, 0.25)
     npt.assert_allclose(s.particle_mass(0.05), 0.125, rtol=1e-5)
 
 

@@ -24,6 +24,8 @@ def test_version_and_defaults(capi):
     assert s.corr_n == 4 and s.use_domain_bounds == 0
     assert list(s.domain_lower) == [-10.0, 0.0, -10.0]
     assert s.hash_compat == 1 and s.exact_arithmetic == 1
+    # extensions without a counterpart in the reference: off
+    assert s.boundary_two_way == 0 and s.boundary_friction == 0.0
 
 
 def test_settings_layout_matches_oracle():
