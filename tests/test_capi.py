@@ -42,6 +42,8 @@ def test_invalid_arguments_are_rejected(capi):
     assert lib.pbf_default_settings(None) == capi.PBF_ERR_INVALID_ARG
     assert b"NULL" in lib.pbf_last_error()
     assert lib.pbf_scene_step(None, ctypes.c_float(0.01), 1) == capi.PBF_ERR_INVALID_ARG
+    assert lib.pbf_scene_set_bodies(None, 0, None, None, None) == capi.PBF_ERR_INVALID_ARG
+    assert lib.pbf_scene_set_body_velocities(None, 0, None, None) == capi.PBF_ERR_INVALID_ARG
     bad = capi.default_settings(kernel_radius=0.0)
     out = ctypes.c_void_p()
     rc = lib.pbf_scene_create(0, ctypes.byref(bad), 0, None, None, 1.0, ctypes.byref(out))
